@@ -1,0 +1,324 @@
+"""Batched implicit-step throughput: scene-steps/s of the PNCG step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--scenes 4096] [--precision mixed|fp64]
+
+Workload: the batching configuration — 4096 independent soft rectangles on the ground
+(H ~ U{4..16}, W ~ U{32..128} pixels of 0.75 mm, per-pixel E log-uniform in [0.1, 2] MPa,
+nu 0.40, density 1100, ground mu ~ U[0.3, 0.9] per scene, top-edge pressure ~ U[0, 5] kPa,
+dt 2 ms, relative gradient-norm tolerance 1e-6), seeded synthetic inputs. One step = one
+implicit step of every scene. The headline arm is the mixed-precision path; the plain FP64
+path is timed on the same batch and reported beside it, with the position error between
+the two after the timed steps.
+
+`value` times K steps with the state resident in HBM (CUDA events on the launching
+stream); `e2e` times the same steps through the public API (ImplicitIntegrator.simulate)
+with the step's nodal loads uploaded from pinned host memory and the node positions read
+back every step. `--impl reference` times the reference algorithm's CPU implementation:
+the reference itself needs NVIDIA Warp, which is not installable here, so its serial FP64
+restatement (oracle/) runs on the host cores, one thread per scene sample.
+Multi-GPU (torchrun): replicas only — each rank advances its own batch, no exchange.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": HBM_FALLBACK_GBS, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu, self.rows, self.stop = gpu, [], threading.Event()
+
+    def _run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([c.strip() for c in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v.strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def algorithmic_bytes(prob, iters, mixed):
+    """Compulsory bytes of one step at the iteration counts run: per iteration,
+    136 T + 216 N + 88 Nb bytes (FP64) or 80 T + 144 N + 72 Nb (mixed) per scene."""
+    B = int(prob["B"])
+    n = np.bincount(np.asarray(prob["node2env"]), minlength=B)
+    t = np.bincount(np.asarray(prob["tri2env"]), minlength=B)
+    b = np.bincount(np.asarray(prob["b2e"]), minlength=B)
+    per = (80 * t + 144 * n + 72 * b) if mixed else (136 * t + 216 * n + 88 * b)
+    return float((np.asarray(iters, np.float64) * per).sum())
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_sample(prob, state_x, state_v, n_threads, per_thread, seed=1):
+    """The serial FP64 oracle on a bounded sample: n_threads threads, each advancing its own
+    subset of `per_thread` scenes by one step from the given state. Returns
+    (scene-steps/s over all threads, sample description)."""
+    import oracle
+    from diff_2d_fem_gb300.scene import subset_problem
+    rng = np.random.default_rng(seed)
+    B = int(prob["B"])
+    picks = rng.choice(B, size=min(B, n_threads * per_thread), replace=False)
+    groups = [np.sort(picks[i::n_threads]) for i in range(n_threads)]
+    full = dict(prob)
+    if state_x is not None:
+        full["x"], full["v"] = state_x, state_v
+    solvers = [oracle.OracleSolver(subset_problem(full, g)) for g in groups if len(g)]
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=s.step) for s in solvers]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    dt = time.perf_counter() - t0
+    n = sum(len(g) for g in groups)
+    return n / dt, f"{n} of {B} scenes x 1 step, {len(solvers)} threads x {per_thread} scenes, {dt:.1f} s"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from diff_2d_fem_gb300 import workloads, scene, ImplicitIntegrator
+    m, kw, dt = workloads.rectangles_on_ground(args.scenes, seed=0)
+    prob = scene.solver_problem(m, ImplicitIntegrator(**kw), dt)
+    threads = min(os.cpu_count() or 1, 64)
+    vals = []
+    desc = ""
+    for k in range(args.warmup + args.steps):
+        v, desc = cpu_sample(prob, None, None, threads, 2, seed=k)
+        if k >= args.warmup:
+            vals.append(v)
+    val = float(np.mean(vals))
+    print(json.dumps({
+        "metric": "batched scene-steps/s (implicit PNCG step)", "value": val, "unit": "scene-steps/s",
+        "impl": "reference", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "config": {"workload": f"rectangles_on_ground x{args.scenes}", "dt": dt},
+        "cpu_baseline": {"value": val, "unit": "scene-steps/s", "cores": threads, "kind": "port",
+                         "sample": desc + "; reference CPU path unavailable (warp-lang not installed), "
+                                          "timing its serial C restatement"},
+        "e2e": {"value": val, "unit": "scene-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_ours(args, rank, world):
+    import torch
+    from diff_2d_fem_gb300 import workloads, scene, ImplicitIntegrator
+    from diff_2d_fem_gb300.device import DeviceSolver
+
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        local = int(os.environ.get("LOCAL_RANK", rank))
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    m, kw, dt = workloads.rectangles_on_ground(args.scenes, seed=rank)
+    integ = ImplicitIntegrator(precision=args.precision, **kw)
+    prob = scene.solver_problem(m, integ, dt)
+    prob["rest"] = np.asarray(m.me.rest_pos, np.float64)
+    mixed = args.precision == "mixed"
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist:
+            tdist.barrier()
+
+    def maxr(v):
+        if not dist:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(solver, K, W):
+        for _ in range(W):
+            solver.step()
+        barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(K):
+            solver.step()
+        ev1.record(stream)
+        barrier()
+        ms = ev0.elapsed_time(ev1)
+        it, ac, st = solver.stats()
+        return ms, it, st
+
+    # ---- headline arm (device-resident)
+    sol = DeviceSolver(prob, precision=args.precision, threads=args.threads, blocks_per_sm=args.bps)
+    with Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if rank == 0 else 0) as clk:
+        ms, it_last, st = timed(sol, args.steps, args.warmup)
+    ms = maxr(ms)
+    n_sc = prob["B"]
+    value = n_sc * args.steps * world / (ms / 1e3)
+    x_head = sol.get_x()
+    bytes_last = algorithmic_bytes(prob, it_last, mixed)
+
+    # per-launch time of the step kernel, on the launching stream (one launch = one step)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sol.step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    launch_ms = e0.elapsed_time(e1)
+    it_l, _, _ = sol.stats()
+    launch_bytes = algorithmic_bytes(prob, it_l, mixed)
+    sol.close()
+    del sol
+    torch.cuda.empty_cache()
+
+    # ---- the other precision on the same batch, same steps, for the ratio and the error
+    other = "fp64" if mixed else "mixed"
+    sol2 = DeviceSolver(prob, precision=other, threads=args.threads, blocks_per_sm=args.bps)
+    ms2, it2, st2 = timed(sol2, args.steps, args.warmup)
+    ms2 = maxr(ms2)
+    value2 = n_sc * args.steps * world / (ms2 / 1e3)
+    x2 = sol2.get_x()
+    sol2.close()
+    del sol2
+    torch.cuda.empty_cache()
+    x64, xmx = (x2, x_head) if mixed else (x_head, x2)
+    disp = np.abs(x64 - prob["x"]).max()
+    pos_err_rel = float(np.abs(xmx - x64).max() / np.abs(x64).max())
+    pos_err_disp = float(np.abs(xmx - x64).max() / max(disp, 1e-300))
+
+    # ---- end to end through the public API: loads up (pinned), simulate, positions down
+    fext = prob["fext"]
+    f_pin = torch.from_numpy(np.ascontiguousarray(fext)).pin_memory()
+    x_pin = torch.empty((prob["x"].shape[0], 2), dtype=torch.float64).pin_memory()
+    m._solver = None
+    integ.simulate(m, dt)                                   # build
+    s = m._solver
+    for _ in range(args.warmup):
+        integ.simulate(m, dt)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.tensor("fext").copy_(f_pin, non_blocking=True)   # the step's loads
+        integ.simulate(m, dt)
+        x_pin.copy_(s.x, non_blocking=True)                 # the step's result
+        torch.cuda.current_stream(dev).synchronize()
+    barrier()
+    e2e_s = maxr(time.perf_counter() - t0)
+    e2e = n_sc * args.steps * world / e2e_s
+    h2d = int(f_pin.numel() * 8)
+    d2h = int(x_pin.numel() * 8)
+    x_e2e = x_pin.numpy().copy()
+    m._solver.close()
+
+    if rank != 0:
+        if dist:
+            tdist.destroy_process_group()
+        return
+
+    # ---- CPU baseline: the oracle on a bounded sample, from the benchmarked state
+    threads = min(os.cpu_count() or 1, 16)
+    cpu_val, cpu_desc = cpu_sample(prob, None, None, threads, 4)
+    cpu_desc += " (first step from rest)"
+
+    peaks, src = _peaks()
+    hbm = float(peaks.get("hbm_gbs", HBM_FALLBACK_GBS))
+    achieved = launch_bytes / (launch_ms / 1e3) / 1e9
+    rec = {
+        "metric": "batched scene-steps/s (implicit PNCG step)",
+        "value": value, "unit": "scene-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "mixed-f32/f64" if mixed else "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"rectangles_on_ground x{n_sc} (H~U{{4..16}}, W~U{{32..128}}, 0.75 mm px, "
+                               f"E log-U[0.1,2] MPa, mu~U[0.3,0.9], p~U[0,5] kPa)",
+                   "dt": dt, "gtol": kw.get("gtol"), "iter_max": int(prob["iter_max"]),
+                   "nodes": int(prob["x"].shape[0]), "triangles": int(len(prob["tri"])),
+                   "l2": "inputs larger than L2 (per-step working set several GB)",
+                   "precision": args.precision, "parallelism": f"replicas x{world}"},
+        "precision_compare": {"other": other, "other_value": value2,
+                              "speedup_vs_other": value / value2 if value2 else None,
+                              "pos_err_rel_to_coords": pos_err_rel, "pos_err_rel_to_displacement": pos_err_disp},
+        "iters_mean": float(np.mean(it_last)), "iters_max": int(np.max(it_last)),
+        "status_ok": bool((st == 0).all()),
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e, "unit": "scene-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                     "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": launch_ms},
+        "cpu_baseline": {"value": cpu_val, "unit": "scene-steps/s", "cores": threads, "kind": "port",
+                         "sample": cpu_desc},
+    }
+    print(json.dumps(rec))
+    if dist:
+        tdist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scenes", type=int, default=4096)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--bps", type=int, default=0)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

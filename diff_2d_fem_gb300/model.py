@@ -1,0 +1,503 @@
+"""Model — the scene container, with the reference's API (sim_model.py).
+
+    model = Model()
+    model.add_ground(0.0, mu=0.8)
+    h = model.add_soft_body(mask, physical_size=(0.054, 0.0045), center=(0.0, 0.003),
+                            E=0.5e6, nu=0.40, density=1100.0)
+    model.finalize()
+    model.gravity = (0.0, -9.81)
+    integ = ImplicitIntegrator()
+    for t in range(T):
+        integ.simulate(model, 2e-3)
+
+Bodies are pixel masks (row 0 at the bottom) rasterised into P1 triangles; every body
+lives in an environment (`env_id`), environments never interact and are solved together.
+The host side here only assembles arrays; the step itself runs on the GPU (integrator.py).
+New, keyword-only, beyond the reference: a per-environment collider friction
+(`set_collider_mu`), which the reference cannot express (its colliders carry one mu for
+every environment, implicit/solver.py:235-242).
+"""
+from __future__ import annotations
+
+import warnings
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import mesh as _mesh
+
+DISC, ELLIPSE, BOX, TRIANGLE, HALFSPACE = 0, 1, 2, 3, 4
+NAMES = {"disc": DISC, "ellipse": ELLIPSE, "box": BOX, "square": BOX, "triangle": TRIANGLE}
+
+
+@dataclass
+class SimConfig:
+    """Material defaults, damping and contact parameters (reference core/config.py:13-29)."""
+    young: float = 1.0e6
+    nu: float = 0.40
+    rho_mass: float = 1000.0
+    damping: float = 0.0
+    ipc_d_hat: Optional[float] = None
+    obstacle_stiffness: Optional[float] = None
+    contact_stiffness: Optional[float] = None
+    obstacle_friction: float = 0.5
+    obstacle_friction_epsv: float = 1.0e-3
+
+
+class Model:
+    def __init__(self, device="cuda", config=None):
+        self.cfg = SimConfig() if config is None else config
+        self.device = device
+        self._colliders = []
+        self._col_mu_env = {}
+        self._bodies = []
+        self._constrained = {}
+        self.me = None
+        self._solver = None
+        self._targets = None
+        self._node_range, self._tri_range = [], []
+        self._v0 = None
+        self._x_host = None
+        self._epoch = 0
+        self.time = 0.0
+        self._gravity = (0.0, 0.0)
+        self._fext = None
+        self._tendons = []
+        self._affine = []
+        self._affine_of = {}
+        self._extra_excl = []
+        self.body_contact = "ipc"
+        self.body_friction = 0.0
+        self.body_kappa = None
+        self.rigid_young = 1.0e9
+        self.rigid_nu = 0.30
+        self._act_version = 0
+        self._ctrl_version = 0
+
+    # ---- contact / material attributes over the config (sim_model.py:118-127)
+    def _p(name):
+        return property(lambda s: getattr(s.cfg, name), lambda s, v: setattr(s.cfg, name, v))
+    dhat = _p("ipc_d_hat")
+    kappa = _p("obstacle_stiffness")
+    self_stiffness = _p("contact_stiffness")
+    mu = _p("obstacle_friction")
+    epsv = _p("obstacle_friction_epsv")
+    damping = _p("damping")
+    del _p
+
+    # ---- colliders (sim_model.py:133-184)
+    def add_disc(self, center, radius, mu=None):
+        return self.add_object("disc", center, radius, mu=mu)
+
+    def add_plane(self, normal, origin, mu=None):
+        n = np.asarray(normal, np.float64)
+        if not np.linalg.norm(n) > 0:
+            raise ValueError("the plane normal must be non-zero")
+        n = n / np.linalg.norm(n)
+        return self._set_collider(HALFSPACE, origin, float(n[0]), float(n[1]), 0.0, mu)
+
+    def add_ground(self, height=0.0, mu=None):
+        return self.add_plane((0.0, 1.0), (0.0, height), mu=mu)
+
+    def add_object(self, kind, center, rx, ry=None, corner_radius=3.0e-3, mu=None):
+        k = NAMES[kind] if isinstance(kind, str) else int(kind)
+        rx = float(rx)
+        ry = rx if ry is None else float(ry)
+        rref = float(corner_radius) if k in (BOX, TRIANGLE) else rx
+        return self._set_collider(k, center, rx, ry, rref, mu)
+
+    def _set_collider(self, kind, center, rx, ry, rref, mu):
+        if self._solver is not None:
+            raise RuntimeError("add colliders before the first simulate()")
+        mu = float(self.cfg.obstacle_friction if mu is None else mu)
+        self._colliders.append(dict(kind=int(kind), cx=float(center[0]), cy=float(center[1]),
+                                    rx=rx, ry=ry, rref=rref, r=rx, mu=mu))
+        return len(self._colliders) - 1
+
+    def set_collider_mu(self, index, mu_per_env):
+        """Per-environment Coulomb coefficient of collider `index` ((n_envs,) array). New
+        in this implementation: the reference has one mu per collider for every
+        environment."""
+        if self._solver is not None:
+            raise RuntimeError("set per-environment friction before the first simulate()")
+        self._col_mu_env[int(index)] = np.asarray(mu_per_env, np.float64).copy()
+
+    # ---- bodies (sim_model.py:199-264)
+    def add_soft_body(self, mask, physical_size, center, E=None, nu=None, density=None, env_id=0, mu=None):
+        if self.me is not None:
+            raise RuntimeError("add bodies before finalize()")
+        mask = (np.asarray(mask) > 0.5).astype(np.uint8)
+        if mask.ndim != 2 or not mask.any():
+            raise ValueError("the mask must be a 2-D array with at least one solid pixel")
+        if E is not None and not np.isscalar(E):
+            E = np.asarray(E, np.float64)
+            if E.shape != mask.shape:
+                raise ValueError(f"stiffness map is {E.shape}, the mask is {mask.shape}")
+            if (E[mask > 0] <= 0).any():
+                raise ValueError("stiffness map must be positive wherever the mask is solid")
+        if int(env_id) < 0:
+            raise ValueError("env_id must be >= 0")
+        if mu is not None:
+            mu = float(mu)
+            if not (np.isfinite(mu) and mu >= 0.0):
+                raise ValueError(f"mu must be a finite number >= 0, not {mu}")
+        c = self.cfg
+        self._bodies.append(dict(mask=mask, size=tuple(float(v) for v in physical_size),
+                                 center=tuple(float(v) for v in center),
+                                 E=(c.young if E is None else (float(E) if np.isscalar(E) else E)),
+                                 nu=float(c.nu if nu is None else nu),
+                                 rho=float(c.rho_mass if density is None else density),
+                                 env=int(env_id), mu=mu))
+        return len(self._bodies) - 1
+
+    def add_affine_body(self, mask, physical_size, center, density=None, env_id=0, E=None, nu=None, mu=None):
+        h = self.add_soft_body(mask, physical_size, center, E=(self.rigid_young if E is None else E),
+                               nu=(self.rigid_nu if nu is None else nu), density=density,
+                               env_id=env_id, mu=mu)
+        if not np.isscalar(self._bodies[h]["E"]):
+            raise ValueError("a rigid body takes a scalar stiffness")
+        self._bodies[h]["affine"] = True
+        return h
+
+    def add_kinematic_body(self, mask, physical_size, center, env_id=0, mu=None):
+        h = self.add_soft_body(mask, physical_size, center, env_id=env_id, mu=mu)
+        self._bodies[h]["kinematic"] = True
+        return h
+
+    # ---- build (sim_model.py:391-429)
+    def finalize(self):
+        if not self._bodies:
+            raise ValueError("add at least one soft body before finalize()")
+        B = self._bodies
+        self.me = _mesh.build_scene([dict(mask_xy=b["mask"].T.copy(), size=b["size"], center=b["center"],
+                                          young=(b["E"] if np.isscalar(b["E"]) else 1.0), nu=b["nu"],
+                                          rho=b["rho"], env=b["env"]) for b in B])
+        me = self.me
+        self._node_range = [np.arange(*me.body_node_range[h]) for h in range(len(B))]
+        self._tri_range = [np.arange(*me.body_tri_range[h]) for h in range(len(B))]
+        for h, b in enumerate(B):
+            if np.isscalar(b["E"]):
+                continue
+            tris = self._tri_range[h]
+            scale = self._pixel_field(h, b["E"])
+            me.mu[tris] = me.mu[tris] * scale
+            me.lam[tris] = me.lam[tris] * scale
+        self._check_layout()
+        self._scale_contact()
+        self._targets = me.rest_pos.astype(np.float64).copy()
+        self._x_host = me.rest_pos.astype(np.float64).copy()
+        self._v0 = np.zeros_like(self._x_host)
+        for h, b in enumerate(B):
+            if b.get("affine"):
+                self._add_affine(h, self._tri_range[h])
+            if b.get("kinematic"):
+                self._constrained[h] = self._node_range[h].copy()
+        return self
+
+    def _pixel_field(self, h, field):
+        q = np.asarray(self.me.tri_quad)[self._tri_range[h]]
+        ny = self._bodies[h]["mask"].shape[0]
+        return np.asarray(field, np.float64)[q % ny, q // ny]
+
+    def _add_affine(self, handle, elems):
+        me = self.me
+        mine = self._affine_of.setdefault(handle, [])
+        if mine and np.intersect1d(elems, np.concatenate(mine)).size:
+            raise ValueError("rigid regions must not overlap")
+        mine.append(np.asarray(elems, np.int64))
+        nodes = np.unique(np.asarray(me.tri)[elems].reshape(-1))
+        # the boundary nodes of one rigid piece never move relative to each other: exclude
+        # every pair of them from contact (sim_model.py:466-476)
+        env = self._bodies[handle]["env"]
+        lo, hi = int(me.boundary_starts[env]), int(me.boundary_starts[env + 1])
+        loc = np.nonzero(np.isin(me.boundary_nodes[lo:hi], nodes))[0]
+        self._extra_excl.append((lo, loc))
+        self._affine.append(dict(body=handle, elems=np.asarray(elems, np.int64), nodes=nodes))
+        return len(self._affine) - 1
+
+    def exclusion_csr(self):
+        """The scene's self-contact exclusion (mesh hops + rigid pieces) as a CSR over the
+        boundary slots, columns environment-local and sorted."""
+        me = self.me
+        ptr, idx = me.excl_ptr, me.excl_idx
+        if not self._extra_excl:
+            return ptr, idx
+        rows = [set(idx[ptr[s]:ptr[s + 1]].tolist()) for s in range(len(ptr) - 1)]
+        for lo, loc in self._extra_excl:
+            for a in loc:
+                rows[lo + a].update(int(v) for v in loc)
+        new_ptr = np.zeros(len(rows) + 1, np.int64)
+        new_ptr[1:] = np.cumsum([len(r) for r in rows])
+        new_idx = np.concatenate([np.sort(np.fromiter(r, np.int64)) for r in rows]) if rows else np.zeros(0, np.int64)
+        return new_ptr, new_idx
+
+    def _scale_contact(self):
+        """Contact parameters left unset, from the scene's own scales (sim_model.py:487-497)."""
+        c = self.cfg
+        soft = [b for b in self._bodies if not b.get("affine") and not b.get("kinematic")]
+        E = min((float(b["E"]) if np.isscalar(b["E"]) else float(b["E"][b["mask"] > 0].min())
+                 for b in soft), default=1.0e6)
+        if c.ipc_d_hat is None:
+            c.ipc_d_hat = self.dx / 8.0
+        if c.obstacle_stiffness is None:
+            c.obstacle_stiffness = 4.0e-3 * E * self.dx / c.ipc_d_hat
+        if c.contact_stiffness is None:
+            c.contact_stiffness = 0.2 * E
+        if self.body_kappa is None:
+            self.body_kappa = 0.1 * E * self.dx / c.ipc_d_hat
+
+    def _check_layout(self):
+        """Bodies of one environment must not start inside one another (sim_model.py:499-535)."""
+        envs = {}
+        for h, b in enumerate(self._bodies):
+            envs.setdefault(b["env"], []).append(h)
+        for env, hs in envs.items():
+            for i, a in enumerate(hs):
+                for c in hs[i + 1:]:
+                    if self._overlap(a, c) or self._overlap(c, a):
+                        raise ValueError(
+                            f"bodies {a} and {c} overlap in environment {env}. Bodies of one "
+                            f"environment collide with each other and must start apart; give "
+                            f"the members of a batch their own environment with env_id=i.")
+            px = [self.pixel_size(h)[0] for h in hs]
+            if max(px) > 1.25 * min(px):
+                warnings.warn(f"environment {env} mixes pixel sizes from {min(px) * 1e3:.3g} to "
+                              f"{max(px) * 1e3:.3g} mm. Contact between bodies has ONE thickness, "
+                              f"set by the largest. Prefer one pixel size per scene.", stacklevel=3)
+
+    def _overlap(self, a, c):
+        A, C = self._bodies[a], self._bodies[c]
+        (aw, ah), (ax, ay) = A["size"], A["center"]
+        (cw, ch), (cx, cy) = C["size"], C["center"]
+        if abs(ax - cx) >= 0.5 * (aw + cw) or abs(ay - cy) >= 0.5 * (ah + ch):
+            return False
+        H, W = A["mask"].shape
+        row, col = np.nonzero(A["mask"])
+        px = ax - 0.5 * aw + (col + 0.5) * aw / W
+        py = ay - 0.5 * ah + (row + 0.5) * ah / H
+        Hc, Wc = C["mask"].shape
+        jc = np.floor((px - (cx - 0.5 * cw)) / (cw / Wc)).astype(int)
+        jr = np.floor((py - (cy - 0.5 * ch)) / (ch / Hc)).astype(int)
+        ok = (jc >= 0) & (jc < Wc) & (jr >= 0) & (jr < Hc)
+        return bool(C["mask"][jr[ok], jc[ok]].any())
+
+    # ---- layout queries (sim_model.py:572-700)
+    @property
+    def n_bodies(self):
+        return len(self._bodies)
+
+    @property
+    def n_envs(self):
+        return int(self.me.n_envs) if self.me is not None else \
+            (max(b["env"] for b in self._bodies) + 1 if self._bodies else 0)
+
+    @property
+    def n_nodes(self):
+        return int(self.me.rest_pos.shape[0])
+
+    @property
+    def n_elements(self):
+        return int(self.me.tri.shape[0])
+
+    def body_env(self, handle):
+        return self._bodies[handle]["env"]
+
+    def body_nodes(self, handle):
+        return self._node_range[handle].copy()
+
+    def body_elements(self, handle):
+        return self._tri_range[handle].copy()
+
+    def pixel_size(self, handle):
+        b = self._bodies[handle]
+        H, W = b["mask"].shape
+        return b["size"][0] / W, b["size"][1] / H
+
+    def element_size(self, handle):
+        return self.pixel_size(handle)[0]
+
+    def _cfl_length(self, handle):
+        return min(self.pixel_size(handle))
+
+    @property
+    def dx(self):
+        """Element size [m]: the largest pixel width over the bodies."""
+        return max(self.element_size(h) for h in range(len(self._bodies)))
+
+    def element_areas(self, handle):
+        return np.asarray(self.me.rest_area, np.float64)[self._tri_range[handle]].copy()
+
+    def rest_x(self, handle):
+        return self.me.rest_pos[self._node_range[handle]].copy()
+
+    def to_elements(self, handle, field):
+        b = self._bodies[handle]
+        field = np.asarray(field, np.float64)
+        if field.shape != b["mask"].shape:
+            raise ValueError(f"field is {field.shape}, the mask is {b['mask'].shape}")
+        return self._pixel_field(handle, field)
+
+    def to_pixels(self, handle, values):
+        H, W = self._bodies[handle]["mask"].shape
+        q = np.asarray(self.me.tri_quad)[self._tri_range[handle]]
+        out = np.zeros((H, W))
+        np.add.at(out, (q % H, q // H), np.asarray(values, np.float64))
+        return out
+
+    def rigid_motion(self, handle, translation=(0.0, 0.0), angle=0.0, about=None):
+        x = self.rest_x(handle)
+        c = np.asarray(self._bodies[handle]["center"] if about is None else about, np.float64)
+        ca, sa = np.cos(angle), np.sin(angle)
+        R = np.array([[ca, -sa], [sa, ca]])
+        return (x - c) @ R.T + c + np.asarray(translation, np.float64)
+
+    # ---- kinematic boundary conditions (sim_model.py:384-388, 686-692)
+    def set_kinematic_constraint(self, handle, node_indices):
+        self._constrained[handle] = self._node_range[handle][np.asarray(node_indices, int)]
+
+    def set_kinematic_target(self, handle, targets):
+        self._targets[self._node_range[handle]] = np.asarray(targets, np.float64)
+
+    def set_kinematic_pose(self, handle, translation=(0.0, 0.0), angle=0.0, about=None):
+        self.set_kinematic_target(handle, self.rigid_motion(handle, translation, angle, about))
+
+    def all_constrained(self):
+        if not self._constrained:
+            return np.zeros(0, np.int64)
+        return np.unique(np.concatenate([np.asarray(v, np.int64) for v in self._constrained.values()]))
+
+    # ---- state I/O (sim_model.py:694-796)
+    def get_x(self):
+        if self._solver is not None:
+            self._x_host = self._solver.get_x()
+        return self._x_host.copy()
+
+    def get_body_x(self, handle):
+        return self.get_x()[self._node_range[handle]]
+
+    def get_body_v(self, handle):
+        v = self._v0 if self._solver is None else self._solver.get_v()
+        return np.asarray(v)[self._node_range[handle]].copy()
+
+    def set_body_velocity(self, handle, velocity=(0.0, 0.0), omega=0.0, about=None):
+        nodes = self._node_range[handle]
+        x = self.get_x()[nodes].astype(np.float64)
+        c = np.asarray(about, np.float64) if about is not None else x.mean(0)
+        r = x - c
+        v = np.asarray(velocity, np.float64)[None, :] + omega * np.stack([-r[:, 1], r[:, 0]], 1)
+        self._v0[nodes] = v
+        if self._solver is not None:
+            self._solver.set_nodes(nodes, v=v)
+
+    def set_body_x(self, handle, x, v=None):
+        nodes = self._node_range[handle]
+        x = np.asarray(x, np.float64).reshape(len(nodes), 2)
+        self._x_host[nodes] = x
+        self._targets[nodes] = x
+        if v is not None:
+            self._v0[nodes] = np.asarray(v, np.float64).reshape(len(nodes), 2)
+        if self._solver is not None:
+            self._solver.set_nodes(nodes, x=x, v=None if v is None else self._v0[nodes], xn=True)
+            self._solver.sync_affine([i for i, a in enumerate(self._affine) if a["body"] == handle])
+
+    def set_body_pose(self, handle, translation=(0.0, 0.0), angle=0.0, about=None, velocity=(0.0, 0.0), omega=0.0):
+        self.set_body_x(handle, self.rigid_motion(handle, translation, angle, about))
+        self.set_body_velocity(handle, velocity, omega)
+
+    def reset(self, env_ids=None):
+        """Back to rest at zero velocity, kinematic targets included (sim_model.py:761-796)."""
+        rest = self.me.rest_pos.astype(np.float64)
+        s = self._solver
+        if env_ids is None:
+            self._targets = rest.copy()
+            self._x_host = rest.copy()
+            self._v0 = np.zeros_like(rest)
+            self._epoch += 1
+            self.time = 0.0
+            if s is not None:
+                s.reset_envs(None)
+            return
+        pick = np.zeros(self.n_envs, np.int32)
+        pick[np.atleast_1d(env_ids)] = 1
+        nodes = pick[np.asarray(self.me.node2env)] != 0
+        self._targets[nodes] = rest[nodes]
+        self._x_host[nodes] = rest[nodes]
+        self._v0[nodes] = 0.0
+        self._epoch += 1
+        if s is not None:
+            s.reset_envs(pick)
+
+    # ---- actuation (sim_model.py:806-967)
+    def _need_mesh(self):
+        if self.me is None:
+            raise RuntimeError("call finalize() before adding actuators")
+
+    @property
+    def gravity(self):
+        return self._gravity
+
+    @gravity.setter
+    def gravity(self, g):
+        self._gravity = (float(g[0]), float(g[1]))
+        self._ctrl_version += 1
+
+    def set_external_force(self, handle, force):
+        """Nodal forces on a body, (n_body_nodes, 2) [N/m], held until changed."""
+        self._need_mesh()
+        if self._fext is None:
+            self._fext = np.zeros((self.me.rest_pos.shape[0], 2), np.float64)
+        self._fext[self._node_range[handle]] = np.asarray(force, np.float64)
+        self._ctrl_version += 1
+
+    def add_tendon(self, handle, through=None, nodes=None, stiffness=None):
+        """Thread a cable through a body (sim_model.py:931-958). Returns a handle."""
+        self._need_mesh()
+        ids = self._node_range[handle]
+        if (through is None) == (nodes is None):
+            raise ValueError("give exactly one of `through` (points) or `nodes` (indices)")
+        if nodes is not None:
+            path = ids[np.asarray(nodes, int)]
+        else:
+            pts = np.atleast_2d(np.asarray(through, np.float64))
+            pos = self.me.rest_pos[ids]
+            dd = np.linalg.norm(pos[None, :, :] - pts[:, None, :], axis=2)
+            path = np.asarray(ids)[dd.argmin(1)]
+            keep = np.concatenate([[True], path[1:] != path[:-1]])
+            path = path[keep]
+        if len(path) < 2:
+            raise ValueError("a tendon needs at least two distinct eyelets")
+        if stiffness is not None and stiffness <= 0:
+            raise ValueError("stiffness must be positive (or None for a tension-controlled cable)")
+        xs = self.me.rest_pos[np.asarray(path)]
+        length = float(np.linalg.norm(np.diff(xs, axis=0), axis=1).sum())
+        self._tendons.append(dict(body=handle, nodes=np.asarray(path, np.int64),
+                                  stiffness=0.0 if stiffness is None else float(stiffness),
+                                  tension=0.0, length=length))
+        self._act_version += 1
+        return len(self._tendons) - 1
+
+    def set_tendon_tension(self, tendon, tension):
+        t = self._tendons[tendon]
+        if t["stiffness"] > 0:
+            raise ValueError("this tendon is length-controlled; use set_tendon_length")
+        t["tension"] = float(tension)
+        self._ctrl_version += 1
+
+    def set_tendon_length(self, tendon, length):
+        t = self._tendons[tendon]
+        if t["stiffness"] <= 0:
+            raise ValueError("this tendon is tension-controlled; use set_tendon_tension")
+        t["length"] = float(length)
+        self._ctrl_version += 1
+
+    def affine_state(self, index):
+        s = self._solver
+        if s is None:
+            a = self._affine[index]
+            m = np.asarray(self.me.mass)[a["nodes"]]
+            c = (m[:, None] * self.me.rest_pos[a["nodes"]]).sum(0) / m.sum()
+            return dict(position=c, angle=0.0, A=np.eye(2))
+        q = s.get_affine_q()[index]
+        A = np.array([[q[1], q[2]], [q[4], q[5]]])
+        return dict(position=np.array([q[0], q[3]]), angle=float(np.arctan2(A[1, 0] - A[0, 1], A[0, 0] + A[1, 1])), A=A)

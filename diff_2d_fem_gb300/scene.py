@@ -1,0 +1,341 @@
+"""The solver problem of a finalized Model: every array the step needs, host side.
+
+This is the reference's ImplicitIntegrator._build (implicit/integrator.py:252-311) together
+with the constructors it calls — PNCG2DSolver.__init__ (implicit/solver.py:97-226),
+AffineBodies.__init__ (implicit/affine.py:282-328), IPCContact.__init__
+(implicit/ipc_contact.py:353-386), RigidModes.build (implicit/affine.py:503-523) and the
+actuation sync (implicit/integrator.py:151-229) — producing the same arrays in the same
+order. The result is a plain dict (the "problem"), consumed by the GPU solver
+(device.py); the test suite's oracle reads the same dict.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+from scipy.sparse import coo_matrix
+from scipy.sparse.csgraph import connected_components
+
+
+def iters_for(model, integ, dt):
+    """Iteration budget of a step (implicit/integrator.py:88-122): iters_per_cfl x the
+    acoustic CFL number of the stiffest soft body, clipped to [40 (120 with IPC contact
+    between bodies), max_iter_cap]. Batch-global, as in the reference."""
+    if integ.max_iter is not None:
+        return int(integ.max_iter)
+    me = model.me
+    mu, lam = np.asarray(me.mu, np.float64), np.asarray(me.lam, np.float64)
+    soft = np.ones(len(mu), bool)
+    for a in model._affine:
+        soft[a["elems"]] = False
+    C = 0.0
+    for h, b in enumerate(model._bodies):
+        el = model._tri_range[h]
+        el = el[soft[el]]
+        if len(el) and not b.get("kinematic"):
+            cp = np.sqrt((lam[el] + 2.0 * mu[el]).max() / b["rho"])
+            C = max(C, cp * dt / model._cfl_length(h))
+    n = int(np.ceil(integ.iters_per_cfl * C))
+    lo = 120 if integ.self_collision and model.body_contact == "ipc" else 40
+    return int(np.clip(n, lo, integ.max_iter_cap))
+
+
+def _affine_arrays(model, mu_s, lam_s, free, x):
+    """AffineBodies (implicit/affine.py:282-344): slaved node lists, the 6-DOF maps, the
+    region moduli summed over area; zeroes the regions' own elements in mu_s/lam_s and
+    returns q fitted to x (least squares), with x's slaved nodes moved to J q."""
+    me = model.me
+    tri = np.asarray(me.tri)
+    mass = np.asarray(me.mass, np.float64)
+    X = np.asarray(me.rest_pos, np.float64)
+    area = np.asarray(me.rest_area, np.float64)
+    node, grp, w, Mu, La, env = [], [], [], [], [], []
+    owner = np.full(X.shape[0], -1)
+    for b, g in enumerate(model._affine):
+        el = np.asarray(g["elems"], np.int64)
+        nd = np.unique(tri[el].reshape(-1))
+        if (owner[nd] >= 0).any():
+            raise ValueError("two rigid regions share a node; merge them or leave a gap of "
+                             "at least one soft element between them")
+        if (free[nd] == 0).any():
+            raise ValueError("a rigid region contains kinematically constrained nodes. A "
+                             "body whose motion is PRESCRIBED needs no rigid region")
+        owner[nd] = b
+        c = (mass[nd, None] * X[nd]).sum(0) / mass[nd].sum()
+        node += list(nd)
+        grp += [b] * len(nd)
+        w.append(np.c_[np.ones(len(nd)), X[nd] - c])
+        Mu.append(float((area[el] * np.asarray(me.mu, np.float64)[el]).sum()))
+        La.append(float((area[el] * np.asarray(me.lam, np.float64)[el]).sum()))
+        env.append(int(np.asarray(me.tri2env)[el[0]]))
+        mu_s[el] = 0.0
+        lam_s[el] = 0.0
+    w_np = np.concatenate(w, 0)
+    node = np.asarray(node, np.int64)
+    grp = np.asarray(grp, np.int64)
+    q = np.zeros((len(model._affine), 6))
+    first = np.concatenate([[0], np.cumsum([len(a) for a in w])])
+    for b in range(len(model._affine)):
+        k = slice(first[b], first[b + 1])
+        sol = np.linalg.lstsq(w_np[k], x[node[k]], rcond=None)[0]
+        q[b, :3], q[b, 3:] = sol[:, 0], sol[:, 1]
+    qg = q[grp]
+    x[node, 0] = w_np[:, 0] * qg[:, 0] + w_np[:, 1] * qg[:, 1] + w_np[:, 2] * qg[:, 2]
+    x[node, 1] = w_np[:, 0] * qg[:, 3] + w_np[:, 1] * qg[:, 4] + w_np[:, 2] * qg[:, 5]
+    return dict(node=node, grp=grp, env=np.asarray(env, np.int64), w=w_np,
+                Mu=np.asarray(Mu), La=np.asarray(La), q=q), owner >= 0
+
+
+def _rigid_arrays(model, free, skip_nodes):
+    """RigidModes.build (implicit/affine.py:503-523): one 3-mode coarse space per connected
+    piece of soft material with no kinematic node and no rigid region, of >= 3 nodes."""
+    me = model.me
+    N = me.rest_pos.shape[0]
+    tri = np.asarray(me.tri)
+    a = np.concatenate([tri[:, 0], tri[:, 1], tri[:, 2]])
+    b = np.concatenate([tri[:, 1], tri[:, 2], tri[:, 0]])
+    ncomp, lab = connected_components(coo_matrix((np.ones(len(a)), (a, b)), shape=(N, N)), directed=False)
+    held = np.zeros(ncomp, bool)
+    held[np.unique(lab[(free == 0).any(1)])] = True
+    if skip_nodes is not None and np.any(skip_nodes):
+        held[np.unique(lab[np.asarray(skip_nodes, bool)])] = True
+    size = np.bincount(lab, minlength=ncomp)
+    keep = np.where(~held & (size >= 3))[0]
+    if len(keep) == 0:
+        return None
+    newid = np.full(ncomp, -1)
+    newid[keep] = np.arange(len(keep))
+    nodes = np.where(newid[lab] >= 0)[0]
+    grp = newid[lab[nodes]]
+    first = np.zeros(len(keep), np.int64)
+    first[grp[::-1]] = nodes[::-1]
+    return dict(node=nodes.astype(np.int64), grp=grp.astype(np.int64),
+                env=np.asarray(me.node2env)[first].astype(np.int64))
+
+
+def _ipc_arrays(model, integ):
+    """IPCContact.__init__ (implicit/ipc_contact.py:353-386)."""
+    me = model.me
+    N = me.rest_pos.shape[0]
+    edges = np.asarray(me.boundary_edges, np.int64)
+    env = np.asarray(me.node2env)[edges[:, 0]]
+    bn = np.asarray(me.boundary_nodes)
+    pos = np.full(N, -1, np.int64)
+    pos[bn] = np.arange(len(bn)) - np.asarray(me.boundary_starts)[np.asarray(me.boundary2env)]
+    m = np.bincount(edges.reshape(-1), minlength=N).astype(np.float64)
+    share = (m - 1.0) / np.maximum(m, 1.0)
+    ptr, idx = model.exclusion_csr()
+    friction = integ.friction
+    mu_node = None
+    if friction and any(b.get("mu") is not None for b in model._bodies):
+        mu_node = np.zeros(N, np.float64)
+        for h, b in enumerate(model._bodies):
+            mu_node[model._node_range[h]] = model.body_friction if b.get("mu") is None else b["mu"]
+    return dict(ea=edges[:, 0], eb=edges[:, 1], ela=pos[edges[:, 0]], elb=pos[edges[:, 1]], e2env=env,
+                ca=share[edges[:, 0]], cb=share[edges[:, 1]],
+                bstart=np.asarray(me.boundary_starts[:-1], np.int64),
+                bpe=np.asarray(me.boundary_per_env, np.int64), excl_ptr=ptr, excl_idx=idx,
+                mu=(model.body_friction if friction else 0.0), per_body=0 if mu_node is None else 1,
+                mu_node=mu_node, dhat=float(model.dhat), kappa=float(model.body_kappa),
+                reach=max(2.0 * model.dx, 2.0 * model.dhat), gap=0.1, bc_floor=0.25)
+
+
+def _tendon_arrays(model):
+    node, prv, nxt, tid = [], [], [], []
+    for i, t in enumerate(model._tendons):
+        o, n = len(node), len(t["nodes"])
+        node += list(t["nodes"])
+        tid += [i] * n
+        prv += [-1] + list(range(o, o + n - 1))
+        nxt += list(range(o + 1, o + n)) + [-1]
+    T = model._tendons
+    return dict(node=np.asarray(node, np.int64), prv=np.asarray(prv, np.int64), nxt=np.asarray(nxt, np.int64),
+                tid=np.asarray(tid, np.int64), t2env=np.asarray([model.body_env(t["body"]) for t in T], np.int64),
+                stiff=np.asarray([t["stiffness"] for t in T], np.float64),
+                L0=np.asarray([t["length"] for t in T], np.float64),
+                Tcmd=np.asarray([t["tension"] for t in T], np.float64))
+
+
+def external_force(model):
+    """The ExternalForce field f = fext + m g (implicit/integrator.py:205-211), or None."""
+    g = model._gravity
+    if model._fext is None and g == (0.0, 0.0):
+        return None
+    f = np.zeros((model.n_nodes, 2)) if model._fext is None else model._fext.copy()
+    f += np.asarray(model.me.mass, np.float64)[:, None] * np.asarray(g, np.float64)[None, :]
+    return f
+
+
+def solver_problem(model, integ, dt):
+    """The problem dict of a finalized Model for a step of size dt."""
+    me = model.me
+    if me is None:
+        raise RuntimeError("call model.finalize() before simulating")
+    if model.body_contact not in ("ipc", "node"):
+        raise ValueError(f"model.body_contact must be 'ipc' or 'node', not {model.body_contact!r}")
+    if model.body_contact == "node" and integ.self_collision:
+        raise NotImplementedError("the 'node' penalty contact is not implemented; use body_contact='ipc'")
+    N = me.rest_pos.shape[0]
+    cfg = model.cfg
+    x = np.asarray(model._x_host, np.float64).copy()
+    v = np.asarray(model._v0, np.float64).copy() if model._v0 is not None else np.zeros_like(x)
+    bc = model.all_constrained()
+    free = np.ones((N, 2), np.float64)
+    free[bc] = 0.0
+    mu_s = np.asarray(me.mu, np.float64).copy()
+    lam_s = np.asarray(me.lam, np.float64).copy()
+    prob = dict(
+        B=int(me.n_envs), x=x, v=v, mass=np.asarray(me.mass, np.float64), free=free,
+        node2env=np.asarray(me.node2env, np.int64), tri=np.asarray(me.tri, np.int64),
+        Bm=np.asarray(me.D_m_inv, np.float64), area=np.asarray(me.rest_area, np.float64),
+        mu=mu_s, lam=lam_s, tri2env=np.asarray(me.tri2env, np.int64),
+        bnd=np.asarray(me.boundary_nodes, np.int64), b2e=np.asarray(me.boundary2env, np.int64),
+        bc_idx=np.asarray(bc, np.int64),
+        colliders=np.array([[c["kind"], c["cx"], c["cy"], c["rx"], c["ry"], c["rref"], c["r"], c["mu"]]
+                            for c in model._colliders], np.float64).reshape(-1, 8),
+        dt=float(dt), drag=math.exp(-float(dt) * cfg.damping), dhat=float(cfg.ipc_d_hat),
+        kappa=float(cfg.obstacle_stiffness), epsv=float(cfg.obstacle_friction_epsv), eps=integ.eps,
+        tol_x=integ.tol_x, near_factor=integ.near_factor, alpha_max=integ.alpha_max,
+        area_shrink=integ.area_shrink, ccd_eta=integ.ccd_eta, ls_tol=integ.ls_tol, gtol=integ.gtol,
+        iter_max=iters_for(model, integ, dt), conv_check=integ.conv_check, friction=int(integ.friction),
+        line_search=int(integ.line_search), n_bt=integ.n_backtrack)
+    if model._col_mu_env:
+        cm = np.repeat(prob["colliders"][None, :, 7], prob["B"], axis=0)
+        for k, arr in model._col_mu_env.items():
+            cm[:, k] = arr
+        prob["col_mu_env"] = cm
+    slaved = None
+    if model._affine:
+        prob["affine"], slaved = _affine_arrays(model, mu_s, lam_s, free, x)
+    ipc = None
+    if integ.self_collision and model.body_contact == "ipc":
+        ipc = prob["ipc"] = _ipc_arrays(model, integ)
+    f = external_force(model)
+    if f is not None:
+        prob["fext"] = f
+    if model._tendons:
+        prob["tendon"] = _tendon_arrays(model)
+    prob["cg_guard"] = float((0.5 if ipc is not None else 0.0) if integ.cg_restart is None else integ.cg_restart)
+    if integ.rigid_modes:
+        rg = _rigid_arrays(model, free, slaved)
+        if rg is not None:
+            prob["rigid"] = rg
+    return prob
+
+
+def min_distance(prob):
+    """Smallest node-edge distance per environment at the problem's positions (1e30 where
+    no pair is within reach) — the reference's IPCContact.min_distance
+    (implicit/ipc_contact.py:441-447), computed on the host: KD-tree candidates, then the
+    exact point-segment distance, vectorised over all environments."""
+    from scipy.spatial import cKDTree
+    ipc = prob["ipc"]
+    B = int(prob["B"])
+    out = np.full(B, 1.0e30)
+    ea, eb = np.asarray(ipc["ea"], np.int64), np.asarray(ipc["eb"], np.int64)
+    if len(ea) == 0:
+        return out
+    x = np.asarray(prob["x"], np.float64)
+    bnd = np.asarray(prob["bnd"], np.int64)
+    b2e = np.asarray(prob["b2e"], np.int64)
+    e2env = np.asarray(ipc["e2env"], np.int64)
+    reach = float(ipc["reach"])
+    L = np.linalg.norm(x[eb] - x[ea], axis=1)
+    span = float(np.ptp(x, 0).max()) + 4.0 * (float(L.max()) + reach)
+    shift = lambda e: np.stack([np.asarray(e, np.float64) * 2.0 * span, np.zeros(len(e))], 1)
+    tn = cKDTree(x[bnd] + shift(b2e))
+    te = cKDTree(0.5 * (x[ea] + x[eb]) + shift(e2env))
+    D = te.sparse_distance_matrix(tn, 0.5 * float(L.max()) + reach, output_type="ndarray")
+    k, jb = D["i"].astype(np.int64), D["j"].astype(np.int64)
+    pn = bnd[jb]
+    ok = (pn != ea[k]) & (pn != eb[k]) & (b2e[jb] == e2env[k])
+    k, jb, pn = k[ok], jb[ok], pn[ok]
+    ptr, idx = np.asarray(ipc["excl_ptr"], np.int64), np.asarray(ipc["excl_idx"], np.int64)
+    M = int(idx.max()) + 2 if len(idx) else 1
+    rows = np.repeat(np.arange(len(ptr) - 1), np.diff(ptr))
+    keys = np.sort(rows * M + idx)
+
+    def is_excl(slot, loc):
+        q = slot * M + np.asarray(loc, np.int64)
+        pos = np.minimum(np.searchsorted(keys, q), len(keys) - 1)
+        return keys[pos] == q if len(keys) else np.zeros(len(q), bool)
+    ok = ~is_excl(jb, np.asarray(ipc["ela"], np.int64)[k]) & ~is_excl(jb, np.asarray(ipc["elb"], np.int64)[k])
+    k, pn = k[ok], pn[ok]
+    a, b = x[ea[k]], x[eb[k]]
+    ab = b - a
+    t = np.clip(((x[pn] - a) * ab).sum(1) / np.maximum((ab * ab).sum(1), 1e-30), 0.0, 1.0)
+    dd = np.linalg.norm(x[pn] - a - t[:, None] * ab, axis=1)
+    near = dd < reach
+    np.minimum.at(out, e2env[k][near], dd[near])
+    return out
+
+
+def subset_problem(prob, envs):
+    """The problem restricted to the environments `envs` (renumbered 0..len-1), with every
+    batch-global parameter (iteration budget, contact scales) kept as it is."""
+    envs = np.asarray(envs, np.int64)
+    B = int(prob["B"])
+    newenv = np.full(B, -1, np.int64)
+    newenv[envs] = np.arange(len(envs))
+    node2env = np.asarray(prob["node2env"], np.int64)
+    keep_n = np.nonzero(newenv[node2env] >= 0)[0]
+    # order nodes by the new environment order, stable
+    keep_n = keep_n[np.argsort(newenv[node2env[keep_n]], kind="stable")]
+    nmap = np.full(len(node2env), -1, np.int64)
+    nmap[keep_n] = np.arange(len(keep_n))
+    tri2env = np.asarray(prob["tri2env"], np.int64)
+    keep_t = np.nonzero(newenv[tri2env] >= 0)[0]
+    keep_t = keep_t[np.argsort(newenv[tri2env[keep_t]], kind="stable")]
+    b2e = np.asarray(prob["b2e"], np.int64)
+    keep_b = np.nonzero(newenv[b2e] >= 0)[0]
+    keep_b = keep_b[np.argsort(newenv[b2e[keep_b]], kind="stable")]
+    out = {k: v for k, v in prob.items() if np.ndim(v) == 0 and not isinstance(v, dict)}
+    out["B"] = len(envs)
+    for k in ("x", "v", "mass", "free", "rest", "fext"):
+        if prob.get(k) is not None:
+            out[k] = np.asarray(prob[k])[keep_n]
+    out["node2env"] = newenv[node2env[keep_n]]
+    out["tri"] = nmap[np.asarray(prob["tri"], np.int64)[keep_t]]
+    for k in ("Bm", "area", "mu", "lam"):
+        out[k] = np.asarray(prob[k])[keep_t]
+    out["tri2env"] = newenv[tri2env[keep_t]]
+    out["bnd"] = nmap[np.asarray(prob["bnd"], np.int64)[keep_b]]
+    out["b2e"] = newenv[b2e[keep_b]]
+    bc = np.asarray(prob.get("bc_idx", np.zeros(0)), np.int64)
+    out["bc_idx"] = np.sort(nmap[bc[nmap[bc] >= 0]])
+    out["colliders"] = np.asarray(prob["colliders"])
+    if prob.get("col_mu_env") is not None:
+        out["col_mu_env"] = np.asarray(prob["col_mu_env"])[envs]
+    if prob.get("ipc") is not None:
+        ip = prob["ipc"]
+        e2env = np.asarray(ip["e2env"], np.int64)
+        ke = np.nonzero(newenv[e2env] >= 0)[0]
+        ke = ke[np.argsort(newenv[e2env[ke]], kind="stable")]
+        ptr = np.asarray(ip["excl_ptr"], np.int64)
+        idx = np.asarray(ip["excl_idx"], np.int64)
+        rows = [idx[ptr[s]:ptr[s + 1]] for s in keep_b]
+        nptr = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int64)
+        bpe = np.bincount(out["b2e"], minlength=len(envs)).astype(np.int64)
+        q = dict(ip)
+        q.update(ea=nmap[np.asarray(ip["ea"], np.int64)[ke]], eb=nmap[np.asarray(ip["eb"], np.int64)[ke]],
+                 ela=np.asarray(ip["ela"])[ke], elb=np.asarray(ip["elb"])[ke], e2env=newenv[e2env[ke]],
+                 ca=np.asarray(ip["ca"])[ke], cb=np.asarray(ip["cb"])[ke],
+                 bstart=np.concatenate([[0], np.cumsum(bpe)[:-1]]).astype(np.int64), bpe=bpe,
+                 excl_ptr=nptr, excl_idx=(np.concatenate(rows) if rows else np.zeros(0, np.int64)),
+                 mu_node=(None if ip.get("mu_node") is None else np.asarray(ip["mu_node"])[keep_n]))
+        out["ipc"] = q
+    if prob.get("rigid") is not None:
+        rg = prob["rigid"]
+        renv = np.asarray(rg["env"], np.int64)
+        kp = np.nonzero(newenv[renv] >= 0)[0]
+        kp = kp[np.argsort(newenv[renv[kp]], kind="stable")]
+        pmap = np.full(len(renv), -1, np.int64)
+        pmap[kp] = np.arange(len(kp))
+        grp = np.asarray(rg["grp"], np.int64)
+        kn = np.nonzero(pmap[grp] >= 0)[0]
+        kn = kn[np.argsort(pmap[grp[kn]], kind="stable")]
+        out["rigid"] = dict(node=nmap[np.asarray(rg["node"], np.int64)[kn]], grp=pmap[grp[kn]], env=newenv[renv[kp]])
+    for key in ("affine", "tendon"):
+        if prob.get(key) is not None:
+            raise NotImplementedError(f"subset_problem: {key} terms are not sliced")
+    return out

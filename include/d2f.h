@@ -1,0 +1,163 @@
+/* d2f.h — C ABI of the GB300 implicit-step library (libd2f.so).
+ *
+ * The library advances a batch of independent 2D scenes (the reference calls them
+ * environments) by one implicit backward-Euler step each: the preconditioned nonlinear
+ * CG solve of the reference's PNCG2DSolver.step_targets (implicit/solver.py:433-451),
+ * with plane-strain Neo-Hookean P1 triangles, collider barriers with lagged friction, IPC
+ * point-edge contact between bodies, affine rigid bodies, the rigid-mode coarse space,
+ * tendons and external forces.
+ *
+ * Ownership: every buffer is device memory owned by the caller (PyTorch tensors on the
+ * Python side). The library borrows the pointers named in d2f_scene_desc for the life of
+ * the handle and allocates nothing itself. All entry points are host functions; the
+ * compute ones enqueue work on the stream given and return without synchronising.
+ *
+ * Errors: every entry point returns D2F_OK (0) or a negative D2F_E* code; d2f_last_error
+ * gives the message of the last failure on the calling thread.
+ */
+#ifndef D2F_H
+#define D2F_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define D2F_ABI_VERSION 1
+
+/* status codes */
+#define D2F_OK 0
+#define D2F_EINVAL (-1)   /* bad argument, size or pointer */
+#define D2F_ECUDA (-2)    /* a CUDA call failed */
+#define D2F_ECAP (-3)     /* a scene's contact candidate list overflowed its capacity */
+#define D2F_ENAN (-4)     /* a scene produced a non-finite step length */
+
+/* precision modes */
+#define D2F_FP64 0        /* every operation in FP64, as the reference runs */
+#define D2F_MIXED 1       /* element, barrier and preconditioner arithmetic in FP32 */
+
+/* Per-scene index ranges into the flat arrays (all scenes' data are contiguous, scene by
+ * scene). One element per scene, device memory. Field order is part of the ABI. */
+typedef struct d2f_seg {
+    int32_t node0, nn;      /* nodes */
+    int32_t tri0, nt;       /* triangles */
+    int32_t bnd0, nb;       /* boundary nodes (slots into bnd[]) */
+    int32_t edge0, ne;      /* boundary edges (IPC) */
+    int32_t cand0, ncap;    /* contact-candidate list: first slot, capacity */
+    int32_t bc0, nbc;       /* kinematic nodes (slots into bc_idx[]) */
+    int32_t aff0, naff;     /* affine regions */
+    int32_t affn0, naffn;   /* affine region node entries */
+    int32_t rig0, nrig;     /* rigid-mode pieces */
+    int32_t rign0, nrign;   /* rigid-mode piece node entries */
+    int32_t ten0, nten;     /* tendons */
+    int32_t tent0, ntent;   /* tendon eyelet entries */
+} d2f_seg;
+
+/* Everything one solver needs. Pointers are device pointers unless noted; arrays of
+ * "real" are double in D2F_FP64 mode and float in D2F_MIXED mode. Field order is part
+ * of the ABI. */
+typedef struct d2f_scene_desc {
+    int32_t abi_version;         /* = D2F_ABI_VERSION */
+    int32_t precision;           /* D2F_FP64 | D2F_MIXED */
+    int32_t n_scenes, N, T, Nb, Ne, n_bc, n_col;
+    int32_t n_aff, n_affn, n_rig, n_rign, n_ten, n_tent, cand_total;
+    int32_t max_nb;              /* largest boundary-node count of one scene (IPC rebuild buffer) */
+    const d2f_seg *segs;         /* n_scenes */
+    /* node state */
+    double *x, *v, *xn, *xhat;   /* N x 2 */
+    void *grad, *grad_prev, *p, *diagH, *diag_el; /* N x 2 real */
+    const double *mass;          /* N */
+    const uint8_t *free_mask;    /* N: bit 0 = x free, bit 1 = y free */
+    const double *fext;          /* N x 2, or NULL: the ExternalForce term (gravity folded in) */
+    const int32_t *inc_ptr;      /* N + 1: CSR of the triangles at each node */
+    const int32_t *inc;          /* 3 T: 3 * triangle + corner, ascending triangle per node */
+    const int32_t *node_bslot;   /* N: boundary slot of the node, or -1 */
+    const int32_t *node_bc;      /* N: kinematic slot of the node, or -1 */
+    const int32_t *node_aff;     /* N: affine node entry of the node, or -1 */
+    const int32_t *node_rig;     /* N: rigid-mode piece node entry of the node, or -1 */
+    /* triangles */
+    const int32_t *tri;          /* T x 3 */
+    const void *Bm;              /* T x 4 real: rest-shape inverse, row-major */
+    const void *area, *mu, *lam; /* T real */
+    void *escr;                  /* T x 12 real: per-corner gradient and diagonal */
+    void *ecache;                /* T x 9 real: F^-T, la log J - mu, edge vectors */
+    /* boundary nodes and colliders */
+    const int32_t *bnd;          /* Nb: node of each boundary slot */
+    const double *colliders;     /* n_col x 8: kind, cx, cy, rx, ry, rref, r, mu */
+    const double *col_mu_env;    /* n_scenes x n_col per-scene collider friction, or NULL */
+    /* kinematic nodes */
+    const int32_t *bc_idx;       /* n_bc */
+    const double *bc_target;     /* n_bc x 2 */
+    /* IPC contact between bodies (Ne > 0 enables it) */
+    const int32_t *ea, *eb, *ela, *elb; /* Ne */
+    const double *ca, *cb;       /* Ne */
+    const int32_t *excl_ptr, *excl_idx; /* CSR over boundary slots: excluded local slots, sorted */
+    const double *mu_node;       /* N, or NULL: per-body friction (harmonic mean per pair) */
+    int32_t *cand;               /* cand_total: packed (edge local << 16 | slot local) */
+    double *xref;                /* Nb x 2: positions the candidate list was built at */
+    /* tendons */
+    const int32_t *t_node, *t_prv, *t_nxt, *t_tid; /* n_tent (prv/nxt/tid are global) */
+    const double *t_stiff, *t_L0, *t_Tcmd;          /* n_ten */
+    double *t_state;             /* n_ten x 4: L, dL, tau, keff */
+    /* affine bodies */
+    const int32_t *a_node, *a_grp; /* n_affn (grp global) */
+    const double *a_w;           /* n_affn x 3 */
+    const double *a_Mu, *a_La;   /* n_aff */
+    double *a_q, *a_pq, *a_gq, *a_gq_prev, *a_zq; /* n_aff x 6 */
+    double *a_H;                 /* n_aff x 18: J^T D J blocks (x, y) */
+    /* rigid-mode coarse space */
+    const int32_t *r_node, *r_grp; /* n_rign (grp global) */
+    double *r_acc, *r_zq;        /* n_rig x 3 */
+    /* per-scene outputs */
+    int32_t *iters, *active, *status; /* n_scenes */
+    int32_t *work;               /* 4 ints of scratch (the scene queue head) */
+    /* parameters */
+    double dt, drag, dhat, kappa, epsv, eps, tol_x, near_factor, alpha_max, area_shrink;
+    double ccd_eta, cg_guard, gtol;
+    double ipc_mu, ipc_dhat, ipc_kappa, reach, gap, bc_floor, skin;
+    int32_t iter_max, conv_check, friction, per_body;
+    int32_t threads;             /* threads per scene block: 128, 256 or 512 (0: 256) */
+    int32_t blocks_per_sm;       /* resident scene blocks per SM (0: library default) */
+} d2f_scene_desc;
+
+typedef struct d2f_solver d2f_solver;
+
+/* Library ABI version (D2F_ABI_VERSION of the build). */
+int32_t d2f_abi_version(void);
+
+/* Validate `desc` and create a solver handle that borrows its pointers.
+ * Replaces the reference's PNCG2DSolver.__init__ (implicit/solver.py:97-226) together
+ * with ImplicitIntegrator._build (implicit/integrator.py:252-311): the Python side builds
+ * the scene arrays, this call binds them. */
+int32_t d2f_create(const d2f_scene_desc *desc, d2f_solver **out);
+
+/* One implicit step of every scene, enqueued on `stream` (a cudaStream_t; NULL = legacy
+ * default stream). Kinematic targets are read from desc->bc_target.
+ * Replaces PNCG2DSolver.step_targets (implicit/solver.py:433-451), as called by
+ * ImplicitIntegrator.simulate (implicit/integrator.py:81-86). */
+int32_t d2f_step(d2f_solver *s, void *stream);
+
+/* Change the step size (and everything derived from it).
+ * Replaces PNCG2DSolver.set_dt (implicit/solver.py:228-233). */
+int32_t d2f_set_dt(d2f_solver *s, double dt, int32_t iter_max);
+
+/* Per-scene status of the last step: iterations, still-active flag and error code are in
+ * desc->iters / desc->active / desc->status (device). This call copies them to host
+ * arrays of n_scenes entries (any may be NULL) after synchronising `stream`.
+ * Replaces ImplicitIntegrator.stats (implicit/integrator.py:124-135). */
+int32_t d2f_stats(d2f_solver *s, void *stream, int32_t *iters, int32_t *active, int32_t *status);
+
+/* Release the handle (the caller's buffers are untouched). */
+int32_t d2f_destroy(d2f_solver *s);
+
+/* Message of the last error on this thread ("" if none). */
+const char *d2f_last_error(void);
+
+/* Number of kernels d2f_step launches per call (for launch accounting). */
+int32_t d2f_kernels_per_step(const d2f_solver *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* D2F_H */

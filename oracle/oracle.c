@@ -15,6 +15,11 @@
 #define BIG 1.0e30
 #define LOG_EPS 1.0e-6
 
+/* Test switch: 1 = every contact pair of a pass uses the step cap as it stood when the
+ * pass began (instead of the reference's running value at the start of each edge). */
+static int g_tc_fixed = 0;
+void d2o_set_tc_fixed(int v) { g_tc_fixed = v; }
+
 typedef struct { double x, y; } v2;
 typedef struct { double a, b, c, d; } m2; /* row-major [[a, b], [c, d]] */
 
@@ -396,7 +401,7 @@ typedef struct {
     double *E, *clr, *alpha;
     double *grad, *diagH;
     const double *free_;
-    double mu, h2, floor_;
+    double mu, h2, floor_, tc0;
     int per_body;
 } ipc_launch;
 
@@ -466,7 +471,7 @@ static void ipc_pair(const ipc_launch *L) {
         double Ll = sqrt(L2);
         double dlo = 1.0e-9 * dhat;
         double onset = 0.02 * dhat;
-        double t_c = L->alpha[e];
+        double t_c = g_tc_fixed ? L->tc0 : L->alpha[e];
         for (int jl = 0; jl < n_be; ++jl) {
             int jb = start + jl;
             int pn = s->bnd[jb];
@@ -554,6 +559,7 @@ static ipc_launch ipc_base(d2o_solver *s, int mode, const double *pdir, double *
     L.per_body = s->friction ? s->per_body : 0;
     L.h2 = s->h2;
     L.floor_ = (mode == 3) ? s->bc_floor * s->ipc_dhat : 0.0;
+    L.tc0 = (mode == 3) ? 1.0 : s->alpha_max;
     return L;
 }
 /* IPCContact.ccd, ipc_contact.py:432-439 */

@@ -19,6 +19,7 @@ from __future__ import annotations
 import os
 import sys
 import time
+import types
 
 import numpy as np
 
@@ -26,6 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import fixture_io  # noqa: E402
 import refload  # noqa: E402
+import scenes  # noqa: E402
 
 
 # ----------------------------------------------------------------------------- extraction
@@ -124,114 +126,10 @@ def record(R, model, integ, dt, n_steps, command=None, name=""):
 
 
 # ----------------------------------------------------------------------------- scenes
-def scene_strip_small(R):
-    m = R.Model(device="cpu")
-    m.add_ground(0.0, mu=0.8)
-    m.add_soft_body(np.ones((3, 12), np.uint8), physical_size=(0.009, 0.00225), center=(0.0, 0.0013),
-                    E=0.5e6, nu=0.40, density=1100.0)
-    m.finalize(); m.gravity = (0.0, -9.81)
-    return record(R, m, R.ImplicitIntegrator(), 2e-3, 4, name="strip_small")
-
-
-def scene_strip_cfg1(R):
-    """The strip on the ground of the headline single-scene configuration, first steps."""
-    m = R.Model(device="cpu")
-    m.add_ground(0.0, mu=0.8)
-    m.add_soft_body(np.ones((6, 72), np.uint8), physical_size=(0.054, 0.0045), center=(0.0, 0.0030),
-                    E=0.5e6, nu=0.40, density=1100.0)
-    m.finalize(); m.gravity = (0.0, -9.81)
-    return record(R, m, R.ImplicitIntegrator(), 2e-3, 2, name="strip_cfg1")
-
-
-def scene_batch_colliders(R):
-    """Three environments with different designs pressed by kinematic top rows onto a disc,
-    an ellipse, a rounded box and a rounded triangle; friction on; IPC self-contact sweeps
-    the kinematic nodes."""
-    rng = np.random.default_rng(3)
-    d1 = np.ones((6, 4), np.uint8); d1[2:4, 1:3] = 0
-    d2 = (rng.random((6, 4)) > 0.15).astype(np.uint8); d2[-1] = 1; d2[:, 0] = 1
-    m = R.Model(device="cpu")
-    m.add_disc(center=(0.0, 0.0), radius=0.004, mu=0.6)
-    m.add_object("ellipse", (0.006, 0.001), 0.002, 0.001, mu=0.3)
-    m.add_object("box", (-0.006, 0.001), 0.0015, 0.001, corner_radius=0.0004, mu=0.5)
-    m.add_object("triangle", (0.0, -0.008), 0.002, corner_radius=0.0003, mu=0.4)
-    hs = [m.add_soft_body(d, physical_size=(0.004, 0.006), center=(0.0, 0.0072), E=1.0e6, nu=0.40,
-                          density=1100.0, env_id=i) for i, d in enumerate([d1, d2, d1])]
-    m.finalize()
-    x0 = [m.rest_x(h) for h in hs]
-    tops = [np.where(x[:, 1] > x[:, 1].max() - 1e-9)[0] for x in x0]
-    for h, t in zip(hs, tops):
-        m.set_kinematic_constraint(h, t)
-    integ = R.ImplicitIntegrator(max_iter=60)
-
-    def command(k):
-        for h, x, t in zip(hs, x0, tops):
-            tgt = x.copy(); tgt[t, 1] -= 0.0012 * (k + 1) / 4
-            m.set_kinematic_target(h, tgt)
-    return record(R, m, integ, 1e-3, 4, command, name="batch_colliders")
-
-
-def scene_grip(R):
-    """Two soft pads with kinematic backs close on a free rigid block above the ground:
-    IPC contact between bodies with friction, an affine body, kinematic sweeps."""
-    PX = 0.5e-3
-    m = R.Model(device="cpu")
-    m.body_friction = 0.8
-    m.add_ground(0.0, mu=0.5)
-    m.add_affine_body(np.ones((4, 4), np.uint8), physical_size=(4 * PX, 4 * PX),
-                      center=(0.0, 2 * PX + 0.9 * PX / 8), density=600.0)
-    pads = [m.add_soft_body(np.ones((4, 2), np.uint8), physical_size=(2 * PX, 4 * PX),
-                            center=(s * 3.25 * PX, 2 * PX + 0.4e-3), E=1.0e6, nu=0.40, density=1100.0)
-            for s in (-1, +1)]
-    m.finalize(); m.gravity = (0.0, -9.81)
-    rest = [m.rest_x(p) for p in pads]
-    for s, p, X in zip((-1, +1), pads, rest):
-        back = X[:, 0].min() if s < 0 else X[:, 0].max()
-        m.set_kinematic_constraint(p, np.where(np.abs(X[:, 0] - back) < 1e-9)[0])
-
-    def command(k):
-        a = min((k + 1) / 4.0, 1.0)
-        for s, p, X in zip((-1, +1), pads, rest):
-            Y = X.copy(); Y[:, 0] -= s * 0.35 * PX * a
-            m.set_kinematic_target(p, Y)
-    return record(R, m, R.ImplicitIntegrator(max_iter=120), 1e-3, 5, command, name="grip")
-
-
-def scene_tendon(R):
-    """A cantilever clamped at its left end and bent by a tension-controlled tendon."""
-    m = R.Model(device="cpu"); m.damping = 50.0
-    h = m.add_soft_body(np.ones((3, 16), np.uint8), physical_size=(0.008, 0.0015), center=(0.0, 0.0),
-                        E=1.0e6, nu=0.40, density=1100.0)
-    m.finalize()
-    X = m.rest_x(h)
-    m.set_kinematic_constraint(h, np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0])
-    cable = m.add_tendon(h, through=[(x, 0.0005) for x in np.unique(np.round(X[:, 0], 9))])
-    integ = R.ImplicitIntegrator(self_collision=False, friction=False, max_iter=80)
-
-    def command(k):
-        m.set_tendon_tension(cable, 5.0 + 5.0 * k)
-    return record(R, m, integ, 1e-3, 4, command, name="tendon")
-
-
-def scene_line_search(R):
-    """The energy line search, on a soft block dropped on a disc collider, no rigid modes."""
-    m = R.Model(device="cpu")
-    m.add_disc(center=(0.0, -0.004), radius=0.004, mu=0.5)
-    m.add_soft_body(np.ones((3, 4), np.uint8), physical_size=(0.002, 0.0015), center=(0.0002, 0.0008),
-                    E=0.5e6, nu=0.40, density=1100.0)
-    m.finalize(); m.gravity = (0.0, -9.81)
-    integ = R.ImplicitIntegrator(line_search=True, rigid_modes=False, max_iter=50)
-    return record(R, m, integ, 2e-3, 4, name="line_search")
-
-
-SCENES = {
-    "strip_small": scene_strip_small,
-    "batch_colliders": scene_batch_colliders,
-    "grip": scene_grip,
-    "tendon": scene_tendon,
-    "line_search": scene_line_search,
-    "strip_cfg1": scene_strip_cfg1,
-}
+def run_scene(R, name):
+    ns = types.SimpleNamespace(Model=R.Model, ImplicitIntegrator=R.ImplicitIntegrator, device="cpu")
+    sc = scenes.SCENES[name](ns)
+    return record(R, sc["model"], sc["integ"], sc["dt"], sc["steps"], sc["command"], name=name)
 
 
 def main(argv):
@@ -243,9 +141,9 @@ def main(argv):
         else:
             names.append(a)
     R = refload.load(ref)
-    for name in (names or list(SCENES)):
+    for name in (names or list(scenes.SCENES)):
         t0 = time.time()
-        prob, steps = SCENES[name](R)
+        prob, steps = run_scene(R, name)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **fixture_io.pack(prob, steps, dict(scene=name)))
         print(f"{name}: {os.path.getsize(path) / 1024:.0f} KB in {time.time() - t0:.0f} s", flush=True)

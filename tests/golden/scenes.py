@@ -1,0 +1,113 @@
+"""The golden scenes, written against the reference's public API (Model /
+ImplicitIntegrator), so that the same definition builds the scene in the reference (to
+record golden vectors, make_golden.py) and in diff_2d_fem_gb300 (to check parity).
+
+Each builder takes a namespace with `Model` and `ImplicitIntegrator` and returns
+dict(model, integ, dt, steps, command) where command(k) sets the commands of step k.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def strip_small(ns):
+    m = ns.Model(device=ns.device)
+    m.add_ground(0.0, mu=0.8)
+    m.add_soft_body(np.ones((3, 12), np.uint8), physical_size=(0.009, 0.00225), center=(0.0, 0.0013),
+                    E=0.5e6, nu=0.40, density=1100.0)
+    m.finalize(); m.gravity = (0.0, -9.81)
+    return dict(model=m, integ=ns.ImplicitIntegrator(), dt=2e-3, steps=4, command=None)
+
+
+def strip_cfg1(ns, steps=12):
+    """The strip on the ground of the single-scene configuration (6x72 pixels, 511 nodes)."""
+    m = ns.Model(device=ns.device)
+    m.add_ground(0.0, mu=0.8)
+    m.add_soft_body(np.ones((6, 72), np.uint8), physical_size=(0.054, 0.0045), center=(0.0, 0.0030),
+                    E=0.5e6, nu=0.40, density=1100.0)
+    m.finalize(); m.gravity = (0.0, -9.81)
+    return dict(model=m, integ=ns.ImplicitIntegrator(), dt=2e-3, steps=steps, command=None)
+
+
+def batch_colliders(ns):
+    """Three environments with different designs pressed by kinematic top rows onto a disc,
+    an ellipse, a rounded box and a rounded triangle; friction on; IPC self-contact sweeps
+    the kinematic nodes."""
+    rng = np.random.default_rng(3)
+    d1 = np.ones((6, 4), np.uint8); d1[2:4, 1:3] = 0
+    d2 = (rng.random((6, 4)) > 0.15).astype(np.uint8); d2[-1] = 1; d2[:, 0] = 1
+    m = ns.Model(device=ns.device)
+    m.add_disc(center=(0.0, 0.0), radius=0.004, mu=0.6)
+    m.add_object("ellipse", (0.006, 0.001), 0.002, 0.001, mu=0.3)
+    m.add_object("box", (-0.006, 0.001), 0.0015, 0.001, corner_radius=0.0004, mu=0.5)
+    m.add_object("triangle", (0.0, -0.008), 0.002, corner_radius=0.0003, mu=0.4)
+    hs = [m.add_soft_body(d, physical_size=(0.004, 0.006), center=(0.0, 0.0072), E=1.0e6, nu=0.40,
+                          density=1100.0, env_id=i) for i, d in enumerate([d1, d2, d1])]
+    m.finalize()
+    x0 = [m.rest_x(h) for h in hs]
+    tops = [np.where(x[:, 1] > x[:, 1].max() - 1e-9)[0] for x in x0]
+    for h, t in zip(hs, tops):
+        m.set_kinematic_constraint(h, t)
+
+    def command(k):
+        for h, x, t in zip(hs, x0, tops):
+            tgt = x.copy(); tgt[t, 1] -= 0.0012 * (k + 1) / 4
+            m.set_kinematic_target(h, tgt)
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=60), dt=1e-3, steps=4, command=command)
+
+
+def grip(ns):
+    """Two soft pads with kinematic backs close on a free rigid block above the ground:
+    IPC contact between bodies with friction, an affine body, kinematic sweeps."""
+    PX = 0.5e-3
+    m = ns.Model(device=ns.device)
+    m.body_friction = 0.8
+    m.add_ground(0.0, mu=0.5)
+    m.add_affine_body(np.ones((4, 4), np.uint8), physical_size=(4 * PX, 4 * PX),
+                      center=(0.0, 2 * PX + 0.9 * PX / 8), density=600.0)
+    pads = [m.add_soft_body(np.ones((4, 2), np.uint8), physical_size=(2 * PX, 4 * PX),
+                            center=(s * 3.25 * PX, 2 * PX + 0.4e-3), E=1.0e6, nu=0.40, density=1100.0)
+            for s in (-1, +1)]
+    m.finalize(); m.gravity = (0.0, -9.81)
+    rest = [m.rest_x(p) for p in pads]
+    for s, p, X in zip((-1, +1), pads, rest):
+        back = X[:, 0].min() if s < 0 else X[:, 0].max()
+        m.set_kinematic_constraint(p, np.where(np.abs(X[:, 0] - back) < 1e-9)[0])
+
+    def command(k):
+        a = min((k + 1) / 4.0, 1.0)
+        for s, p, X in zip((-1, +1), pads, rest):
+            Y = X.copy(); Y[:, 0] -= s * 0.35 * PX * a
+            m.set_kinematic_target(p, Y)
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=120), dt=1e-3, steps=5, command=command)
+
+
+def tendon(ns):
+    """A cantilever clamped at its left end and bent by a tension-controlled tendon."""
+    m = ns.Model(device=ns.device); m.damping = 50.0
+    h = m.add_soft_body(np.ones((3, 16), np.uint8), physical_size=(0.008, 0.0015), center=(0.0, 0.0),
+                        E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    X = m.rest_x(h)
+    m.set_kinematic_constraint(h, np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0])
+    cable = m.add_tendon(h, through=[(x, 0.0005) for x in np.unique(np.round(X[:, 0], 9))])
+
+    def command(k):
+        m.set_tendon_tension(cable, 5.0 + 5.0 * k)
+    return dict(model=m, integ=ns.ImplicitIntegrator(self_collision=False, friction=False, max_iter=80),
+                dt=1e-3, steps=4, command=command)
+
+
+def line_search(ns):
+    """The energy line search, on a soft block dropped on a disc collider, no rigid modes."""
+    m = ns.Model(device=ns.device)
+    m.add_disc(center=(0.0, -0.004), radius=0.004, mu=0.5)
+    m.add_soft_body(np.ones((3, 4), np.uint8), physical_size=(0.002, 0.0015), center=(0.0002, 0.0008),
+                    E=0.5e6, nu=0.40, density=1100.0)
+    m.finalize(); m.gravity = (0.0, -9.81)
+    return dict(model=m, integ=ns.ImplicitIntegrator(line_search=True, rigid_modes=False, max_iter=50),
+                dt=2e-3, steps=4, command=None)
+
+
+SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
+          "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1}
