@@ -48,7 +48,8 @@ class SceneDesc(C.Structure):
 
 
 EXPORTS = ("d2f_abi_version", "d2f_create", "d2f_step", "d2f_set_dt", "d2f_stats", "d2f_destroy",
-           "d2f_last_error", "d2f_kernels_per_step")
+           "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc")
+NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
 def lib_path():
@@ -80,6 +81,8 @@ def load(build_if_missing: bool = True):
     L.d2f_last_error.restype = C.c_char_p
     L.d2f_kernels_per_step.argtypes = [_P]
     L.d2f_kernels_per_step.restype = _I
+    L.d2f_step_noalloc.argtypes = [C.POINTER(SceneDesc), _P]
+    L.d2f_step_noalloc.restype = _I
     if L.d2f_abi_version() != D2F_ABI_VERSION:
         raise RuntimeError("libd2f.so ABI version mismatch; rebuild it")
     _LIB = L

@@ -295,6 +295,11 @@ class DeviceSolver:
     def step(self):
         _lib.check(self.L.d2f_step(self.h, self._stream_ptr()), "d2f_step")
 
+    def step_noalloc(self):
+        """The same step through d2f_step_noalloc: this solver's inputs and outputs, the
+        library's static scratch instead of this solver's scratch buffers."""
+        _lib.check(self.L.d2f_step_noalloc(C.byref(self.desc), self._stream_ptr()), "d2f_step_noalloc")
+
     def set_dt(self, dt, iter_max):
         self.desc.dt = float(dt)
         _lib.check(self.L.d2f_set_dt(self.h, float(dt), int(iter_max)), "d2f_set_dt")

@@ -157,6 +157,21 @@ const char *d2f_last_error(void);
 /* Number of kernels d2f_step launches per call (for launch accounting). */
 int32_t d2f_kernels_per_step(const d2f_solver *s);
 
+/* Size of the library's static device scratch used by d2f_step_noalloc (16 MiB). */
+#define D2F_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* One implicit step of every scene, like d2f_step, for callers that cannot allocate
+ * device memory (a host that forbids cudaMalloc after start-up, a plugin handed plain
+ * pointers by its host). No handle and no allocation: the caller passes the descriptor
+ * with its inputs and outputs; the scratch fields (escr, ecache, cand, xref, work) are
+ * ignored and taken from a static device array of D2F_NOALLOC_SCRATCH_BYTES that every
+ * GPU loading the library holds until exit. A batch needing more scratch than that is
+ * refused with D2F_EINVAL and a message. The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU race — serialise them.
+ * No counterpart in the reference: its solver always owns its own buffers. */
+int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
