@@ -164,6 +164,7 @@ def run_ours(args, rank, world):
 
     m, kw, dt = workloads.rectangles_on_ground(args.scenes, seed=rank)
     integ = ImplicitIntegrator(precision=args.precision, **kw)
+    integ.threads, integ.blocks_per_sm = 0, 0
     prob = scene.solver_problem(m, integ, dt)
     prob["rest"] = np.asarray(m.me.rest_pos, np.float64)
     mixed = args.precision == "mixed"
@@ -195,8 +196,29 @@ def run_ours(args, rank, world):
         it, ac, st = solver.stats()
         return ms, it, st
 
+    if args.profile_only:  # the step kernel alone, for profilers: warmup + steps, nothing else
+        sol = DeviceSolver(prob, precision=args.precision, threads=args.threads or 128,
+                           blocks_per_sm=args.bps or 4)
+        for _ in range(args.warmup + args.steps):
+            sol.step()
+        torch.cuda.synchronize(dev)
+        it, ac, st = sol.stats()
+        print(json.dumps({"profile_only": True, "precision": args.precision, "scenes": int(prob["B"]),
+                          "iters_mean": float(np.mean(it)), "status_ok": bool((st == 0).all())}))
+        return
+
+    # ---- launch shape: the autotuner, on a sample of this batch's scenes (untimed)
+    from diff_2d_fem_gb300.tune import tune
+    shapes = {}
+    for prec in ("mixed", "fp64"):
+        if args.threads:
+            shapes[prec] = ((args.threads, args.bps), [])
+        else:
+            shapes[prec] = tune(prob, prec, sample=args.tune_sample)
+    head_nt, head_bps = shapes[args.precision][0]
+
     # ---- headline arm (device-resident)
-    sol = DeviceSolver(prob, precision=args.precision, threads=args.threads, blocks_per_sm=args.bps)
+    sol = DeviceSolver(prob, precision=args.precision, threads=head_nt, blocks_per_sm=head_bps)
     with Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if rank == 0 else 0) as clk:
         ms, it_last, st = timed(sol, args.steps, args.warmup)
     ms = maxr(ms)
@@ -220,7 +242,7 @@ def run_ours(args, rank, world):
 
     # ---- the other precision on the same batch, same steps, for the ratio and the error
     other = "fp64" if mixed else "mixed"
-    sol2 = DeviceSolver(prob, precision=other, threads=args.threads, blocks_per_sm=args.bps)
+    sol2 = DeviceSolver(prob, precision=other, threads=shapes[other][0][0], blocks_per_sm=shapes[other][0][1])
     ms2, it2, st2 = timed(sol2, args.steps, args.warmup)
     ms2 = maxr(ms2)
     value2 = n_sc * args.steps * world / (ms2 / 1e3)
@@ -238,6 +260,7 @@ def run_ours(args, rank, world):
     f_pin = torch.from_numpy(np.ascontiguousarray(fext)).pin_memory()
     x_pin = torch.empty((prob["x"].shape[0], 2), dtype=torch.float64).pin_memory()
     m._solver = None
+    integ.threads, integ.blocks_per_sm = head_nt, head_bps
     integ.simulate(m, dt)                                   # build
     s = m._solver
     for _ in range(args.warmup):
@@ -281,7 +304,10 @@ def run_ours(args, rank, world):
                    "dt": dt, "gtol": kw.get("gtol"), "iter_max": int(prob["iter_max"]),
                    "nodes": int(prob["x"].shape[0]), "triangles": int(len(prob["tri"])),
                    "l2": "inputs larger than L2 (per-step working set several GB)",
-                   "precision": args.precision, "parallelism": f"replicas x{world}"},
+                   "precision": args.precision, "parallelism": f"replicas x{world}",
+                   "launch_shape": {p: {"threads": v[0][0], "blocks_per_sm": v[0][1],
+                                        "tuned_ms": [[round(t[0], 2), t[1], t[2]] for t in v[1]]}
+                                    for p, v in shapes.items()}},
         "precision_compare": {"other": other, "other_value": value2,
                               "speedup_vs_other": value / value2 if value2 else None,
                               "pos_err_rel_to_coords": pos_err_rel, "pos_err_rel_to_displacement": pos_err_disp},
@@ -309,8 +335,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--threads", type=int, default=0, help="launch shape; 0 = autotune")
     ap.add_argument("--bps", type=int, default=0)
+    ap.add_argument("--tune-sample", type=int, default=1024)
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run only warmup + steps of the step kernel (for ncu)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -29,10 +29,10 @@ DESC_FIELDS = (
     + [(n, _I) for n in ("n_scenes", "N", "T", "Nb", "Ne", "n_bc", "n_col", "n_aff", "n_affn", "n_rig",
                          "n_rign", "n_ten", "n_tent", "cand_total", "max_nb")]
     + [(n, _P) for n in (
-        "segs", "x", "v", "xn", "xhat", "grad", "grad_prev", "p", "diagH", "diag_el", "mass", "free_mask",
-        "fext", "inc_ptr", "inc", "node_bslot", "node_bc", "node_aff", "node_rig", "tri", "Bm", "area", "mu",
-        "lam", "escr", "ecache", "bnd", "colliders", "col_mu_env", "bc_idx", "bc_target", "ea", "eb", "ela",
-        "elb", "ca", "cb", "excl_ptr", "excl_idx", "mu_node", "cand", "xref", "t_node", "t_prv", "t_nxt",
+        "segs", "x", "v", "xn", "xhat", "xu", "xrest", "grad", "grad_prev", "p", "diagH", "diag_el", "mass", "free_mask",
+        "fext", "inc_ptr", "inc", "inc8", "node_bslot", "node_bc", "node_aff", "node_rig", "tri", "Bm", "area", "mu",
+        "lam", "Dm", "escr", "ecache", "bnd", "colliders", "col_mu_env", "bc_idx", "bc_target", "ea", "eb", "ela",
+        "elb", "ca", "cb", "excl_ptr", "excl_idx", "mu_node", "cand", "cand_tr", "xref", "t_node", "t_prv", "t_nxt",
         "t_tid", "t_stiff", "t_L0", "t_Tcmd", "t_state", "a_node", "a_grp", "a_w", "a_Mu", "a_La", "a_q",
         "a_pq", "a_gq", "a_gq_prev", "a_zq", "a_H", "r_node", "r_grp", "r_acc", "r_zq", "iters", "active",
         "status", "work")]

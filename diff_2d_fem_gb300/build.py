@@ -2,7 +2,8 @@
 
     python -m diff_2d_fem_gb300.build
 
-One translation unit, one -gencode (sm_103a), no CMake. The library lands in
+Three translation units (FP64 kernels, mixed kernels, C ABI) compiled in parallel, one
+-gencode (sm_103a), no CMake. The library lands in
 diff_2d_fem_gb300/_build/libd2f.so and is rebuilt when a source is newer than it.
 """
 from __future__ import annotations
@@ -15,8 +16,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libd2f.so")
-SOURCES = [os.path.join(HERE, "csrc", "pncg_step.cu")]
-DEPS = SOURCES + [os.path.join(HERE, "csrc", "d2f_math.cuh"), os.path.join(ROOT, "include", "d2f.h")]
+CSRC = os.path.join(HERE, "csrc")
+SOURCES = [os.path.join(CSRC, f) for f in ("pncg_fp64.cu", "pncg_mixed.cu", "d2f_capi.cu")]
+DEPS = SOURCES + [os.path.join(CSRC, "pncg_kernel.cuh"), os.path.join(CSRC, "d2f_math.cuh"),
+                  os.path.join(ROOT, "include", "d2f.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -26,17 +29,30 @@ def nvcc():
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile the three translation units in parallel, link libd2f.so."""
     os.makedirs(OUT_DIR, exist_ok=True)
     newest = max(os.path.getmtime(p) for p in DEPS + [__file__])
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
-    tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc(), "-O3", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", "-lineinfo",
-           "--use_fast_math" if os.environ.get("D2F_FAST_MATH") else "-ftz=false",
-           "-I", os.path.join(ROOT, "include")] + ARCH + ["-o", tmp] + SOURCES
+    tag = f"{os.getpid()}"
+    flags = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", "-I", os.path.join(ROOT, "include")] + ARCH
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    subprocess.run(cmd, check=True)
+        flags.append("-Xptxas=-v")
+    objs, procs = [], []
+    for src in SOURCES:
+        obj = os.path.join(OUT_DIR, os.path.basename(src) + f".{tag}.o")
+        objs.append(obj)
+        procs.append(subprocess.Popen([nvcc(), "-c"] + flags + ["-o", obj, src]))
+    rcs = [p.wait() for p in procs]
+    if any(rcs):
+        for o in objs:
+            if os.path.exists(o):
+                os.remove(o)
+        raise RuntimeError(f"nvcc failed ({rcs})")
+    tmp = LIB + f".tmp{tag}"
+    subprocess.run([nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs, check=True)
+    for o in objs:
+        os.remove(o)
     os.replace(tmp, LIB)
     return LIB
 

@@ -177,6 +177,34 @@ __device__ inline double accd(double px, double py, double ax, double ay, double
     return t;
 }
 
+// The ACCD advance of one pair run against an unbounded cap, summarised so that its result
+// for ANY cap m <= t_c0 can be read off afterwards: accd(..., m) == (m <= T ? m : R).
+// R is the return value with cap t_c0; T is the advance at which the loop stopped (the first
+// step that would have crossed the gap, or the last one taken), +inf when it reached t_c0 or
+// nothing moves. The reference reads the cap once per edge, after the edges before it have
+// lowered it (ipc_contact.py:211, 241); this lets the caller replay that order exactly.
+__device__ inline double accd_profile(double px, double py, double ax, double ay, double bx, double by,
+                                      double dpx, double dpy, double dax, double day, double dbx, double dby,
+                                      double g, double t_c0, double &T) {
+    double mx = (dpx + dax + dbx) / 3.0, my = (dpy + day + dby) / 3.0;
+    dpx -= mx; dpy -= my; dax -= mx; day -= my; dbx -= mx; dby -= my;
+    double lp = sqrt(dpx * dpx + dpy * dpy) + dmax(sqrt(dax * dax + day * day), sqrt(dbx * dbx + dby * dby));
+    T = 1.0e300;
+    if (lp <= 1.0e-30) return t_c0;
+    double d = seg_dist(px, py, ax, ay, bx, by);
+    double t = 0.0, tl = (d - g) / lp;
+    for (int k = 0; k < 32; ++k) {
+        double tn = t + tl;
+        if (tn >= t_c0) return t_c0;
+        d = seg_dist(px + tn * dpx, py + tn * dpy, ax + tn * dax, ay + tn * day, bx + tn * dbx, by + tn * dby);
+        if (k > 0 && d < g) { T = tn; return t; }
+        t = tn;
+        tl = 0.9 * d / lp;
+    }
+    T = t;
+    return t;
+}
+
 // ---- Neo-Hookean on a 2x2 (FP64), core/math.py:75-93: used by the affine blocks
 struct M2 { double a, b, c, d; };
 __device__ __forceinline__ double det2(M2 A) { return A.a * A.d - A.c * A.b; }
@@ -203,7 +231,7 @@ __device__ __forceinline__ M2 nh_d2(M2 F, M2 dF, double mu, double la) {
 __device__ __forceinline__ double ddot2(M2 A, M2 B) { return A.a * B.a + A.b * B.b + A.c * B.c + A.d * B.d; }
 
 // ---- 6x6 block: reduced Hessian, Cholesky with diagonal fallback, solve; affine.py:60-147
-__device__ inline void reduced_hessian(M2 A, double Mu, double La, double h2, const double *Hs, double H[6][6]) {
+__device__ inline void reduced_hessian(M2 A, double Mu, double La, double h2, const double *Hs, double (*H)[6]) {
     // Hs: x block then y block, 6 unique entries each: 00 01 02 11 12 22
     const int u[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     for (int r = 0; r < 6; ++r)
@@ -233,7 +261,7 @@ __device__ inline void reduced_hessian(M2 A, double Mu, double La, double h2, co
     }
 }
 
-__device__ inline void chol6(const double H[6][6], double L[6][6]) {
+__device__ inline void chol6(const double (*H)[6], double (*L)[6]) {
     for (int r = 0; r < 6; ++r)
         for (int c = 0; c < 6; ++c) L[r][c] = 0.0;
     bool ok = true;
@@ -258,7 +286,7 @@ __device__ inline void chol6(const double H[6][6], double L[6][6]) {
     }
 }
 
-__device__ inline void chol6_solve(const double L[6][6], const double *b, double *x) {
+__device__ inline void chol6_solve(const double (*L)[6], const double *b, double *x) {
     double y[6];
     for (int i = 0; i < 6; ++i) {
         double s = b[i];

@@ -1,0 +1,37 @@
+// pncg_fp64.cu — the step kernel instantiated for the plain FP64 path.
+#include "pncg_kernel.cuh"
+
+namespace d2f {
+
+template <int NT, int MINB>
+static cudaError_t launch_v(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
+    auto k = pncg_step_kernel<double, NT, MINB>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k<<<grid, NT, smem, st>>>(d);
+    return cudaGetLastError();
+}
+
+template <int NT, int MINB>
+static int occupancy_v(int smem) {
+    int nb = 0;
+    auto k = pncg_step_kernel<double, NT, MINB>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, NT, smem) != cudaSuccess) return 1;
+    return nb > 0 ? nb : 1;
+}
+
+cudaError_t launch_fp64(int nt, int minb, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
+#define D2F_L(N, MB) if (nt == N && minb == MB) return launch_v<N, MB>(d, grid, smem, st);
+    D2F_VARIANTS(D2F_L)
+#undef D2F_L
+    return cudaErrorInvalidConfiguration;
+}
+
+int occupancy_fp64(int nt, int minb, int smem) {
+#define D2F_O(N, MB) if (nt == N && minb == MB) return occupancy_v<N, MB>(smem);
+    D2F_VARIANTS(D2F_O)
+#undef D2F_O
+    return 1;
+}
+
+}  // namespace d2f

@@ -1,4 +1,4 @@
-// pncg_step.cu — the implicit step of every scene of a batch, one persistent kernel launch.
+// pncg_kernel.cuh — the implicit step of every scene of a batch, one persistent kernel launch.
 //
 // GB300 design. A batch is many independent scenes of a few hundred to a few thousand
 // nodes. One thread block owns one scene for the whole step: it runs every PNCG iteration
@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#pragma once
 #include "../../include/d2f.h"
 #include "d2f_math.cuh"
 
@@ -118,8 +119,9 @@ __device__ __forceinline__ bool excluded(const d2f_scene_desc &d, int slot, int 
 }
 
 // ---------------------------------------------------------------------- the kernel
-template <class R, int NT>
-__global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d2f_scene_desc d) {
+template <class R, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_constant__ d2f_scene_desc d) {
+    constexpr bool MIXED = sizeof(R) == 4;
     using R2 = typename R2T<R>::T;
     using R4 = typename R4T<R>::T;
     constexpr int NW = NT / 32;
@@ -127,6 +129,9 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
     __shared__ Col cols[MAX_COL];
     __shared__ double red[NW * 20 + 20];
     __shared__ int sc_next;
+    __shared__ int s_wcnt[NW];
+    __shared__ double s_H6[6][6], s_L6[6][6];
+    __shared__ double colmu[MAX_COL];
     extern __shared__ float2 pos32[];  // boundary positions for the candidate-list rebuild
 
     const int tid = threadIdx.x;
@@ -154,6 +159,10 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
     const double2 *Fx = reinterpret_cast<const double2 *>(d.fext);
     const double2 *Tgt = reinterpret_cast<const double2 *>(d.bc_target);
     double2 *Xref = reinterpret_cast<double2 *>(d.xref);
+    double2 *Ctr = reinterpret_cast<double2 *>(d.cand_tr);
+    double2 *U = reinterpret_cast<double2 *>(d.xu);                 // x - rest (mixed path)
+    const double2 *Xr = reinterpret_cast<const double2 *>(d.xrest);
+    const R4 *Dmr = reinterpret_cast<const R4 *>(d.Dm);
 
     if (tid < n_col && tid < MAX_COL) {
         const double *c = d.colliders + 8 * tid;
@@ -173,11 +182,8 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
         const int nbl = sg.nb;
         const double near = d.near_factor * dhat;
 
-        // ---- scene-specific collider friction
-        double colmu[MAX_COL];
-#pragma unroll 1
-        for (int k = 0; k < n_col && k < MAX_COL; ++k)
-            colmu[k] = d.col_mu_env ? d.col_mu_env[sc * n_col + k] : cols[k].mu;
+        // ---- scene-specific collider friction (shared; written before the step-start barrier)
+        if (tid < n_col && tid < MAX_COL) colmu[tid] = d.col_mu_env ? d.col_mu_env[sc * n_col + tid] : cols[tid].mu;
 
         // ================================================================ step setup
         // init_step_kernel (kernels.py:41-50); p = grad = 0 (solver.py:447)
@@ -230,25 +236,43 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
             const float rad = (float)(d.reach + d.skin);
             const float slack = 1.0e-5f * rad;
             const long npair = (long)sg.ne * nbl;
-            for (long q = tid; q < npair; q += NT) {
-                int k = (int)(q / nbl), j = (int)(q - (long)k * nbl);
-                int ge = sg.edge0 + k;
-                int a = d.ea[ge], b = d.eb[ge];
-                int pn = d.bnd[sg.bnd0 + j];
-                if (pn == a || pn == b) continue;
-                int la = d.node_bslot[a] - sg.bnd0, lb = d.node_bslot[b] - sg.bnd0;
-                float2 pa = pos32[la], pb = pos32[lb], pp = pos32[j];
-                // point-segment distance in FP32 with slack: a conservative pre-filter
-                float abx = pb.x - pa.x, aby = pb.y - pa.y;
-                float wx = pp.x - pa.x, wy = pp.y - pa.y;
-                float t = (wx * abx + wy * aby) / fmaxf(abx * abx + aby * aby, 1e-30f);
-                t = fminf(fmaxf(t, 0.f), 1.f);
-                float dx = wx - t * abx, dy = wy - t * aby;
-                float d32 = sqrtf(dx * dx + dy * dy);
-                if (d32 > rad + slack) continue;
-                if (excluded(d, sg.bnd0 + j, d.ela[ge]) || excluded(d, sg.bnd0 + j, d.elb[ge])) continue;
-                int slot = atomicAdd(&S.count, 1);
-                if (slot < sg.ncap) d.cand[sg.cand0 + slot] = (int)(((unsigned)k << 16) | (unsigned)j);
+            // ordered stream compaction: the list comes out sorted by (edge, boundary slot),
+            // the order in which the reference visits the pairs
+            for (long base = 0; base < npair; base += NT) {
+                const long q = base + tid;
+                bool keep = false;
+                int k = 0, j = 0;
+                if (q < npair) {
+                    k = (int)(q / nbl);
+                    j = (int)(q - (long)k * nbl);
+                    const int ge = sg.edge0 + k;
+                    const int a = d.ea[ge], b = d.eb[ge];
+                    const int pn = d.bnd[sg.bnd0 + j];
+                    if (pn != a && pn != b) {
+                        const int la = d.node_bslot[a] - sg.bnd0, lb = d.node_bslot[b] - sg.bnd0;
+                        const float2 pa = pos32[la], pb = pos32[lb], pp = pos32[j];
+                        // point-segment distance in FP32 with slack: a conservative pre-filter
+                        const float abx = pb.x - pa.x, aby = pb.y - pa.y;
+                        const float wx = pp.x - pa.x, wy = pp.y - pa.y;
+                        float t = (wx * abx + wy * aby) / fmaxf(abx * abx + aby * aby, 1e-30f);
+                        t = fminf(fmaxf(t, 0.f), 1.f);
+                        const float dx = wx - t * abx, dy = wy - t * aby;
+                        keep = sqrtf(dx * dx + dy * dy) <= rad + slack &&
+                               !excluded(d, sg.bnd0 + j, d.ela[ge]) && !excluded(d, sg.bnd0 + j, d.elb[ge]);
+                    }
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                const int lane = tid & 31, warp = tid >> 5;
+                if (lane == 0) s_wcnt[warp] = __popc(bal);
+                __syncthreads();                      // s_wcnt and S.count readable
+                int off = S.count + __popc(bal & ((1u << lane) - 1u)), tot = 0;
+                for (int w = 0; w < NW; ++w) {
+                    if (w < warp) off += s_wcnt[w];
+                    tot += s_wcnt[w];
+                }
+                if (keep && off < sg.ncap) d.cand[sg.cand0 + off] = (int)(((unsigned)k << 16) | (unsigned)j);
+                __syncthreads();                      // every thread has read them
+                if (tid == 0) S.count += tot;         // read after the next chunk's first barrier
             }
             __syncthreads();
             if (tid == 0) {
@@ -268,7 +292,7 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
             double2 t = Tgt[b], x = X[n];
             return make_double2(t.x - x.x, t.y - x.y);
         };
-        auto ipc_pairs = [&](int mode, double &acc_pHp, double &acc_alpha, double t_c) {
+        auto ipc_pairs = [&](int mode, double &acc_pHp, double t_c) {
             const double idhat = d.ipc_dhat, ikappa = d.ipc_kappa, reach = d.reach, gap = d.gap;
             const double dlo = 1.0e-9 * idhat, onset = 0.02 * idhat;
             const double mu_s = d.friction ? d.ipc_mu : 0.0;
@@ -289,7 +313,10 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
                 if (tt <= 0.0) { dvx = wx; dvy = wy; }
                 else if (tt >= 1.0) { dvx = xp.x - xb.x; dvy = xp.y - xb.y; }
                 double dd = sqrt(dvx * dvx + dvy * dvy);
-                if (!(dd < reach)) continue;
+                if (!(dd < reach)) {
+                    if (mode == 1 || mode == 3) Ctr[sg.cand0 + c] = make_double2(1.0e300, 1.0e300);
+                    continue;
+                }
                 if (mode == 1 || mode == 3) {
                     double keep = dmax(gap * dd, idhat - onset);
                     if (dd < idhat) keep = dd - dmin(2.0 * (idhat - dd) + onset, 0.5 * dd);
@@ -300,8 +327,10 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
                         R2 u0 = P[pn], u1 = P[a], u2 = P[b];
                         qp = make_double2(u0.x, u0.y); qa = make_double2(u1.x, u1.y); qb = make_double2(u2.x, u2.y);
                     }
-                    acc_alpha = dmin(acc_alpha, accd(xp.x, xp.y, xa.x, xa.y, xb.x, xb.y, qp.x, qp.y,
-                                                      qa.x, qa.y, qb.x, qb.y, keep, t_c));
+                    double T;
+                    const double Rv = accd_profile(xp.x, xp.y, xa.x, xa.y, xb.x, xb.y, qp.x, qp.y,
+                                                   qa.x, qa.y, qb.x, qb.y, keep, t_c, T);
+                    Ctr[sg.cand0 + c] = make_double2(T, Rv);
                 }
                 if (mode == 3) continue;
                 double mu_p = mu_s;
@@ -402,6 +431,23 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
             }
         };
 
+        // The reference's serial order for the ACCD cap: each edge reads the cap once, as the
+        // edges before it left it, and its pairs lower it (ipc_contact.py:211, 241). Replayed
+        // by one thread over the ordered candidate list from the per-pair profiles.
+        auto tc_scan = [&](double m0) -> double {
+            double m = m0, t_c = m0;
+            int prevk = -1;
+            const int nc = S.ncand;
+#pragma unroll 4
+            for (int c = 0; c < nc; ++c) {
+                const int k = (int)((unsigned)d.cand[sg.cand0 + c] >> 16);
+                const double2 pr = Ctr[sg.cand0 + c];
+                if (k != prevk) { t_c = m; prevk = k; }
+                m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+            }
+            return m;
+        };
+
         // kinematic sweep (IPCContact._sweep, ipc_contact.py:456-463 with bc_motion /
         // ccd mode 3 / far cap / bc_advance, :299-331)
         auto sweep = [&]() {
@@ -411,27 +457,44 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
                 double2 q = kin_dir(d.bc_idx[b]);
                 qi = dmax(qi, sqrt(q.x * q.x + q.y * q.y));
             }
-            double dummy = 0.0, al = 1.0;
-            ipc_pairs(3, dummy, al, 1.0);
-            double v[2] = {qi, al};
-            const int ops[2] = {1, 2};
-            block_reduce<NT, 2>(v, ops, red);
-            double alpha_s = v[1];
-            if (v[0] > 0.0) alpha_s = dmin(alpha_s, 0.45 * d.reach / v[0]);
+            double dummy = 0.0;
+            ipc_pairs(3, dummy, 1.0);
+            double v[1] = {qi};
+            const int ops[1] = {1};
+            block_reduce<NT, 1>(v, ops, red);
+            if (tid == 0) {
+                double a_s = tc_scan(1.0);
+                if (v[0] > 0.0) a_s = dmin(a_s, 0.45 * d.reach / v[0]);
+                S.alpha_s = a_s;
+            }
+            __syncthreads();
+            const double alpha_s = S.alpha_s;
             for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
                 int n = d.bc_idx[b];
                 double2 tg = Tgt[b], x = X[n];
                 double2 nx = alpha_s >= 1.0 ? tg : make_double2(x.x + alpha_s * (tg.x - x.x), x.y + alpha_s * (tg.y - x.y));
                 X[n] = nx;
                 Xh[n] = nx;
+                if constexpr (MIXED) {
+                    const double2 xr = Xr[n];
+                    U[n] = make_double2(nx.x - xr.x, nx.y - xr.y);
+                }
             }
-            if (tid == 0) { S.q_inf = v[0]; S.alpha_s = alpha_s; }
+            if (tid == 0) S.q_inf = v[0];
             __syncthreads();
         };
 
         if (scene_ipc && sg.nbc > 0) {  // IPCContact.advance_bc, ipc_contact.py:465-473
             sweep();
             if (tid == 0) S.pending = !(S.alpha_s >= 1.0);
+            __syncthreads();
+        }
+
+        if constexpr (MIXED) {  // displacement from rest, FP64, for the FP32 element routine
+            for (int i = n0 + tid; i < n1; i += NT) {
+                const double2 xi = X[i], xr = Xr[i];
+                U[i] = make_double2(xi.x - xr.x, xi.y - xr.y);
+            }
             __syncthreads();
         }
 
@@ -451,19 +514,44 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
             // ---------------------------------------------- A1: triangle pass (grad + diag)
             for (int t = t0 + tid; t < t1; t += NT) {
                 const int i0 = __ldg(d.tri + 3 * t), i1 = __ldg(d.tri + 3 * t + 1), i2 = __ldg(d.tri + 3 * t + 2);
-                const double2 x0 = X[i0], x1 = X[i1], x2 = X[i2];
-                const R e1x = R(x1.x - x0.x), e1y = R(x1.y - x0.y), e2x = R(x2.x - x0.x), e2y = R(x2.y - x0.y);
                 const R4 B = Bm[t];
                 const R A = Ar[t], mu = Mu[t], la = La[t];
-                const R F00 = e1x * B.x + e2x * B.z, F01 = e1x * B.y + e2x * B.w;
-                const R F10 = e1y * B.x + e2y * B.z, F11 = e1y * B.y + e2y * B.w;
-                const R J = F00 * F11 - F10 * F01;
-                const R logJ = rlog<R>(rmax<R>(J, R(1.0e-6)));
-                const R iJ = J != R(0) ? R(1) / J : R(0);
-                const R G00 = F11 * iJ, G01 = -F10 * iJ, G10 = -F01 * iJ, G11 = F00 * iJ;  // F^-T
-                const R c1 = la * logJ - mu;
-                const R P00 = mu * F00 + c1 * G00, P01 = mu * F01 + c1 * G01;
-                const R P10 = mu * F10 + c1 * G10, P11 = mu * F11 + c1 * G11;
+                R e1x, e1y, e2x, e2y, G00, G01, G10, G11, c1, P00, P01, P10, P11;
+                if constexpr (MIXED) {
+                    // F = I + H, H from FP64 displacement differences: every term of P below
+                    // is O(strain), so FP32 rounding stays relative to the stress, not to mu.
+                    const double2 u0 = U[i0], u1 = U[i1], u2 = U[i2];
+                    const R d1x = R(u1.x - u0.x), d1y = R(u1.y - u0.y), d2x = R(u2.x - u0.x), d2y = R(u2.y - u0.y);
+                    const R4 Dm = Dmr[t];  // rest edge vectors (X1 - X0, X2 - X0)
+                    e1x = Dm.x + d1x; e1y = Dm.y + d1y; e2x = Dm.z + d2x; e2y = Dm.w + d2y;
+                    const R H00 = d1x * B.x + d2x * B.z, H01 = d1x * B.y + d2x * B.w;
+                    const R H10 = d1y * B.x + d2y * B.z, H11 = d1y * B.y + d2y * B.w;
+                    const R dH = H00 * H11 - H01 * H10;
+                    const R Jm1 = (H00 + H11) + dH;                         // J - 1
+                    const R J = R(1) + Jm1;
+                    const R logJ = J > R(1.0e-6) ? log1pf(Jm1) : rlog<R>(R(1.0e-6));
+                    const R iJ = J != R(0) ? R(1) / J : R(0);
+                    G00 = (R(1) + H11) * iJ; G01 = -H10 * iJ; G10 = -H01 * iJ; G11 = (R(1) + H00) * iJ;
+                    c1 = la * logJ - mu;
+                    // mu (F - F^-T) + la log J F^-T with F - F^-T = ((J + 1) H_diag + det H, J H_off + ...) / J
+                    const R onepJ = R(1) + J, ll = la * logJ;
+                    P00 = mu * ((H00 * onepJ + dH) * iJ) + ll * G00;
+                    P01 = mu * ((J * H01 + H10) * iJ) + ll * G01;
+                    P10 = mu * ((J * H10 + H01) * iJ) + ll * G10;
+                    P11 = mu * ((H11 * onepJ + dH) * iJ) + ll * G11;
+                } else {
+                    const double2 x0 = X[i0], x1 = X[i1], x2 = X[i2];
+                    e1x = R(x1.x - x0.x); e1y = R(x1.y - x0.y); e2x = R(x2.x - x0.x); e2y = R(x2.y - x0.y);
+                    const R F00 = e1x * B.x + e2x * B.z, F01 = e1x * B.y + e2x * B.w;
+                    const R F10 = e1y * B.x + e2y * B.z, F11 = e1y * B.y + e2y * B.w;
+                    const R J = F00 * F11 - F10 * F01;
+                    const R logJ = rlog<R>(rmax<R>(J, R(1.0e-6)));
+                    const R iJ = J != R(0) ? R(1) / J : R(0);
+                    G00 = F11 * iJ; G01 = -F10 * iJ; G10 = -F01 * iJ; G11 = F00 * iJ;  // F^-T
+                    c1 = la * logJ - mu;
+                    P00 = mu * F00 + c1 * G00; P01 = mu * F01 + c1 * G01;
+                    P10 = mu * F10 + c1 * G10; P11 = mu * F11 + c1 * G11;
+                }
                 const R hA = rh2 * A;
                 const R g1x = hA * (P00 * B.x + P01 * B.y), g1y = hA * (P10 * B.x + P11 * B.y);
                 const R g2x = hA * (P00 * B.z + P01 * B.w), g2y = hA * (P10 * B.z + P11 * B.w);
@@ -499,9 +587,28 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
                 R gx = (fm & 1) ? R(m) * R(xi.x - xh.x) : R(0);
                 R gy = (fm & 2) ? R(m) * R(xi.y - xh.y) : R(0);
                 R dx = R(m), dy = R(m);
-                for (int k = __ldg(d.inc_ptr + i); k < __ldg(d.inc_ptr + i + 1); ++k) {
-                    const R4 c = Esc[__ldg(d.inc + k)];
-                    gx += c.x; gy += c.y; dx += c.z; dy += c.w;
+                {
+                    // the node's corners, ascending triangle: 8 slots in two vector loads, then
+                    // their contributions fetched together (ILP), summed in order
+                    const int4 ca = __ldg(reinterpret_cast<const int4 *>(d.inc8) + 2 * i);
+                    const int4 cb = __ldg(reinterpret_cast<const int4 *>(d.inc8) + 2 * i + 1);
+                    const int cs[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+#pragma unroll
+                    for (int h = 0; h < 8; h += 4) {  // two batches of four loads in flight
+                        R4 cv[4];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            if (cs[h + q] >= 0) cv[q] = Esc[cs[h + q]];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            if (cs[h + q] >= 0) { gx += cv[q].x; gy += cv[q].y; dx += cv[q].z; dy += cv[q].w; }
+                    }
+                    // nodes of more than 8 triangles continue in the CSR
+                    const int k0 = __ldg(d.inc_ptr + i) + 8, k1 = __ldg(d.inc_ptr + i + 1);
+                    for (int k = k0; k < k1; ++k) {
+                        const R4 c = Esc[__ldg(d.inc + k)];
+                        gx += c.x; gy += c.y; dx += c.z; dy += c.w;
+                    }
                 }
                 if (scene_rig) Del[i] = mk2<R>(dx, dy);
                 if (d.node_bslot[i] >= 0) {
@@ -582,8 +689,8 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
             // ---------------------------------------------- A3: contact between bodies, tendons
             if (scene_ipc) {
                 ipc_refresh(false);
-                double z0 = 0.0, z1 = 0.0;
-                ipc_pairs(0, z0, z1, 0.0);
+                double z0 = 0.0;
+                ipc_pairs(0, z0, 0.0);
                 __syncthreads();
             }
             if (sg.nten > 0) {  // Tendon.grad_diag, actuation.py:169-212, 298-303
@@ -767,7 +874,7 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
                         double g[6], y[6], z[6], zy[6];
                         const double hp[6] = {0.0, h2 * Pm.a, h2 * Pm.b, 0.0, h2 * Pm.c, h2 * Pm.d};
                         for (int r = 0; r < 6; ++r) g[r] = d.a_gq[6 * b + r] + hp[r];
-                        double H[6][6], L[6][6];
+                        double (*H)[6] = s_H6, (*L)[6] = s_L6;   // shared: keeps 72 doubles out of registers
                         reduced_hessian(A, d.a_Mu[b], d.a_La[b], h2, d.a_H + 18 * b, H);
                         chol6(H, L);
                         for (int r = 0; r < 6; ++r) y[r] = g[r] - d.a_gq_prev[6 * b + r];
@@ -943,7 +1050,7 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
                 }
                 // IPC mode 1: curvature along p and the ACCD step limit (t_c = the step cap at
                 // the start of the contact pass, alpha_max)
-                if (scene_ipc) ipc_pairs(1, acc_pHp, acc_alpha, d.alpha_max);
+                if (scene_ipc) ipc_pairs(1, acc_pHp, d.alpha_max);
                 // Tendon.pHp (actuation.py:244-268, 305-310)
                 for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
                     double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3], dL = 0.0;
@@ -972,7 +1079,10 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
                 if (tid == 0) {
                     const double ph = v[0], pinf = v[1], clr = v[2];
                     double a = v[3];
-                    if (scene_ipc && pinf > 0.0) a = dmin(a, 0.45 * d.reach / pinf);  // ipc_far_cap_kernel
+                    if (scene_ipc) {
+                        a = dmin(a, tc_scan(d.alpha_max));                       // ACCD, reference order
+                        if (pinf > 0.0) a = dmin(a, 0.45 * d.reach / pinf);      // ipc_far_cap_kernel
+                    }
                     S.pHp = ph; S.p_inf = pinf; S.clr_min = clr;
                     S.alpha = a;
                     // alpha_finalize_kernel (kernels.py:374-423), plus the optional relative
@@ -1014,13 +1124,21 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
                 const double al = S.alpha;
                 for (int i = n0 + tid; i < n1; i += NT) {
                     const int ka = d.node_aff[i];
+                    double2 nx;
                     if (ka >= 0) {
                         const double *w = d.a_w + 3 * ka, *q = d.a_q + 6 * d.a_grp[ka];
-                        X[i] = make_double2(w[0] * q[0] + w[1] * q[1] + w[2] * q[2], w[0] * q[3] + w[1] * q[4] + w[2] * q[5]);
+                        nx = make_double2(w[0] * q[0] + w[1] * q[1] + w[2] * q[2], w[0] * q[3] + w[1] * q[4] + w[2] * q[5]);
                     } else if (act) {
                         const R2 pp = P[i];
                         const double2 xi = X[i];
-                        X[i] = make_double2(xi.x + al * double(pp.x), xi.y + al * double(pp.y));
+                        nx = make_double2(xi.x + al * double(pp.x), xi.y + al * double(pp.y));
+                    } else {
+                        continue;
+                    }
+                    X[i] = nx;
+                    if constexpr (MIXED) {
+                        const double2 xr = Xr[i];
+                        U[i] = make_double2(nx.x - xr.x, nx.y - xr.y);
                     }
                 }
                 __syncthreads();
@@ -1043,253 +1161,16 @@ __global__ void __launch_bounds__(NT) pncg_step_kernel(const __grid_constant__ d
 
 }  // namespace d2f
 
-// ============================================================================ C ABI
-#include <stdio.h>
-#include <string.h>
 
-struct d2f_solver {
-    d2f_scene_desc d;
-    int grid;
-    int smem;
-};
+// Launch shapes the library is built with: (threads per scene block, minimum resident
+// blocks per SM the register budget is fitted to). d2f_scene_desc.threads / blocks_per_sm
+// select one; the autotuner (tune.py) measures them.
+#define D2F_VARIANTS(X) X(128, 4) X(256, 1) X(256, 2) X(256, 3) X(512, 1)
 
-static thread_local char g_err[512];
-
-static int fail(int code, const char *msg) {
-    snprintf(g_err, sizeof g_err, "%s", msg);
-    return code;
-}
-
-template <class R, int NT>
-static cudaError_t launch_one(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
-    auto k = d2f::pncg_step_kernel<R, NT>;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    k<<<grid, NT, smem, st>>>(d);
-    return cudaGetLastError();
-}
-
-template <class R, int NT>
-static int occupancy(int smem) {
-    int nb = 0;
-    auto k = d2f::pncg_step_kernel<R, NT>;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, NT, smem) != cudaSuccess) return 1;
-    return nb > 0 ? nb : 1;
-}
-
-extern "C" {
-
-int32_t d2f_abi_version(void) { return D2F_ABI_VERSION; }
-
-const char *d2f_last_error(void) { return g_err; }
-
-}  // extern "C"
-
-// Checks every size and pointer of a descriptor; the scratch pointers (escr, ecache, cand,
-// xref, work) only when `scratch` is set.
-static int validate(const d2f_scene_desc &d, bool scratch) {
-    if (d.abi_version != D2F_ABI_VERSION) return fail(D2F_EINVAL, "d2f: ABI version mismatch");
-    if (d.precision != D2F_FP64 && d.precision != D2F_MIXED) return fail(D2F_EINVAL, "d2f: unknown precision mode");
-    if (d.n_scenes <= 0 || d.N <= 0 || d.T <= 0) return fail(D2F_EINVAL, "d2f: empty scene");
-    if (d.n_col < 0 || d.n_col > d2f::MAX_COL) return fail(D2F_EINVAL, "d2f: at most 16 colliders");
-    if (!d.segs || !d.x || !d.v || !d.xn || !d.xhat || !d.grad || !d.grad_prev || !d.p || !d.diagH ||
-        !d.mass || !d.free_mask || !d.inc_ptr || !d.inc || !d.node_bslot || !d.node_bc || !d.node_aff ||
-        !d.node_rig || !d.tri || !d.Bm || !d.area || !d.mu || !d.lam || !d.iters || !d.active || !d.status)
-        return fail(D2F_EINVAL, "d2f: a required device pointer is null");
-    if (scratch && (!d.escr || !d.ecache || !d.work)) return fail(D2F_EINVAL, "d2f: a scratch pointer is null");
-    if (d.Nb > 0 && !d.bnd) return fail(D2F_EINVAL, "d2f: boundary nodes without bnd[]");
-    if (d.n_col > 0 && !d.colliders) return fail(D2F_EINVAL, "d2f: colliders pointer is null");
-    if (d.n_bc > 0 && (!d.bc_idx || !d.bc_target)) return fail(D2F_EINVAL, "d2f: kinematic arrays missing");
-    if (d.Ne > 0 && (!d.ea || !d.eb || !d.ela || !d.elb || !d.ca || !d.cb || !d.excl_ptr || !d.excl_idx ||
-                     d.cand_total <= 0))
-        return fail(D2F_EINVAL, "d2f: IPC arrays missing");
-    if (d.Ne > 0 && scratch && (!d.cand || !d.xref)) return fail(D2F_EINVAL, "d2f: IPC scratch missing");
-    if (d.Ne > 0 && (d.max_nb <= 0 || d.max_nb > 24 * 1024))
-        return fail(D2F_EINVAL, "d2f: max_nb must be in 1..24576 with IPC contact");
-    if (d.n_rig > 0 && (!d.diag_el || !d.r_node || !d.r_grp || !d.r_acc || !d.r_zq))
-        return fail(D2F_EINVAL, "d2f: rigid-mode arrays missing");
-    if (d.n_aff > 0 && (!d.a_node || !d.a_grp || !d.a_w || !d.a_Mu || !d.a_La || !d.a_q || !d.a_pq ||
-                        !d.a_gq || !d.a_gq_prev || !d.a_zq || !d.a_H))
-        return fail(D2F_EINVAL, "d2f: affine arrays missing");
-    if (d.n_ten > 0 && (!d.t_node || !d.t_prv || !d.t_nxt || !d.t_tid || !d.t_stiff || !d.t_L0 ||
-                        !d.t_Tcmd || !d.t_state))
-        return fail(D2F_EINVAL, "d2f: tendon arrays missing");
-    if (!(d.dt > 0.0) || d.iter_max < 0) return fail(D2F_EINVAL, "d2f: dt must be > 0, iter_max >= 0");
-    int nt = d.threads ? d.threads : 256;
-    if (nt != 128 && nt != 256 && nt != 512) return fail(D2F_EINVAL, "d2f: threads must be 128, 256 or 512");
-    return D2F_OK;
-}
-
-// Grid (scene blocks) and dynamic shared memory of a launch on the current device.
-static int launch_shape(const d2f_scene_desc &d, int *grid, int *smem) {
-    *smem = d.Ne > 0 ? d.max_nb * (int)sizeof(float2) : 0;
-    int dev = 0, nsm = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        return fail(D2F_ECUDA, "d2f: no CUDA device");
-    const int nt = d.threads ? d.threads : 256;
-    const bool mixed = d.precision == D2F_MIXED;
-    int occ = 1;
-    if (nt == 128) occ = mixed ? occupancy<float, 128>(*smem) : occupancy<double, 128>(*smem);
-    else if (nt == 256) occ = mixed ? occupancy<float, 256>(*smem) : occupancy<double, 256>(*smem);
-    else occ = mixed ? occupancy<float, 512>(*smem) : occupancy<double, 512>(*smem);
-    int bps = d.blocks_per_sm > 0 ? (d.blocks_per_sm < occ ? d.blocks_per_sm : occ) : occ;
-    *grid = nsm * bps;
-    if (*grid > d.n_scenes) *grid = d.n_scenes;
-    return D2F_OK;
-}
-
-static cudaError_t launch(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
-    const bool mixed = d.precision == D2F_MIXED;
-    switch (d.threads ? d.threads : 256) {
-        case 128: return mixed ? launch_one<float, 128>(d, grid, smem, st) : launch_one<double, 128>(d, grid, smem, st);
-        case 512: return mixed ? launch_one<float, 512>(d, grid, smem, st) : launch_one<double, 512>(d, grid, smem, st);
-        default: return mixed ? launch_one<float, 256>(d, grid, smem, st) : launch_one<double, 256>(d, grid, smem, st);
-    }
-}
-
-extern "C" {
-
-int32_t d2f_create(const d2f_scene_desc *desc, d2f_solver **out) {
-    g_err[0] = 0;
-    if (!desc || !out) return fail(D2F_EINVAL, "d2f_create: null argument");
-    int rc = validate(*desc, true);
-    if (rc != D2F_OK) return rc;
-    d2f_solver *s = new d2f_solver();
-    s->d = *desc;
-    s->d.threads = desc->threads ? desc->threads : 256;
-    rc = launch_shape(s->d, &s->grid, &s->smem);
-    if (rc != D2F_OK) {
-        delete s;
-        return rc;
-    }
-    *out = s;
-    return D2F_OK;
-}
-
-int32_t d2f_step(d2f_solver *s, void *stream) {
-    if (!s) return fail(D2F_EINVAL, "d2f_step: null handle");
-    cudaStream_t st = (cudaStream_t)stream;
-    if (cudaMemsetAsync(s->d.work, 0, 4 * sizeof(int32_t), st) != cudaSuccess)
-        return fail(D2F_ECUDA, "d2f_step: cudaMemsetAsync failed");
-    cudaError_t e = launch(s->d, s->grid, s->smem, st);
-    if (e != cudaSuccess) {
-        snprintf(g_err, sizeof g_err, "d2f_step: launch failed: %s", cudaGetErrorString(e));
-        return D2F_ECUDA;
-    }
-    return D2F_OK;
-}
-
-int32_t d2f_set_dt(d2f_solver *s, double dt, int32_t iter_max) {
-    if (!s) return fail(D2F_EINVAL, "d2f_set_dt: null handle");
-    if (!(dt > 0.0) || iter_max < 0) return fail(D2F_EINVAL, "d2f_set_dt: dt must be > 0, iter_max >= 0");
-    s->d.dt = dt;
-    s->d.iter_max = iter_max;
-    return D2F_OK;
-}
-
-int32_t d2f_stats(d2f_solver *s, void *stream, int32_t *iters, int32_t *active, int32_t *status) {
-    if (!s) return fail(D2F_EINVAL, "d2f_stats: null handle");
-    cudaStream_t st = (cudaStream_t)stream;
-    size_t n = (size_t)s->d.n_scenes * sizeof(int32_t);
-    if ((iters && cudaMemcpyAsync(iters, s->d.iters, n, cudaMemcpyDeviceToHost, st) != cudaSuccess) ||
-        (active && cudaMemcpyAsync(active, s->d.active, n, cudaMemcpyDeviceToHost, st) != cudaSuccess) ||
-        (status && cudaMemcpyAsync(status, s->d.status, n, cudaMemcpyDeviceToHost, st) != cudaSuccess))
-        return fail(D2F_ECUDA, "d2f_stats: copy failed");
-    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(D2F_ECUDA, "d2f_stats: stream sync failed");
-    return D2F_OK;
-}
-
-int32_t d2f_destroy(d2f_solver *s) {
-    delete s;
-    return D2F_OK;
-}
-
-int32_t d2f_kernels_per_step(const d2f_solver *s) { return s ? 1 : 0; }
-
-}  // extern "C"
-
-// ============================================================================ step without allocation
-// Some callers cannot call cudaMalloc: code running inside a host that forbids device
-// allocation after start-up (a real-time control loop, a plugin whose host owns every
-// device buffer and hands it plain pointers, a process whose memory is already reserved).
-// d2f_step_noalloc gives them the same step with no allocation anywhere: the per-triangle
-// scratch, the contact-candidate lists, the boundary reference positions and the scene
-// queue head come from one file-scope device array instead of caller buffers. Every GPU
-// that loads this library holds that array (D2F_NOALLOC_SCRATCH_BYTES) until the process
-// exits. The array is shared by every call on a device and keeps the last call's contents;
-// the queue head is cleared on each call and everything else is rewritten before it is
-// read, so no state carries over. Calls whose work overlaps on the GPU (different streams,
-// or different threads) race on it: serialise them.
-#include <mutex>
-
-static __device__ __align__(256) unsigned char d2f_noalloc_scratch[D2F_NOALLOC_SCRATCH_BYTES];
-
-namespace {
-constexpr int kMaxDevices = 64;
-void *g_noalloc_base[kMaxDevices];
-std::mutex g_noalloc_mu;
-inline size_t round256(size_t n) { return (n + 255) & ~(size_t)255; }
-}  // namespace
-
-extern "C" int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream) {
-    g_err[0] = 0;
-    if (!desc) return fail(D2F_EINVAL, "d2f_step_noalloc: null descriptor");
-    int rc = validate(*desc, false);
-    if (rc != D2F_OK) return rc;
-    const d2f_scene_desc &in = *desc;
-    const size_t rsz = in.precision == D2F_MIXED ? sizeof(float) : sizeof(double);
-    const size_t b_work = round256(4 * sizeof(int32_t));
-    const size_t b_escr = round256((size_t)in.T * 12 * rsz);
-    const size_t b_ecache = round256((size_t)in.T * 9 * rsz);
-    const size_t b_cand = in.Ne > 0 ? round256((size_t)in.cand_total * sizeof(int32_t)) : 0;
-    const size_t b_xref = in.Ne > 0 ? round256((size_t)in.Nb * 2 * sizeof(double)) : 0;
-    const size_t need = b_work + b_escr + b_ecache + b_cand + b_xref;
-    if (need > (size_t)D2F_NOALLOC_SCRATCH_BYTES) {
-        snprintf(g_err, sizeof g_err,
-                 "d2f_step_noalloc: this batch needs %zu bytes of scratch (%d triangles, %d candidate "
-                 "slots, %d boundary nodes); the static scratch holds %zu bytes. Use d2f_create/d2f_step "
-                 "with caller-allocated scratch for batches this large.",
-                 need, in.T, in.cand_total, in.Nb, (size_t)D2F_NOALLOC_SCRATCH_BYTES);
-        return D2F_EINVAL;
-    }
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return fail(D2F_ECUDA, "d2f_step_noalloc: no current CUDA device");
-    if (dev < 0 || dev >= kMaxDevices) return fail(D2F_EINVAL, "d2f_step_noalloc: device index out of range");
-    void *base = nullptr;
-    {
-        // set-up, once per device, with that device current: the host-side name of a
-        // __device__ array is not its device address; ask the runtime for the address.
-        std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_base[dev]) {
-            void *p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, d2f_noalloc_scratch);
-            if (e != cudaSuccess || !p) {
-                snprintf(g_err, sizeof g_err, "d2f_step_noalloc: cudaGetSymbolAddress failed: %s",
-                         cudaGetErrorString(e));
-                return D2F_ECUDA;
-            }
-            g_noalloc_base[dev] = p;
-        }
-        base = g_noalloc_base[dev];
-    }
-    d2f_scene_desc d = in;
-    unsigned char *q = static_cast<unsigned char *>(base);
-    d.work = reinterpret_cast<int32_t *>(q); q += b_work;
-    d.escr = q; q += b_escr;
-    d.ecache = q; q += b_ecache;
-    d.cand = in.Ne > 0 ? reinterpret_cast<int32_t *>(q) : nullptr; q += b_cand;
-    d.xref = in.Ne > 0 ? reinterpret_cast<double *>(q) : nullptr;
-    d.threads = in.threads ? in.threads : 256;
-    int grid = 0, smem = 0;
-    rc = launch_shape(d, &grid, &smem);
-    if (rc != D2F_OK) return rc;
-    cudaStream_t st = (cudaStream_t)stream;
-    if (cudaMemsetAsync(d.work, 0, 4 * sizeof(int32_t), st) != cudaSuccess)  // the queue head starts at 0
-        return fail(D2F_ECUDA, "d2f_step_noalloc: cudaMemsetAsync failed");
-    cudaError_t e = launch(d, grid, smem, st);
-    if (e != cudaSuccess) {
-        snprintf(g_err, sizeof g_err, "d2f_step_noalloc: launch failed: %s", cudaGetErrorString(e));
-        return D2F_ECUDA;
-    }
-    return D2F_OK;
-}
+namespace d2f {
+// one translation unit per precision instantiates the variants (pncg_fp64.cu, pncg_mixed.cu)
+cudaError_t launch_fp64(int nt, int minb, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st);
+cudaError_t launch_mixed(int nt, int minb, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st);
+int occupancy_fp64(int nt, int minb, int smem);
+int occupancy_mixed(int nt, int minb, int smem);
+}  // namespace d2f

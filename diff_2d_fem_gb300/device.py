@@ -183,6 +183,12 @@ class DeviceSolver:
         self.x = T_("x", x, f64)
         self.v = T_("v", np.asarray(prob.get("v", np.zeros_like(x)), np.float64), f64)
         self.xn = T_("xn", np.zeros_like(x), f64)
+        if self.mixed:
+            # the FP32 element routine works on displacements from the rest shape
+            rest = np.asarray(prob.get("rest", x), np.float64)
+            T_("xrest", rest, f64)
+            T_("xu", x - rest, f64)
+            T_("Dm", np.concatenate([rest[tri[:, 1]] - rest[tri[:, 0]], rest[tri[:, 2]] - rest[tri[:, 0]]], 1), rdt)
         self.xhat = T_("xhat", np.zeros_like(x), f64)
         for nm in ("grad", "grad_prev", "p", "diagH", "diag_el"):
             T_(nm, np.zeros((N, 2)), rdt)
@@ -193,6 +199,12 @@ class DeviceSolver:
             T_("fext", fext, f64)
         T_("inc_ptr", inc_ptr, i32)
         T_("inc", order, i32)
+        inc8 = np.full((N, 8), -1, np.int64)
+        cnt = np.diff(inc_ptr)
+        slot = np.arange(len(order)) - np.repeat(inc_ptr[:-1], cnt)
+        first8 = slot < 8
+        inc8[np.repeat(np.arange(N), cnt)[first8], slot[first8]] = order[first8]
+        T_("inc8", inc8, i32)
         T_("node_bslot", node_bslot, i32)
         T_("node_bc", node_bc, i32)
         T_("node_aff", node_aff, i32)
@@ -222,6 +234,7 @@ class DeviceSolver:
             if ipc.get("mu_node") is not None and ipc.get("per_body", 1):
                 T_("mu_node", ipc["mu_node"], f64)
             T_("cand", np.zeros(max(cand_total, 1)), i32)
+            T_("cand_tr", np.zeros((max(cand_total, 1), 2)), f64)
             T_("xref", np.zeros((Nb, 2)), f64)
         if td is not None:
             for nm, key in (("t_node", "node"), ("t_prv", "prv"), ("t_nxt", "nxt"), ("t_tid", "tid")):

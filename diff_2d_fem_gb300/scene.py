@@ -185,7 +185,8 @@ def solver_problem(model, integ, dt):
     mu_s = np.asarray(me.mu, np.float64).copy()
     lam_s = np.asarray(me.lam, np.float64).copy()
     prob = dict(
-        B=int(me.n_envs), x=x, v=v, mass=np.asarray(me.mass, np.float64), free=free,
+        B=int(me.n_envs), x=x, v=v, rest=np.asarray(me.rest_pos, np.float64),
+        mass=np.asarray(me.mass, np.float64), free=free,
         node2env=np.asarray(me.node2env, np.int64), tri=np.asarray(me.tri, np.int64),
         Bm=np.asarray(me.D_m_inv, np.float64), area=np.asarray(me.rest_area, np.float64),
         mu=mu_s, lam=lam_s, tri2env=np.asarray(me.tri2env, np.int64),

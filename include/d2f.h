@@ -66,12 +66,15 @@ typedef struct d2f_scene_desc {
     const d2f_seg *segs;         /* n_scenes */
     /* node state */
     double *x, *v, *xn, *xhat;   /* N x 2 */
+    double *xu;                  /* N x 2: x - rest (mixed precision; else NULL) */
+    const double *xrest;         /* N x 2: rest positions (mixed precision; else NULL) */
     void *grad, *grad_prev, *p, *diagH, *diag_el; /* N x 2 real */
     const double *mass;          /* N */
     const uint8_t *free_mask;    /* N: bit 0 = x free, bit 1 = y free */
     const double *fext;          /* N x 2, or NULL: the ExternalForce term (gravity folded in) */
     const int32_t *inc_ptr;      /* N + 1: CSR of the triangles at each node */
     const int32_t *inc;          /* 3 T: 3 * triangle + corner, ascending triangle per node */
+    const int32_t *inc8;         /* N x 8: the first 8 entries of each node's inc list, -1 padded */
     const int32_t *node_bslot;   /* N: boundary slot of the node, or -1 */
     const int32_t *node_bc;      /* N: kinematic slot of the node, or -1 */
     const int32_t *node_aff;     /* N: affine node entry of the node, or -1 */
@@ -80,6 +83,7 @@ typedef struct d2f_scene_desc {
     const int32_t *tri;          /* T x 3 */
     const void *Bm;              /* T x 4 real: rest-shape inverse, row-major */
     const void *area, *mu, *lam; /* T real */
+    const void *Dm;              /* T x 4 real: rest edge vectors X1-X0, X2-X0 (mixed; else NULL) */
     void *escr;                  /* T x 12 real: per-corner gradient and diagonal */
     void *ecache;                /* T x 9 real: F^-T, la log J - mu, edge vectors */
     /* boundary nodes and colliders */
@@ -94,7 +98,8 @@ typedef struct d2f_scene_desc {
     const double *ca, *cb;       /* Ne */
     const int32_t *excl_ptr, *excl_idx; /* CSR over boundary slots: excluded local slots, sorted */
     const double *mu_node;       /* N, or NULL: per-body friction (harmonic mean per pair) */
-    int32_t *cand;               /* cand_total: packed (edge local << 16 | slot local) */
+    int32_t *cand;               /* cand_total: packed (edge local << 16 | slot local), sorted */
+    double *cand_tr;             /* cand_total x 2: per-pair ACCD profile of the current pass */
     double *xref;                /* Nb x 2: positions the candidate list was built at */
     /* tendons */
     const int32_t *t_node, *t_prv, *t_nxt, *t_tid; /* n_tent (prv/nxt/tid are global) */
@@ -118,7 +123,8 @@ typedef struct d2f_scene_desc {
     double ipc_mu, ipc_dhat, ipc_kappa, reach, gap, bc_floor, skin;
     int32_t iter_max, conv_check, friction, per_body;
     int32_t threads;             /* threads per scene block: 128, 256 or 512 (0: 256) */
-    int32_t blocks_per_sm;       /* resident scene blocks per SM (0: library default) */
+    int32_t blocks_per_sm;       /* resident scene blocks per SM the register budget targets
+                                    (0: the library's default for that width) */
 } d2f_scene_desc;
 
 typedef struct d2f_solver d2f_solver;
@@ -163,7 +169,7 @@ int32_t d2f_kernels_per_step(const d2f_solver *s);
 /* One implicit step of every scene, like d2f_step, for callers that cannot allocate
  * device memory (a host that forbids cudaMalloc after start-up, a plugin handed plain
  * pointers by its host). No handle and no allocation: the caller passes the descriptor
- * with its inputs and outputs; the scratch fields (escr, ecache, cand, xref, work) are
+ * with its inputs and outputs; the scratch fields (escr, ecache, cand, cand_tr, xref, work) are
  * ignored and taken from a static device array of D2F_NOALLOC_SCRATCH_BYTES that every
  * GPU loading the library holds until exit. A batch needing more scratch than that is
  * refused with D2F_EINVAL and a message. The first call on a device looks up the array's

@@ -51,11 +51,11 @@ def test_create_rejects_bad_descriptors_without_a_gpu():
 def test_struct_mirrors_header():
     """Every field of d2f_scene_desc / d2f_seg in the header appears in the ctypes mirror in
     the same order."""
-    txt = open(HDR).read()
+    txt = re.sub(r"/\*.*?\*/", "", open(HDR).read(), flags=re.S)
     body = txt[txt.index("typedef struct d2f_scene_desc {"):txt.index("} d2f_scene_desc;")]
     names = []
     for line in body.splitlines()[1:]:
-        line = line.split("/*")[0].strip()
+        line = line.strip()
         if not line:
             continue
         decl = re.sub(r"^(const\s+)?[a-z0-9_]+\s+", "", line.rstrip(";"))
@@ -64,7 +64,7 @@ def test_struct_mirrors_header():
     seg = txt[txt.index("typedef struct d2f_seg {"):txt.index("} d2f_seg;")]
     sn = []
     for line in seg.splitlines()[1:]:
-        line = line.split("/*")[0].strip().rstrip(";")
+        line = line.strip().rstrip(";")
         if line:
             sn += [v.strip() for v in re.sub(r"^int32_t\s+", "", line).split(",")]
     assert sn == [n for n, _ in _lib.Seg._fields_]

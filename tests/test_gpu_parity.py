@@ -48,13 +48,19 @@ def test_fp64_matches_reference(name):
         assert e < TOL_FP64, f"{name} step {k}: rel err {e:.3e} (iters {it.tolist()} vs {st['iters'].tolist()})"
 
 
-@pytest.mark.parametrize("name", ["strip_small", "strip_cfg1", "grip"])
-def test_mixed_close_to_fp64(name):
+@pytest.mark.parametrize("name", ["strip_small", "strip_cfg1", "grip", "tendon"])
+def test_mixed_close_to_fp64_when_converged(name):
+    """Mixed precision against FP64 on CONVERGED steps: the iteration cap is lifted so both
+    run to the reference's energy tolerance; a step cut off by the cap stops at an iterate
+    that depends on the rounding of every earlier iteration, in either precision."""
     prob, steps, _ = load_fixture(name)
-    res = _run_device(prob, steps, "mixed")
-    for k, ((x, it), st) in enumerate(zip(res, steps)):
-        e = rel_err(x, st["x"])
-        assert e < TOL_MIXED, f"{name} step {k}: rel err {e:.3e}"
+    prob = dict(prob)
+    prob["iter_max"] = 3000
+    r64 = _run_device(prob, steps, "fp64")
+    rmx = _run_device(prob, steps, "mixed")
+    for k, ((x64, _), (xmx, it)) in enumerate(zip(r64, rmx)):
+        e = rel_err(xmx, x64)
+        assert e < TOL_MIXED, f"{name} step {k}: rel err {e:.3e} (iters {it.tolist()})"
 
 
 def test_config1_strip_200_steps_matches_oracle():
