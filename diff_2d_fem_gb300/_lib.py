@@ -31,7 +31,7 @@ DESC_FIELDS = (
     + [(n, _P) for n in (
         "segs", "x", "v", "xn", "xhat", "xu", "xrest", "grad", "grad_prev", "p", "diagH", "diag_el", "mass", "free_mask",
         "fext", "inc_ptr", "inc", "inc8", "node_bslot", "node_bc", "node_aff", "node_rig", "tri", "Bm", "area", "mu",
-        "lam", "Dm", "escr", "ecache", "bnd", "colliders", "col_mu_env", "bc_idx", "bc_target", "ea", "eb", "ela",
+        "lam", "Dm", "escr", "ecache", "mscr", "bnd", "colliders", "col_mu_env", "bc_idx", "bc_target", "ea", "eb", "ela",
         "elb", "ca", "cb", "excl_ptr", "excl_idx", "mu_node", "cand", "cand_tr", "xref", "t_node", "t_prv", "t_nxt",
         "t_tid", "t_stiff", "t_L0", "t_Tcmd", "t_state", "a_node", "a_grp", "a_w", "a_Mu", "a_La", "a_q",
         "a_pq", "a_gq", "a_gq_prev", "a_zq", "a_H", "r_node", "r_grp", "r_acc", "r_zq", "iters", "active",
@@ -48,7 +48,7 @@ class SceneDesc(C.Structure):
 
 
 EXPORTS = ("d2f_abi_version", "d2f_create", "d2f_step", "d2f_set_dt", "d2f_stats", "d2f_destroy",
-           "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc")
+           "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc", "d2f_mixed_scratch_bytes")
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
@@ -83,6 +83,8 @@ def load(build_if_missing: bool = True):
     L.d2f_kernels_per_step.restype = _I
     L.d2f_step_noalloc.argtypes = [C.POINTER(SceneDesc), _P]
     L.d2f_step_noalloc.restype = _I
+    L.d2f_mixed_scratch_bytes.argtypes = [_I, _I, _I, _I, _I]
+    L.d2f_mixed_scratch_bytes.restype = C.c_size_t
     if L.d2f_abi_version() != D2F_ABI_VERSION:
         raise RuntimeError("libd2f.so ABI version mismatch; rebuild it")
     _LIB = L

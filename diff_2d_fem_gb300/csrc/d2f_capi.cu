@@ -20,22 +20,18 @@ static int fail(int code, const char *msg) {
     return code;
 }
 
-// the variant for (threads, blocks_per_sm): the largest MINB <= blocks_per_sm (1 if 0)
+// The built variant for (threads, blocks_per_sm): an exact match, else the first variant of
+// that width, else (128, 4).
 static void pick_variant(int nt, int bps, int *vnt, int *vminb) {
-    int best_nt = 256, best_mb = 2;
-    bool found = false;
-#define D2F_PICK(N, MB) \
-    if (N == nt && MB <= (bps > 0 ? bps : 2) && (!found || MB > best_mb)) { best_nt = N; best_mb = MB; found = true; }
+    int fnt = 0, fmb = 0;
+#define D2F_PICK(N, MB)                               \
+    if (N == nt && MB == bps) { *vnt = N; *vminb = MB; return; } \
+    if (N == nt && !fnt) { fnt = N; fmb = MB; }
     D2F_VARIANTS(D2F_PICK)
 #undef D2F_PICK
-    if (!found) {  // no variant for nt: the smallest MINB of that width, or the default
-        best_nt = 256; best_mb = 2;
-#define D2F_FIRST(N, MB) if (N == nt && !found) { best_nt = N; best_mb = MB; found = true; }
-        D2F_VARIANTS(D2F_FIRST)
-#undef D2F_FIRST
-    }
-    *vnt = best_nt;
-    *vminb = best_mb;
+    if (fnt) { *vnt = fnt; *vminb = fmb; return; }
+    *vnt = 128;
+    *vminb = 4;
 }
 
 static int occupancy(const d2f_scene_desc &d, int smem, int vnt, int vminb) {
@@ -62,8 +58,9 @@ static int validate(const d2f_scene_desc &d, bool scratch) {
         !d.node_rig || !d.tri || !d.Bm || !d.area || !d.mu || !d.lam || !d.iters || !d.active || !d.status)
         return fail(D2F_EINVAL, "d2f: a required device pointer is null");
     if (scratch && (!d.escr || !d.ecache || !d.work)) return fail(D2F_EINVAL, "d2f: a scratch pointer is null");
-    if (d.precision == D2F_MIXED && (!d.xu || !d.xrest || !d.Dm))
-        return fail(D2F_EINVAL, "d2f: mixed precision needs xu, xrest and Dm");
+    if (d.precision == D2F_MIXED && (!d.xrest || !d.Dm))
+        return fail(D2F_EINVAL, "d2f: mixed precision needs xrest and Dm");
+    if (d.precision == D2F_MIXED && scratch && !d.mscr) return fail(D2F_EINVAL, "d2f: mixed precision needs mscr");
     if (d.Nb > 0 && !d.bnd) return fail(D2F_EINVAL, "d2f: boundary nodes without bnd[]");
     if (d.n_col > 0 && !d.colliders) return fail(D2F_EINVAL, "d2f: colliders pointer is null");
     if (d.n_bc > 0 && (!d.bc_idx || !d.bc_target)) return fail(D2F_EINVAL, "d2f: kinematic arrays missing");
@@ -82,8 +79,8 @@ static int validate(const d2f_scene_desc &d, bool scratch) {
                         !d.t_Tcmd || !d.t_state))
         return fail(D2F_EINVAL, "d2f: tendon arrays missing");
     if (!(d.dt > 0.0) || d.iter_max < 0) return fail(D2F_EINVAL, "d2f: dt must be > 0, iter_max >= 0");
-    int nt = d.threads ? d.threads : 256;
-    if (nt != 128 && nt != 256 && nt != 512) return fail(D2F_EINVAL, "d2f: threads must be 128, 256 or 512");
+    int nt = d.threads ? d.threads : 128;
+    if (nt != 32 && nt != 64 && nt != 128 && nt != 256) return fail(D2F_EINVAL, "d2f: threads must be 32, 64, 128 or 256");
     if (!d.inc8) return fail(D2F_EINVAL, "d2f: inc8 (padded node-corner table) is null");
     return D2F_OK;
 }
@@ -95,7 +92,7 @@ static int launch_shape(const d2f_scene_desc &d, int *grid, int *smem) {
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return fail(D2F_ECUDA, "d2f: no CUDA device");
     int vnt, vminb;
-    pick_variant(d.threads ? d.threads : 256, d.blocks_per_sm, &vnt, &vminb);
+    pick_variant(d.threads ? d.threads : 128, d.blocks_per_sm, &vnt, &vminb);
     const int occ = occupancy(d, *smem, vnt, vminb);
     const int bps = d.blocks_per_sm > 0 ? (d.blocks_per_sm < occ ? d.blocks_per_sm : occ) : occ;
     *grid = nsm * bps;
@@ -105,7 +102,7 @@ static int launch_shape(const d2f_scene_desc &d, int *grid, int *smem) {
 
 static cudaError_t launch(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
     int vnt, vminb;
-    pick_variant(d.threads ? d.threads : 256, d.blocks_per_sm, &vnt, &vminb);
+    pick_variant(d.threads ? d.threads : 128, d.blocks_per_sm, &vnt, &vminb);
     return d.precision == D2F_MIXED ? d2f::launch_mixed(vnt, vminb, d, grid, smem, st)
                                     : d2f::launch_fp64(vnt, vminb, d, grid, smem, st);
 }
@@ -119,7 +116,7 @@ int32_t d2f_create(const d2f_scene_desc *desc, d2f_solver **out) {
     if (rc != D2F_OK) return rc;
     d2f_solver *s = new d2f_solver();
     s->d = *desc;
-    s->d.threads = desc->threads ? desc->threads : 256;
+    s->d.threads = desc->threads ? desc->threads : 128;
     rc = launch_shape(s->d, &s->grid, &s->smem);
     if (rc != D2F_OK) {
         delete s;
@@ -207,7 +204,9 @@ extern "C" int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream) {
     const size_t b_cand = in.Ne > 0 ? round256((size_t)in.cand_total * sizeof(int32_t)) : 0;
     const size_t b_ctr = in.Ne > 0 ? round256((size_t)in.cand_total * 2 * sizeof(double)) : 0;
     const size_t b_xref = in.Ne > 0 ? round256((size_t)in.Nb * 2 * sizeof(double)) : 0;
-    const size_t need = b_work + b_escr + b_ecache + b_cand + b_ctr + b_xref;
+    const size_t b_mscr = in.precision == D2F_MIXED
+                              ? round256(d2f_mixed_scratch_bytes(in.N, in.T, in.Nb, in.n_col, in.n_rig)) : 0;
+    const size_t need = b_work + b_escr + b_ecache + b_cand + b_ctr + b_xref + b_mscr;
     if (need > (size_t)D2F_NOALLOC_SCRATCH_BYTES) {
         snprintf(g_err, sizeof g_err,
                  "d2f_step_noalloc: this batch needs %zu bytes of scratch (%d triangles, %d candidate "
@@ -243,8 +242,9 @@ extern "C" int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream) {
     d.ecache = q; q += b_ecache;
     d.cand = in.Ne > 0 ? reinterpret_cast<int32_t *>(q) : nullptr; q += b_cand;
     d.cand_tr = in.Ne > 0 ? reinterpret_cast<double *>(q) : nullptr; q += b_ctr;
-    d.xref = in.Ne > 0 ? reinterpret_cast<double *>(q) : nullptr;
-    d.threads = in.threads ? in.threads : 256;
+    d.xref = in.Ne > 0 ? reinterpret_cast<double *>(q) : nullptr; q += b_xref;
+    d.mscr = in.precision == D2F_MIXED ? q : nullptr;
+    d.threads = in.threads ? in.threads : 128;
     int grid = 0, smem = 0;
     rc = launch_shape(d, &grid, &smem);
     if (rc != D2F_OK) return rc;

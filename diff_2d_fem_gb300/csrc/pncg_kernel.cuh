@@ -98,6 +98,7 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const int (&ops)[N
 struct SceneSh {
     double alpha, pHp, gTp, beta, p_inf, clr_min, dE0, gn0, q_inf, alpha_s, dispmax;
     double gPg, g_p, g_Py, y_p, y_Py, gn2;
+    double motion, csx, csy, mpx, mpy;  // mixed path: motion since the candidate build, centroid shift
     int active, pending, iters, ncand, count, status, rebuild;
 };
 
@@ -1165,7 +1166,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
 // Launch shapes the library is built with: (threads per scene block, minimum resident
 // blocks per SM the register budget is fitted to). d2f_scene_desc.threads / blocks_per_sm
 // select one; the autotuner (tune.py) measures them.
-#define D2F_VARIANTS(X) X(128, 4) X(256, 1) X(256, 2) X(256, 3) X(512, 1)
+#define D2F_VARIANTS(X) X(32, 16) X(64, 8) X(128, 4) X(256, 3)
 
 namespace d2f {
 // one translation unit per precision instantiates the variants (pncg_fp64.cu, pncg_mixed.cu)

@@ -1,11 +1,11 @@
-// pncg_mixed.cu — the step kernel instantiated for the mixed FP32/FP64 path.
-#include "pncg_kernel.cuh"
+// pncg_mixed.cu — the mixed FP32/FP64 step kernel (pncg_mixed_kernel.cuh), instantiated.
+#include "pncg_mixed_kernel.cuh"
 
 namespace d2f {
 
 template <int NT, int MINB>
 static cudaError_t launch_v(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
-    auto k = pncg_step_kernel<float, NT, MINB>;
+    auto k = pncg_mixed_kernel<NT, MINB>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     k<<<grid, NT, smem, st>>>(d);
     return cudaGetLastError();
@@ -14,7 +14,7 @@ static cudaError_t launch_v(const d2f_scene_desc &d, int grid, int smem, cudaStr
 template <int NT, int MINB>
 static int occupancy_v(int smem) {
     int nb = 0;
-    auto k = pncg_step_kernel<float, NT, MINB>;
+    auto k = pncg_mixed_kernel<NT, MINB>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, NT, smem) != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
@@ -35,3 +35,7 @@ int occupancy_mixed(int nt, int minb, int smem) {
 }
 
 }  // namespace d2f
+
+extern "C" size_t d2f_mixed_scratch_bytes(int32_t N, int32_t T, int32_t Nb, int32_t n_col, int32_t n_rig) {
+    return d2f::mixed_layout(N, T, Nb, n_col, n_rig).total;
+}

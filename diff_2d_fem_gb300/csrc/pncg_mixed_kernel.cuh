@@ -1,0 +1,1257 @@
+// pncg_mixed_kernel.cuh — the mixed-precision implicit step: FP32 iterations on increments
+// from the step-start state, FP64 where the reference's accuracy argument needs it.
+//
+// GB300 executes FP64 at ~1/64 of its FP32 rate, so in this path an iteration performs
+// (almost) no FP64 instruction:
+//
+//   * positions: x = x_n + dx with x_n the FP64 state at the start of the step and dx an
+//     FP32 increment. Everything an iteration needs is formed from dx plus per-step
+//     quantities computed once in FP64:
+//       - triangles: F = I + H, H = (dU0 + dx-differences) B, dU0 = the FP64 edge
+//         differences of (x_n - X_rest) rounded once per step — so F is formed from FP64
+//         edge differences, and the first Piola stress is evaluated in the
+//         cancellation-free form mu((J-1)I + J H - cof H)/J + la log1p(J-1)(I + cof H)/J;
+//       - inertia: x - x_hat = dx - dt e^(-dt c) v;
+//       - half-space colliders: phi = phi0 + n.dx with phi0 = n.(x_n - c) in FP64 per step,
+//         so the barrier distance keeps FP64 accuracy near contact; other collider shapes,
+//         IPC pairs, tendons and affine bodies evaluate in FP64 from x_n + dx;
+//       - friction: slip velocity dx / dt;
+//       - rigid modes: arms r = (x_n - c_n) + dx - (c - c_n).
+//   * dot products: each thread accumulates its FP32 products with compensated (TwoSum)
+//     FP32 pairs, warps merge the pairs, and the per-warp partials are summed in FP64. The
+//     Dai-Kou beta, the step length, the convergence ratio and the energy model stay FP64.
+//   * step caps (inversion, CCD, |p|, clearance) are FP32 minima/maxima.
+// At the end of the step x = x_n + dx and v = (x - x_n)/dt in FP64.
+#pragma once
+#include <type_traits>
+
+#include "pncg_kernel.cuh"
+
+namespace d2f {
+
+// ---------------------------------------------------------------------- compensated FP32 sums
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF &a, float b) {  // Knuth TwoSum
+    const float s = a.hi + b;
+    const float bp = s - a.hi;
+    const float err = (a.hi - (s - bp)) + (b - bp);
+    a.hi = s;
+    a.lo += err;
+}
+__device__ __forceinline__ FF ff_merge(FF a, FF b) {
+    const float s = a.hi + b.hi;
+    const float bp = s - a.hi;
+    const float err = (a.hi - (s - bp)) + (b.hi - bp);
+    const float lo = err + a.lo + b.lo;
+    const float hi = s + lo;
+    return FF{hi, lo - (hi - s)};
+}
+
+// Block reduction: NS compensated sums (returned as FP64) and NM FP32 extrema
+// (ops 1 = max, 2 = min). Deterministic. `fred` holds NW*(2*NS+NM) floats, `dres` NS doubles,
+// `mres` NM floats.
+template <int NT, int NS, int NM>
+__device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], const int (&mops)[NM],
+                                                double (&out_s)[NS], float (&out_m)[NM], float *fred,
+                                                double *dres, float *mres) {
+    constexpr int NW = NT / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            FF b{__shfl_down_sync(0xffffffffu, s[k].hi, o), __shfl_down_sync(0xffffffffu, s[k].lo, o)};
+            s[k] = ff_merge(s[k], b);
+        }
+#pragma unroll
+        for (int k = 0; k < NM; ++k) {
+            const float b = __shfl_down_sync(0xffffffffu, m[k], o);
+            m[k] = mops[k] == 1 ? fmaxf(m[k], b) : fminf(m[k], b);
+        }
+    }
+    if (lane == 0) {
+        float *w = fred + warp * (2 * NS + NM);
+#pragma unroll
+        for (int k = 0; k < NS; ++k) { w[2 * k] = s[k].hi; w[2 * k + 1] = s[k].lo; }
+#pragma unroll
+        for (int k = 0; k < NM; ++k) w[2 * NS + k] = m[k];
+    }
+    __syncthreads();
+    // the per-warp partials: sum k by thread k (FP64), extremum k by thread NS + k
+    {
+        const int k = threadIdx.x;
+        if (k < NS) {
+            double acc = 0.0;
+            for (int q = 0; q < NW; ++q) acc += (double)fred[q * (2 * NS + NM) + 2 * k] + (double)fred[q * (2 * NS + NM) + 2 * k + 1];
+            dres[k] = acc;
+        } else if (k < NS + NM) {
+            const int j = k - NS;
+            float a = fred[2 * NS + j];
+            for (int q = 1; q < NW; ++q) {
+                const float b = fred[q * (2 * NS + NM) + 2 * NS + j];
+                a = mops[j] == 1 ? fmaxf(a, b) : fminf(a, b);
+            }
+            mres[j] = a;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NS; ++k) out_s[k] = dres[k];
+#pragma unroll
+    for (int k = 0; k < NM; ++k) out_m[k] = mres[k];
+    __syncthreads();
+}
+
+// Byte layout of the mixed path's per-step scratch (d2f_scene_desc.mscr), 256-aligned parts.
+struct MixedLayout {
+    size_t xd, xhv, fh, rarm, m32, du0, phi0, rcs, dref, total;
+};
+__host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, long n_col, long n_rig) {
+    auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    MixedLayout L;
+    size_t o = 0;
+    L.xd = o; o = up(o + (size_t)N * 8);
+    L.xhv = o; o = up(o + (size_t)N * 8);
+    L.fh = o; o = up(o + (size_t)N * 8);
+    L.rarm = o; o = up(o + (size_t)N * 8);
+    L.m32 = o; o = up(o + (size_t)N * 4);
+    L.du0 = o; o = up(o + (size_t)T * 16);
+    L.phi0 = o; o = up(o + (size_t)Nb * (n_col > 0 ? n_col : 1) * 4);
+    L.rcs = o; o = up(o + (size_t)(n_rig > 0 ? n_rig : 1) * 8);
+    L.dref = o; o = up(o + (size_t)(Nb > 0 ? Nb : 1) * 8);
+    L.total = o;
+    return L;
+}
+
+// ---------------------------------------------------------------------- the kernel
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_constant__ d2f_scene_desc d) {
+    constexpr int NW = NT / 32;
+    __shared__ SceneSh S;
+    __shared__ Col cols[MAX_COL];
+    __shared__ double red[NW * 20 + 20];
+    __shared__ float fred[NW * 40];
+    __shared__ double dres[20];
+    __shared__ float mres[8];
+    __shared__ int sc_next;
+    __shared__ int s_wcnt[NW];
+    __shared__ double s_H6[6][6], s_L6[6][6];
+    __shared__ double colmu[MAX_COL];
+    __shared__ float s_zf[8][3], s_cs[8][2];  // rigid-mode correction of up to 8 pieces, FP32
+    __shared__ float colf[MAX_COL][2], colmuf[MAX_COL];  // half-space normals, friction (FP32)
+    extern __shared__ float2 pos32[];
+
+    const int tid = threadIdx.x;
+    const double dt = d.dt, h2 = dt * dt, inv_dt = 1.0 / dt;
+    const double dhat = d.dhat;
+    const float fh2 = (float)h2, fkappa = (float)d.kappa, fdhat = (float)dhat, fepsv = (float)d.epsv,
+                finv_dt = (float)inv_dt, feta = (float)d.ccd_eta;
+    const bool has_ipc = d.Ne > 0;
+    const int n_col = d.n_col;
+
+    double2 *__restrict__ X = reinterpret_cast<double2 *>(d.x);
+    double2 *__restrict__ Xn = reinterpret_cast<double2 *>(d.xn);
+    double2 *__restrict__ Vv = reinterpret_cast<double2 *>(d.v);
+    float2 *__restrict__ G = reinterpret_cast<float2 *>(d.grad);
+    float2 *__restrict__ Gp = reinterpret_cast<float2 *>(d.grad_prev);
+    float2 *__restrict__ P = reinterpret_cast<float2 *>(d.p);
+    float2 *__restrict__ D = reinterpret_cast<float2 *>(d.diagH);
+    float2 *__restrict__ Del = reinterpret_cast<float2 *>(d.diag_el);
+    const float4 *__restrict__ Bm = reinterpret_cast<const float4 *>(d.Bm);
+    const float *__restrict__ Ar = reinterpret_cast<const float *>(d.area);
+    const float *__restrict__ Mu = reinterpret_cast<const float *>(d.mu);
+    const float *__restrict__ La = reinterpret_cast<const float *>(d.lam);
+    float4 *__restrict__ Esc = reinterpret_cast<float4 *>(d.escr);
+    float *__restrict__ Ec = reinterpret_cast<float *>(d.ecache);
+    const double2 *__restrict__ Fx = reinterpret_cast<const double2 *>(d.fext);
+    const double2 *__restrict__ Tgt = reinterpret_cast<const double2 *>(d.bc_target);
+    double2 *__restrict__ Ctr = reinterpret_cast<double2 *>(d.cand_tr);
+    const double2 *__restrict__ Xr = reinterpret_cast<const double2 *>(d.xrest);
+    const float4 *__restrict__ Dmr = reinterpret_cast<const float4 *>(d.Dm);
+    const MixedLayout ML = mixed_layout(d.N, d.T, d.Nb, d.n_col, d.n_rig);
+    unsigned char *ms = static_cast<unsigned char *>(d.mscr);
+    float2 *__restrict__ XD = reinterpret_cast<float2 *>(ms + ML.xd);     // x - x_n
+    float2 *__restrict__ XHV = reinterpret_cast<float2 *>(ms + ML.xhv);   // x_hat - x_n
+    float2 *__restrict__ FH = reinterpret_cast<float2 *>(ms + ML.fh);     // h^2 f
+    float2 *__restrict__ RARM = reinterpret_cast<float2 *>(ms + ML.rarm); // x_n - c_n (rigid pieces)
+    float *__restrict__ M32 = reinterpret_cast<float *>(ms + ML.m32);
+    float4 *__restrict__ DU0 = reinterpret_cast<float4 *>(ms + ML.du0);   // step-start displacement edges
+    float *__restrict__ PHI0 = reinterpret_cast<float *>(ms + ML.phi0);   // half-space distances at x_n
+    float2 *__restrict__ DREF = reinterpret_cast<float2 *>(ms + ML.dref); // dx when the candidate list was built
+    float2 *__restrict__ RCS = reinterpret_cast<float2 *>(ms + ML.rcs);   // rigid pieces: centroid shift
+
+    if (tid < n_col && tid < MAX_COL) {
+        const double *c = d.colliders + 8 * tid;
+        cols[tid] = Col{(int)c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7]};
+        colf[tid][0] = (float)c[3];
+        colf[tid][1] = (float)c[4];
+    }
+
+    for (;;) {
+        if (tid == 0) sc_next = atomicAdd(d.work, 1);
+        __syncthreads();
+        const int sc = sc_next;
+        if (sc >= d.n_scenes) break;
+        const d2f_seg sg = d.segs[sc];
+        const int n0 = sg.node0, n1 = sg.node0 + sg.nn;
+        const int t0 = sg.tri0, t1 = sg.tri0 + sg.nt;
+        const bool scene_ipc = has_ipc && sg.ne > 0;
+        const bool scene_rig = sg.nrig > 0;
+        const bool scene_rare = scene_ipc || sg.naff > 0 || sg.nten > 0;  // terms with FP64 contributions
+        const int nbl = sg.nb;
+        const double near = d.near_factor * dhat;
+        if (tid < n_col && tid < MAX_COL) {
+            colmu[tid] = d.col_mu_env ? d.col_mu_env[sc * n_col + tid] : cols[tid].mu;
+            colmuf[tid] = (float)colmu[tid];
+        }
+
+        auto xpos = [&](int n) -> double2 {  // FP64 position
+            const double2 a = Xn[n];
+            const float2 b = XD[n];
+            return make_double2(a.x + (double)b.x, a.y + (double)b.y);
+        };
+
+        // ================================================================ step setup (FP64, once per step)
+        for (int i = n0 + tid; i < n1; i += NT) {
+            const double2 xi = X[i], vi = Vv[i];
+            Xn[i] = xi;
+            XD[i] = make_float2(0.f, 0.f);
+            XHV[i] = make_float2((float)(dt * d.drag * vi.x), (float)(dt * d.drag * vi.y));
+            M32[i] = (float)d.mass[i];
+            if (d.fext) {
+                const double2 f = Fx[i];
+                FH[i] = make_float2((float)(h2 * f.x), (float)(h2 * f.y));
+            }
+            G[i] = make_float2(0.f, 0.f);
+            P[i] = make_float2(0.f, 0.f);
+        }
+        if (tid == 0) {
+            S.active = 1; S.iters = 0; S.dE0 = 0.0; S.status = 0; S.pending = 0;
+            S.alpha = d.alpha_max; S.pHp = 0.0; S.q_inf = 0.0; S.alpha_s = 1.0;
+            S.ncand = 0; S.rebuild = 1; S.gn0 = 0.0; S.beta = 0.0;
+            S.motion = 0.0; S.csx = 0.0; S.csy = 0.0;
+        }
+        __syncthreads();
+        for (int t = t0 + tid; t < t1; t += NT) {  // displacement edges at x_n, FP64 then rounded once
+            const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
+            const double2 a0 = Xn[i0], a1 = Xn[i1], a2 = Xn[i2], r0 = Xr[i0], r1 = Xr[i1], r2 = Xr[i2];
+            DU0[t] = make_float4((float)((a1.x - a0.x) - (r1.x - r0.x)), (float)((a1.y - a0.y) - (r1.y - r0.y)),
+                                 (float)((a2.x - a0.x) - (r2.x - r0.x)), (float)((a2.y - a0.y) - (r2.y - r0.y)));
+        }
+        for (int j = tid; j < nbl; j += NT) {  // half-space distances at x_n
+            const double2 xb = Xn[d.bnd[sg.bnd0 + j]];
+            for (int k = 0; k < n_col; ++k) {
+                const Col c = cols[k];
+                if (c.kind == 4) PHI0[(size_t)(sg.bnd0 + j) * n_col + k] = (float)(c.rx * (xb.x - c.cx) + c.ry * (xb.y - c.cy));
+            }
+        }
+        if (!scene_ipc) {  // apply_bc_kernel, kernels.py:53-59: x = target
+            for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
+                const int n = d.bc_idx[b];
+                const double2 tg = Tgt[b], xn = Xn[n];
+                XD[n] = make_float2((float)(tg.x - xn.x), (float)(tg.y - xn.y));
+            }
+        }
+        // rigid pieces: step-start centroid c_n (FP64) and the arms x_n - c_n (FP32)
+        for (int b = sg.rig0; b < sg.rig0 + sg.nrig; ++b) {
+            double c[3] = {0.0, 0.0, 0.0};
+            for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
+                if (d.r_grp[k] != b) continue;
+                const int i = d.r_node[k];
+                const double m = d.mass[i];
+                const double2 xi = Xn[i];
+                c[0] += m * xi.x; c[1] += m * xi.y; c[2] += m;
+            }
+            const int ops3[3] = {0, 0, 0};
+            block_reduce<NT, 3>(c, ops3, red);
+            const double cx = c[0] / c[2], cy = c[1] / c[2];
+            for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
+                if (d.r_grp[k] != b) continue;
+                const int i = d.r_node[k];
+                const double2 xi = Xn[i];
+                RARM[i] = make_float2((float)(xi.x - cx), (float)(xi.y - cy));
+            }
+            if (tid == 0) { d.r_acc[3 * b] = cx; d.r_acc[3 * b + 1] = cy; d.r_acc[3 * b + 2] = c[2]; }
+        }
+        __syncthreads();
+
+        // ---------------------------------------------------------------- contact candidates
+        // As in the FP64 kernel, but the list is rebuilt at every step start (x_n changed) and
+        // its validity inside a step is the FP32 motion dx - dx_ref of the boundary nodes.
+        auto ipc_refresh = [&]() {
+            // rebuild when the nodes may have moved skin/2 since the last build: every node
+            // moves at most alpha |p|_inf per iteration (alpha_s q_inf per sweep), summed in
+            // S.motion — a bound, so no reduction over the nodes is needed
+            if (!(S.rebuild || 2.0 * S.motion >= d.skin)) return;
+            __syncthreads();
+            const double2 anchor = xpos(d.bnd[sg.bnd0]);
+            for (int j = tid; j < nbl; j += NT) {
+                const int n = d.bnd[sg.bnd0 + j];
+                const double2 xb = xpos(n);
+                DREF[sg.bnd0 + j] = XD[n];
+                pos32[j] = make_float2((float)(xb.x - anchor.x), (float)(xb.y - anchor.y));
+            }
+            if (tid == 0) S.count = 0;
+            __syncthreads();
+            const float rad = (float)(d.reach + d.skin);
+            const float slack = 1.0e-5f * rad;
+            const long npair = (long)sg.ne * nbl;
+            for (long base = 0; base < npair; base += NT) {
+                const long q = base + tid;
+                bool keep = false;
+                int k = 0, j = 0;
+                if (q < npair) {
+                    k = (int)(q / nbl);
+                    j = (int)(q - (long)k * nbl);
+                    const int ge = sg.edge0 + k;
+                    const int a = d.ea[ge], b = d.eb[ge];
+                    const int pn = d.bnd[sg.bnd0 + j];
+                    if (pn != a && pn != b) {
+                        const int la = d.node_bslot[a] - sg.bnd0, lb = d.node_bslot[b] - sg.bnd0;
+                        const float2 pa = pos32[la], pb = pos32[lb], pp = pos32[j];
+                        const float abx = pb.x - pa.x, aby = pb.y - pa.y;
+                        const float wx = pp.x - pa.x, wy = pp.y - pa.y;
+                        float t = (wx * abx + wy * aby) / fmaxf(abx * abx + aby * aby, 1e-30f);
+                        t = fminf(fmaxf(t, 0.f), 1.f);
+                        const float dx = wx - t * abx, dy = wy - t * aby;
+                        keep = sqrtf(dx * dx + dy * dy) <= rad + slack &&
+                               !excluded(d, sg.bnd0 + j, d.ela[ge]) && !excluded(d, sg.bnd0 + j, d.elb[ge]);
+                    }
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                const int lane = tid & 31, warp = tid >> 5;
+                if (lane == 0) s_wcnt[warp] = __popc(bal);
+                __syncthreads();
+                int off = S.count + __popc(bal & ((1u << lane) - 1u)), tot = 0;
+                for (int w = 0; w < NW; ++w) {
+                    if (w < warp) off += s_wcnt[w];
+                    tot += s_wcnt[w];
+                }
+                if (keep && off < sg.ncap) d.cand[sg.cand0 + off] = (int)(((unsigned)k << 16) | (unsigned)j);
+                __syncthreads();
+                if (tid == 0) S.count += tot;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                if (S.count > sg.ncap) { S.status = D2F_ECAP; S.ncand = sg.ncap; }
+                else S.ncand = S.count;
+                S.rebuild = 0;
+                S.motion = 0.0;
+            }
+            __syncthreads();
+        };
+
+        auto kin_dir = [&](int n) -> double2 {
+            const int b = d.node_bc[n];
+            if (b < 0) return make_double2(0.0, 0.0);
+            const double2 t = Tgt[b], x = xpos(n);
+            return make_double2(t.x - x.x, t.y - x.y);
+        };
+        // IPC pairs (ipc_pair_kernel + _pair, ipc_contact.py:130-296) in FP64 at x_n + dx
+        auto ipc_pairs = [&](int mode, double &acc_pHp, double t_c) {
+            const double idhat = d.ipc_dhat, ikappa = d.ipc_kappa, reach = d.reach, gap = d.gap;
+            const double dlo = 1.0e-9 * idhat, onset = 0.02 * idhat;
+            const double mu_s = d.friction ? d.ipc_mu : 0.0;
+            const int per_body = d.friction ? d.per_body : 0;
+            const double floor_ = d.bc_floor * idhat;
+            const int nc = S.ncand;
+            for (int c = tid; c < nc; c += NT) {
+                const unsigned packed = (unsigned)d.cand[sg.cand0 + c];
+                const int k = (int)(packed >> 16), j = (int)(packed & 0xffffu);
+                const int ge = sg.edge0 + k;
+                const int a = d.ea[ge], b = d.eb[ge], pn = d.bnd[sg.bnd0 + j];
+                const double2 xa = xpos(a), xb = xpos(b), xp = xpos(pn);
+                const double abx = xb.x - xa.x, aby = xb.y - xa.y;
+                const double L2 = dmax(abx * abx + aby * aby, 1.0e-30), Ll = sqrt(L2);
+                const double wx = xp.x - xa.x, wy = xp.y - xa.y;
+                const double tt = (wx * abx + wy * aby) / L2;
+                double dvx = wx - tt * abx, dvy = wy - tt * aby;
+                if (tt <= 0.0) { dvx = wx; dvy = wy; }
+                else if (tt >= 1.0) { dvx = xp.x - xb.x; dvy = xp.y - xb.y; }
+                const double dd = sqrt(dvx * dvx + dvy * dvy);
+                if (!(dd < reach)) {
+                    if (mode == 1 || mode == 3) Ctr[sg.cand0 + c] = make_double2(1.0e300, 1.0e300);
+                    continue;
+                }
+                if (mode == 1 || mode == 3) {
+                    double keep = dmax(gap * dd, idhat - onset);
+                    if (dd < idhat) keep = dd - dmin(2.0 * (idhat - dd) + onset, 0.5 * dd);
+                    if (mode == 3) keep = dmin(dd, dmax(gap * dd, floor_));
+                    double2 qp, qa, qb;
+                    if (mode == 3) { qp = kin_dir(pn); qa = kin_dir(a); qb = kin_dir(b); }
+                    else {
+                        const float2 u0 = P[pn], u1 = P[a], u2 = P[b];
+                        qp = make_double2(u0.x, u0.y); qa = make_double2(u1.x, u1.y); qb = make_double2(u2.x, u2.y);
+                    }
+                    double T;
+                    const double Rv = accd_profile(xp.x, xp.y, xa.x, xa.y, xb.x, xb.y, qp.x, qp.y, qa.x, qa.y,
+                                                   qb.x, qb.y, keep, t_c, T);
+                    Ctr[sg.cand0 + c] = make_double2(T, Rv);
+                }
+                if (mode == 3) continue;
+                double mu_p = mu_s;
+                if (per_body) {
+                    const double mi = d.mu_node[pn], mj = d.mu_node[a], sm = mi + mj;
+                    mu_p = sm > 0.0 ? 2.0 * mi * mj / sm : 0.0;
+                }
+                auto term = [&](double coef, int ip, int ia, int ib, double wa, double wb, double dist, double nx,
+                                double ny, double ddd) {
+                    const double bp = barrier_bp<double>(dist, idhat);
+                    const double f_n = -ikappa * bp;
+                    const double tnx = -ny, tny = nx;
+                    const float2 di = XD[ip], da = XD[ia], db = XD[ib];  // slip since the step began
+                    const double ux = (double)di.x - wa * (double)da.x - wb * (double)db.x;
+                    const double uy = (double)di.y - wa * (double)da.y - wb * (double)db.y;
+                    const double ut = ux * tnx + uy * tny;
+                    const double vt = dabs(ut) * inv_dt;
+                    const double kt = mu_p * f_n * inv_dt / dmax(vt, d.epsv);
+                    if (mode == 0) {
+                        const double bpp = barrier_bpp<double>(dist, idhat);
+                        const double s = mu_p * f_n * (ut * inv_dt / dmax(vt, d.epsv));
+                        const double gx = h2 * (-f_n * nx + s * tnx), gy = h2 * (-f_n * ny + s * tny);
+                        const double hx = h2 * (ikappa * bpp * nx * nx + kt * tnx * tnx);
+                        const double hy = h2 * (ikappa * bpp * ny * ny + kt * tny * tny);
+                        const int ids[3] = {ip, ia, ib};
+                        const double cg[3] = {coef, -coef * wa, -coef * wb};
+                        const double ch[3] = {coef, coef * wa * wa, coef * wb * wb};
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            const int n = ids[q];
+                            const uint8_t fm = d.free_mask[n];
+                            float *gp_ = reinterpret_cast<float *>(G + n);
+                            float *dp_ = reinterpret_cast<float *>(D + n);
+                            if (fm & 1) atomicAdd(gp_, (float)(cg[q] * gx));
+                            if (fm & 2) atomicAdd(gp_ + 1, (float)(cg[q] * gy));
+                            atomicAdd(dp_, (float)(ch[q] * hx));
+                            atomicAdd(dp_ + 1, (float)(ch[q] * hy));
+                        }
+                    } else {
+                        const double bpp = barrier_bpp<double>(dist, idhat);
+                        const float2 u0 = P[ip], u1 = P[ia], u2 = P[ib];
+                        const double qx = (double)u0.x - wa * (double)u1.x - wb * (double)u2.x;
+                        const double qy = (double)u0.y - wa * (double)u1.y - wb * (double)u2.y;
+                        const double dn = qx * nx + qy * ny, dt_ = qx * tnx + qy * tny;
+                        const double val = dmax(ikappa * (bpp * dn * dn + bp * ddd), 0.0);
+                        acc_pHp += coef * h2 * (val + kt * dt_ * dt_);
+                    }
+                };
+                if (tt > 0.0 && tt < 1.0 && dd < idhat) {
+                    const double dist = dmax(dd, dlo);
+                    double ddd = 0.0;
+                    if (mode == 1) {
+                        const float2 pb_ = P[b], pa_ = P[a], pp_ = P[pn];
+                        const double dex = (double)pb_.x - (double)pa_.x, dey = (double)pb_.y - (double)pa_.y;
+                        const double dwx = (double)pp_.x - (double)pa_.x, dwy = (double)pp_.y - (double)pa_.y;
+                        const double c0 = abx * wy - aby * wx;
+                        const double c1 = (dex * wy - dey * wx) + (abx * dwy - aby * dwx);
+                        const double c2 = 2.0 * (dex * dwy - dey * dwx);
+                        const double L1 = (abx * dex + aby * dey) / Ll;
+                        const double Lq = ((dex * dex + dey * dey) - L1 * L1) / Ll;
+                        const double s0 = c0 / Ll;
+                        const double s1 = (c1 - s0 * L1) / Ll;
+                        ddd = (c2 - 2.0 * s1 * L1 - s0 * Lq) / Ll;
+                        if (c0 < 0.0) ddd = -ddd;
+                    }
+                    term(1.0, pn, a, b, 1.0 - tt, tt, dist, dvx / dist, dvy / dist, ddd);
+                }
+                double coef_a = -d.ca[ge];
+                if (tt <= 0.0) coef_a += 1.0;
+                double d_a = sqrt(wx * wx + wy * wy);
+                if (coef_a != 0.0 && d_a < idhat) {
+                    d_a = dmax(d_a, dlo);
+                    const double nx = wx / d_a, ny = wy / d_a;
+                    double ddd = 0.0;
+                    if (mode == 1) {
+                        const float2 pp_ = P[pn], pa_ = P[a];
+                        const double dwx = (double)pp_.x - (double)pa_.x, dwy = (double)pp_.y - (double)pa_.y;
+                        const double dn = dwx * nx + dwy * ny;
+                        ddd = ((dwx * dwx + dwy * dwy) - dn * dn) / d_a;
+                    }
+                    term(coef_a, pn, a, b, 1.0, 0.0, d_a, nx, ny, ddd);
+                }
+                double coef_b = -d.cb[ge];
+                if (tt >= 1.0) coef_b += 1.0;
+                const double wbx = xp.x - xb.x, wby = xp.y - xb.y;
+                double d_b = sqrt(wbx * wbx + wby * wby);
+                if (coef_b != 0.0 && d_b < idhat) {
+                    d_b = dmax(d_b, dlo);
+                    const double nx = wbx / d_b, ny = wby / d_b;
+                    double ddd = 0.0;
+                    if (mode == 1) {
+                        const float2 pp_ = P[pn], pb_ = P[b];
+                        const double dwx = (double)pp_.x - (double)pb_.x, dwy = (double)pp_.y - (double)pb_.y;
+                        const double dn = dwx * nx + dwy * ny;
+                        ddd = ((dwx * dwx + dwy * dwy) - dn * dn) / d_b;
+                    }
+                    term(coef_b, pn, a, b, 0.0, 1.0, d_b, nx, ny, ddd);
+                }
+            }
+        };
+        auto tc_scan = [&](double m0) -> double {
+            double m = m0, t_c = m0;
+            int prevk = -1;
+            const int nc = S.ncand;
+#pragma unroll 4
+            for (int c = 0; c < nc; ++c) {
+                const int k = (int)((unsigned)d.cand[sg.cand0 + c] >> 16);
+                const double2 pr = Ctr[sg.cand0 + c];
+                if (k != prevk) { t_c = m; prevk = k; }
+                m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+            }
+            return m;
+        };
+        auto sweep = [&]() {  // kinematic nodes advanced by the step limit, ipc_contact.py:456-463
+            ipc_refresh();
+            double qi = 0.0;
+            for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
+                const double2 q = kin_dir(d.bc_idx[b]);
+                qi = dmax(qi, sqrt(q.x * q.x + q.y * q.y));
+            }
+            double dummy = 0.0;
+            ipc_pairs(3, dummy, 1.0);
+            double v[1] = {qi};
+            const int ops[1] = {1};
+            block_reduce<NT, 1>(v, ops, red);
+            if (tid == 0) {
+                double a_s = tc_scan(1.0);
+                if (v[0] > 0.0) a_s = dmin(a_s, 0.45 * d.reach / v[0]);
+                S.alpha_s = a_s;
+                S.q_inf = v[0];
+                S.motion += dmin(a_s, 1.0) * v[0];
+            }
+            __syncthreads();
+            const double alpha_s = S.alpha_s;
+            for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
+                const int n = d.bc_idx[b];
+                const double2 tg = Tgt[b], x = xpos(n), xn = Xn[n];
+                const double2 nx = alpha_s >= 1.0 ? tg : make_double2(x.x + alpha_s * (tg.x - x.x), x.y + alpha_s * (tg.y - x.y));
+                XD[n] = make_float2((float)(nx.x - xn.x), (float)(nx.y - xn.y));
+            }
+            __syncthreads();
+        };
+
+        if (scene_ipc && sg.nbc > 0) {
+            sweep();
+            if (tid == 0) S.pending = !(S.alpha_s >= 1.0);
+            __syncthreads();
+        }
+
+        // ================================================================ PNCG iterations (FP32)
+        for (int it = 0; it < d.iter_max; ++it) {
+            if (scene_ipc && S.pending) {
+                sweep();
+                if (tid == 0) {
+                    if (S.q_inf > 0.0) S.active = 1;
+                    if (it % 8 == 7) S.pending = !(S.alpha_s >= 1.0);
+                }
+                __syncthreads();
+            }
+            if (!S.active && !S.pending) break;
+            if (S.status != 0) break;
+
+            // ---------------------------------------------- A1: triangles (gradient + diagonal)
+            for (int t = t0 + tid; t < t1; t += NT) {
+                const int i0 = __ldg(d.tri + 3 * t), i1 = __ldg(d.tri + 3 * t + 1), i2 = __ldg(d.tri + 3 * t + 2);
+                const float4 B = Bm[t], du = DU0[t], Dm = Dmr[t];
+                const float A = Ar[t], mu = Mu[t], la = La[t];
+                const float2 u0 = XD[i0], u1 = XD[i1], u2 = XD[i2];
+                const float d1x = du.x + (u1.x - u0.x), d1y = du.y + (u1.y - u0.y);
+                const float d2x = du.z + (u2.x - u0.x), d2y = du.w + (u2.y - u0.y);
+                const float H00 = d1x * B.x + d2x * B.z, H01 = d1x * B.y + d2x * B.w;
+                const float H10 = d1y * B.x + d2y * B.z, H11 = d1y * B.y + d2y * B.w;
+                const float dH = H00 * H11 - H01 * H10;
+                const float Jm1 = (H00 + H11) + dH;
+                const float J = 1.f + Jm1;
+                const float logJ = J > 1.0e-6f ? log1pf(Jm1) : logf(1.0e-6f);
+                const float iJ = J != 0.f ? 1.f / J : 0.f;
+                const float G00 = (1.f + H11) * iJ, G01 = -H10 * iJ, G10 = -H01 * iJ, G11 = (1.f + H00) * iJ;
+                const float c1 = la * logJ - mu;
+                const float onepJ = 1.f + J, ll = la * logJ;
+                const float P00 = mu * ((H00 * onepJ + dH) * iJ) + ll * G00;
+                const float P01 = mu * ((J * H01 + H10) * iJ) + ll * G01;
+                const float P10 = mu * ((J * H10 + H01) * iJ) + ll * G10;
+                const float P11 = mu * ((H11 * onepJ + dH) * iJ) + ll * G11;
+                const float hA = fh2 * A;
+                const float g1x = hA * (P00 * B.x + P01 * B.y), g1y = hA * (P10 * B.x + P11 * B.y);
+                const float g2x = hA * (P00 * B.z + P01 * B.w), g2y = hA * (P10 * B.z + P11 * B.w);
+                const float kk = la - c1;
+                const float b0x = -(B.x + B.z), b0y = -(B.y + B.w);
+                auto dg = [&](float bx, float by, float &dxo, float &dyo) {
+                    const float bb = mu * (bx * bx + by * by);
+                    const float gx = G00 * bx + G01 * by, gy = G10 * bx + G11 * by;
+                    dxo = hA * fmaxf(bb + kk * gx * gx, 0.f);
+                    dyo = hA * fmaxf(bb + kk * gy * gy, 0.f);
+                };
+                float d0x, d0y, d1x_, d1y_, d2x_, d2y_;
+                dg(b0x, b0y, d0x, d0y);
+                dg(B.x, B.y, d1x_, d1y_);
+                dg(B.z, B.w, d2x_, d2y_);
+                Esc[3 * t] = make_float4(-(g1x + g2x), -(g1y + g2y), d0x, d0y);
+                Esc[3 * t + 1] = make_float4(g1x, g1y, d1x_, d1y_);
+                Esc[3 * t + 2] = make_float4(g2x, g2y, d2x_, d2y_);
+                float *ec = Ec + 9 * (size_t)t;
+                ec[0] = G00; ec[1] = G01; ec[2] = G10; ec[3] = G11; ec[4] = c1;
+                ec[5] = Dm.x + d1x; ec[6] = Dm.y + d1y; ec[7] = Dm.z + d2x; ec[8] = Dm.w + d2y;
+            }
+            __syncthreads();
+
+            // ---------------------------------------------- A2: nodes (gather, colliders, friction, force)
+            for (int i = n0 + tid; i < n1; i += NT) {
+                Gp[i] = G[i];
+                const float2 dx_ = XD[i], hv = XHV[i];
+                const float m = M32[i];
+                const uint8_t fm = d.free_mask[i];
+                float gx = (fm & 1) ? m * (dx_.x - hv.x) : 0.f;
+                float gy = (fm & 2) ? m * (dx_.y - hv.y) : 0.f;
+                float dxx = m, dyy = m;
+                {
+                    const int4 ca = __ldg(reinterpret_cast<const int4 *>(d.inc8) + 2 * i);
+                    const int4 cb = __ldg(reinterpret_cast<const int4 *>(d.inc8) + 2 * i + 1);
+                    const int cs[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+                    float4 cv[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (cs[q] >= 0) cv[q] = Esc[cs[q]];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (cs[q] >= 0) { gx += cv[q].x; gy += cv[q].y; dxx += cv[q].z; dyy += cv[q].w; }
+                    const int k0 = __ldg(d.inc_ptr + i) + 8, k1 = __ldg(d.inc_ptr + i + 1);
+                    for (int k = k0; k < k1; ++k) {
+                        const float4 c = Esc[__ldg(d.inc + k)];
+                        gx += c.x; gy += c.y; dxx += c.z; dyy += c.w;
+                    }
+                }
+                if (scene_rig) Del[i] = make_float2(dxx, dyy);
+                const int bs = d.node_bslot[i];
+                if (bs >= 0) {
+                    for (int k = 0; k < n_col; ++k) {
+                        const Col c = cols[k];
+                        float dd, nx, ny, tang = 0.f, H00 = 0.f, H11 = 0.f, gn = 1.f;
+                        if (c.kind == 4) {  // half-space: phi0 (FP64 per step) + n.dx
+                            nx = colf[k][0]; ny = colf[k][1];
+                            dd = PHI0[(size_t)bs * n_col + k] + (nx * dx_.x + ny * dx_.y);
+                        } else {           // curved colliders in FP64
+                            const double2 xi = xpos(i);
+                            double ddd, nnx, nny, dc = 1.0;
+                            SdfHit hh;
+                            if (c.kind == 0) {
+                                const double ex = xi.x - c.cx, ey = xi.y - c.cy;
+                                dc = sqrt(ex * ex + ey * ey);
+                                ddd = dc - c.r; nnx = ex / dc; nny = ey / dc;
+                            } else {
+                                hh = sdf_eval(c.kind, c.cx, c.cy, c.rx, c.ry, c.rref, xi.x, xi.y);
+                                ddd = hh.d; nnx = hh.gx; nny = hh.gy;
+                                gn = (float)sqrt(nnx * nnx + nny * nny);
+                            }
+                            dd = (float)ddd; nx = (float)nnx; ny = (float)nny;
+                            if (c.kind == 0) tang = 1.f / (float)dc;
+                            else { H00 = (float)hh.H00; H11 = (float)hh.H11; }
+                        }
+                        if (dd <= 0.f || dd >= fdhat) continue;
+                        const float bp = barrier_bp<float>(dd, fdhat), bpp = barrier_bpp<float>(dd, fdhat);
+                        const float s = fh2 * fkappa * bp;
+                        gx += s * nx; gy += s * ny;
+                        float hx, hy;
+                        if (c.kind == 0) {
+                            const float tg = bp * tang;
+                            hx = fkappa * (bpp * nx * nx + tg * (1.f - nx * nx));
+                            hy = fkappa * (bpp * ny * ny + tg * (1.f - ny * ny));
+                        } else {
+                            hx = fkappa * (bpp * nx * nx + bp * H00);
+                            hy = fkappa * (bpp * ny * ny + bp * H11);
+                        }
+                        dxx += fh2 * fmaxf(hx, 0.f);
+                        dyy += fh2 * fmaxf(hy, 0.f);
+                        if (d.friction && (fm & 3)) {  // lagged friction, slip velocity dx/dt
+                            const float inx = nx / fmaxf(gn, 1e-30f), iny = ny / fmaxf(gn, 1e-30f);
+                            const float f_n = fkappa * fabsf(bp) * gn;
+                            const float vx = dx_.x * finv_dt, vy = dx_.y * finv_dt;
+                            const float vn = vx * inx + vy * iny;
+                            const float vtx = vx - vn * inx, vty = vy - vn * iny;
+                            const float den = fmaxf(sqrtf(vtx * vtx + vty * vty), fepsv);
+                            const float sf = fh2 * colmuf[k] * f_n;
+                            if (fm & 1) gx += sf * (vtx / den);
+                            if (fm & 2) gy += sf * (vty / den);
+                            const float kt = sf * finv_dt / den;
+                            if (fm & 1) dxx += kt * iny * iny;
+                            if (fm & 2) dyy += kt * inx * inx;
+                        }
+                    }
+                }
+                if (d.fext) {
+                    const float2 f = FH[i];
+                    gx -= f.x; gy -= f.y;
+                }
+                G[i] = make_float2(gx, gy);
+                D[i] = make_float2(dxx, dyy);
+            }
+            __syncthreads();
+
+            // ---------------------------------------------- A3: contact between bodies, tendons (FP64)
+            if (scene_ipc) {
+                ipc_refresh();
+                double z0 = 0.0;
+                ipc_pairs(0, z0, 0.0);
+                __syncthreads();
+            }
+            if (sg.nten > 0) {
+                for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
+                    double L = 0.0;
+                    for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
+                        if (d.t_tid[j] != k) continue;
+                        const int m = d.t_nxt[j];
+                        if (m < 0) continue;
+                        const double2 xa = xpos(d.t_node[j]), xb = xpos(d.t_node[m]);
+                        const double ex = xb.x - xa.x, ey = xb.y - xa.y;
+                        L += sqrt(ex * ex + ey * ey);
+                    }
+                    double tau, keff;
+                    if (d.t_stiff[k] > 0.0) {
+                        const double ext = L - d.t_L0[k];
+                        tau = ext > 0.0 ? d.t_stiff[k] * ext : 0.0;
+                        keff = ext > 0.0 ? d.t_stiff[k] : 0.0;
+                    } else {
+                        tau = dmax(d.t_Tcmd[k], 0.0); keff = 0.0;
+                    }
+                    double *ts = d.t_state + 4 * k;
+                    ts[0] = L; ts[2] = tau; ts[3] = keff;
+                }
+                __syncthreads();
+                for (int j = sg.tent0 + tid; j < sg.tent0 + sg.ntent; j += NT) {
+                    const int n = d.t_node[j], k = d.t_tid[j];
+                    const double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3];
+                    double gLx = 0, gLy = 0, geox = 0, geoy = 0;
+                    const double2 xn_ = xpos(n);
+                    if (d.t_prv[j] >= 0) {
+                        const double2 xa = xpos(d.t_node[d.t_prv[j]]);
+                        const double tx = xn_.x - xa.x, ty = xn_.y - xa.y, ln = dmax(sqrt(tx * tx + ty * ty), 1.0e-12);
+                        const double sx = tx / ln, sy = ty / ln, il = 1.0 / ln;
+                        gLx += sx; gLy += sy;
+                        geox += (1.0 - sx * sx) * il; geoy += (1.0 - sy * sy) * il;
+                    }
+                    if (d.t_nxt[j] >= 0) {
+                        const double2 xb = xpos(d.t_node[d.t_nxt[j]]);
+                        const double tx = xb.x - xn_.x, ty = xb.y - xn_.y, ln = dmax(sqrt(tx * tx + ty * ty), 1.0e-12);
+                        const double sx = tx / ln, sy = ty / ln, il = 1.0 / ln;
+                        gLx -= sx; gLy -= sy;
+                        geox += (1.0 - sx * sx) * il; geoy += (1.0 - sy * sy) * il;
+                    }
+                    float *gp_ = reinterpret_cast<float *>(G + n);
+                    float *dp_ = reinterpret_cast<float *>(D + n);
+                    atomicAdd(gp_, (float)(h2 * tau * gLx));
+                    atomicAdd(gp_ + 1, (float)(h2 * tau * gLy));
+                    atomicAdd(dp_, (float)(h2 * (tau * geox + keff * gLx * gLx)));
+                    atomicAdd(dp_ + 1, (float)(h2 * (tau * geoy + keff * gLy * gLy)));
+                }
+                __syncthreads();
+            }
+
+            // ---------------------------------------------- A4: body-level modes
+            for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b) {  // AffineBodies.gather, affine.py:156-175
+                double v[18];
+#pragma unroll
+                for (int q = 0; q < 18; ++q) v[q] = 0.0;
+                for (int k = sg.affn0 + tid; k < sg.affn0 + sg.naffn; k += NT) {
+                    if (d.a_grp[k] != b) continue;
+                    const int i = d.a_node[k];
+                    const double *w = d.a_w + 3 * k;
+                    const float2 g = G[i], dg = D[i];
+                    const double gx = g.x, gy = g.y, dx = dg.x, dy = dg.y;
+                    v[0] += gx * w[0]; v[1] += gx * w[1]; v[2] += gx * w[2];
+                    v[3] += gy * w[0]; v[4] += gy * w[1]; v[5] += gy * w[2];
+                    const double o[6] = {w[0] * w[0], w[0] * w[1], w[0] * w[2], w[1] * w[1], w[1] * w[2], w[2] * w[2]};
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) { v[6 + q] += dx * o[q]; v[12 + q] += dy * o[q]; }
+                }
+                const int ops[18] = {0};
+                block_reduce<NT, 18>(v, ops, red);
+                if (tid == 0) {
+                    for (int q = 0; q < 6; ++q) {
+                        d.a_gq_prev[6 * b + q] = d.a_gq[6 * b + q];
+                        d.a_gq[6 * b + q] = v[q];
+                    }
+                    for (int q = 0; q < 12; ++q) d.a_H[18 * b + q] = v[6 + q];
+                }
+            }
+            if (sg.naff > 0) {
+                __syncthreads();
+                for (int k = sg.affn0 + tid; k < sg.affn0 + sg.naffn; k += NT) G[d.a_node[k]] = make_float2(0.f, 0.f);
+            }
+            if (tid == 0) { S.gPg = 0.0; S.g_Py = 0.0; S.y_Py = 0.0; }
+            // one rigid piece (a free soft body): its gather is folded into the Dai-Kou pass below;
+            // several pieces: one reduction each here
+            const bool rig1 = sg.nrig == 1;
+            for (int b = sg.rig0; !rig1 && b < sg.rig0 + sg.nrig; ++b) {  // RigidModes.gather, affine.py:404-453
+                const int lb = b - sg.rig0;
+                // centroid shift since the step began: sum m dx / M
+                FF cs2[2] = {{0.f, 0.f}, {0.f, 0.f}};
+                for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
+                    if (d.r_grp[k] != b) continue;
+                    const int i = d.r_node[k];
+                    const float m = M32[i];
+                    const float2 u = XD[i];
+                    ff_add(cs2[0], m * u.x);
+                    ff_add(cs2[1], m * u.y);
+                }
+                float nm[1] = {0.f};
+                const int nmo[1] = {1};
+                double so[2];
+                float mo_[1];
+                block_reduce_mx<NT, 2, 1>(cs2, nm, nmo, so, mo_, fred, dres, mres);
+                const double Mtot = d.r_acc[3 * b + 2];
+                const float csx = (float)(so[0] / Mtot), csy = (float)(so[1] / Mtot);
+                FF v[11];
+#pragma unroll
+                for (int q = 0; q < 11; ++q) v[q] = FF{0.f, 0.f};
+                for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
+                    if (d.r_grp[k] != b) continue;
+                    const int i = d.r_node[k];
+                    const float2 a0 = RARM[i], u = XD[i];
+                    const float rx = a0.x + (u.x - csx), ry = a0.y + (u.y - csy);
+                    const float2 g = G[i], gp = Gp[i], dg = D[i], de = Del[i];
+                    const float m = M32[i];
+                    const float dx = fmaxf(dg.x - de.x, 0.f) + m, dy = fmaxf(dg.y - de.y, 0.f) + m;
+                    ff_add(v[0], g.x); ff_add(v[1], g.y); ff_add(v[2], rx * g.y - ry * g.x);
+                    ff_add(v[3], gp.x); ff_add(v[4], gp.y); ff_add(v[5], rx * gp.y - ry * gp.x);
+                    ff_add(v[6], dx); ff_add(v[7], -dx * ry); ff_add(v[8], dy); ff_add(v[9], dy * rx);
+                    ff_add(v[10], dx * ry * ry + dy * rx * rx);
+                }
+                double vs[11];
+                block_reduce_mx<NT, 11, 1>(v, nm, nmo, vs, mo_, fred, dres, mres);
+                if (tid == 0) {
+                    const double a[9] = {vs[6], 0.0, vs[7], 0.0, vs[8], vs[9], vs[7], vs[9], vs[10]};
+                    const double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[6] * a[5]) +
+                                       a[2] * (a[3] * a[7] - a[6] * a[4]);
+                    double Hi[9] = {0};
+                    if (det != 0.0) {
+                        const double r = 1.0 / det;
+                        Hi[0] = (a[4] * a[8] - a[5] * a[7]) * r; Hi[1] = (a[2] * a[7] - a[1] * a[8]) * r;
+                        Hi[2] = (a[1] * a[5] - a[2] * a[4]) * r; Hi[3] = (a[5] * a[6] - a[3] * a[8]) * r;
+                        Hi[4] = (a[0] * a[8] - a[2] * a[6]) * r; Hi[5] = (a[2] * a[3] - a[0] * a[5]) * r;
+                        Hi[6] = (a[3] * a[7] - a[4] * a[6]) * r; Hi[7] = (a[1] * a[6] - a[0] * a[7]) * r;
+                        Hi[8] = (a[0] * a[4] - a[1] * a[3]) * r;
+                    }
+                    const double g[3] = {vs[0], vs[1], vs[2]}, y[3] = {vs[0] - vs[3], vs[1] - vs[4], vs[2] - vs[5]};
+                    double z[3], zy[3];
+                    for (int r = 0; r < 3; ++r) {
+                        z[r] = Hi[3 * r] * g[0] + Hi[3 * r + 1] * g[1] + Hi[3 * r + 2] * g[2];
+                        zy[r] = Hi[3 * r] * y[0] + Hi[3 * r + 1] * y[1] + Hi[3 * r + 2] * y[2];
+                    }
+                    for (int r = 0; r < 3; ++r) d.r_zq[3 * b + r] = z[r];
+                    RCS[b] = make_float2(csx, csy);
+                    if (lb < 8) {
+                        s_zf[lb][0] = (float)z[0]; s_zf[lb][1] = (float)z[1]; s_zf[lb][2] = (float)z[2];
+                        s_cs[lb][0] = csx; s_cs[lb][1] = csy;
+                    }
+                    S.gPg += g[0] * z[0] + g[1] * z[1] + g[2] * z[2];
+                    S.g_Py += g[0] * zy[0] + g[1] * zy[1] + g[2] * zy[2];
+                    S.y_Py += y[0] * zy[0] + y[1] * zy[1] + y[2] * zy[2];
+                }
+                __syncthreads();
+            }
+
+            // ---------------------------------------------- B1: mask + Dai-Kou dot products
+            // (+ the single rigid piece's B^T g, B^T g_prev, B^T D' B, affine.py:421-453)
+            auto b2 = [&](const double *vs) {
+                if (tid == 0) {  // B2: per-scene scalars, FP64
+                    double gPg = vs[0] + S.gPg, g_p = vs[1], g_Py = vs[2] + S.g_Py, y_p = vs[3], y_Py = vs[4] + S.y_Py;
+                    for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b) {  // affine_reduce_kernel, affine.py:178-205
+                        double *q = d.a_q + 6 * b;
+                        const M2 A{q[1], q[2], q[4], q[5]};
+                        const M2 Pm = nh_P(A, d.a_Mu[b], d.a_La[b]);
+                        double g[6], y[6], z[6], zy[6];
+                        const double hp[6] = {0.0, h2 * Pm.a, h2 * Pm.b, 0.0, h2 * Pm.c, h2 * Pm.d};
+                        for (int r = 0; r < 6; ++r) g[r] = d.a_gq[6 * b + r] + hp[r];
+                        double (*H)[6] = s_H6, (*L)[6] = s_L6;
+                        reduced_hessian(A, d.a_Mu[b], d.a_La[b], h2, d.a_H + 18 * b, H);
+                        chol6(H, L);
+                        for (int r = 0; r < 6; ++r) y[r] = g[r] - d.a_gq_prev[6 * b + r];
+                        chol6_solve(L, g, z);
+                        chol6_solve(L, y, zy);
+                        const double *pq = d.a_pq + 6 * b;
+                        for (int r = 0; r < 6; ++r) {
+                            gPg += g[r] * z[r]; g_p += g[r] * pq[r]; g_Py += g[r] * zy[r];
+                            y_p += y[r] * pq[r]; y_Py += y[r] * zy[r];
+                        }
+                        for (int r = 0; r < 6; ++r) { d.a_gq[6 * b + r] = g[r]; d.a_zq[6 * b + r] = z[r]; }
+                    }
+                    double bta = 0.0;  // finalize_beta_kernel, kernels.py:195-217
+                    if (it > 0 && dabs(y_p) > 1.0e-30) bta = g_Py / y_p - y_Py * g_p / (y_p * y_p);
+                    double gtp = -gPg + bta * g_p;
+                    if (gtp >= 0.0) { bta = 0.0; gtp = -gPg; }
+                    if (d.cg_guard > 0.0 && it > 0) {  // cg_guard_kernel, solver.py:76-94
+                        const double hold = (scene_ipc && S.pending) ? S.q_inf : 0.0;
+                        if (hold <= 0.0 && y_p < d.cg_guard * S.alpha * S.pHp) { bta = 0.0; gtp = -gPg; }
+                    }
+                    S.beta = bta; S.gTp = gtp; S.gn2 = vs[5];
+                    for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
+                        for (int r = 0; r < 6; ++r) d.a_pq[6 * b + r] = -d.a_zq[6 * b + r] + bta * d.a_pq[6 * b + r];
+                }
+                __syncthreads();
+            };
+            auto b1 = [&](auto rig_tag) {
+                constexpr bool RIG = decltype(rig_tag)::value;
+                constexpr int NS = RIG ? 17 : 6;
+                FF v[NS];
+#pragma unroll
+                for (int q = 0; q < NS; ++q) v[q] = FF{0.f, 0.f};
+                const float csx = (float)S.csx, csy = (float)S.csy;
+                for (int i = n0 + tid; i < n1; i += NT) {
+                    const uint8_t fm = d.free_mask[i];
+                    float2 g = G[i];
+                    const float2 dg = D[i], gp = Gp[i], pp = P[i];
+                    if constexpr (RIG) {
+                        if (d.node_rig[i] >= 0) {  // a free node: the mask does not change g
+                            const float2 a0 = RARM[i], u = XD[i], de = Del[i];
+                            const float rx = a0.x + (u.x - csx), ry = a0.y + (u.y - csy);
+                            const float m = M32[i];
+                            const float dx = fmaxf(dg.x - de.x, 0.f) + m, dy = fmaxf(dg.y - de.y, 0.f) + m;
+                            ff_add(v[6], g.x); ff_add(v[7], g.y); ff_add(v[8], rx * g.y - ry * g.x);
+                            ff_add(v[9], gp.x); ff_add(v[10], gp.y); ff_add(v[11], rx * gp.y - ry * gp.x);
+                            ff_add(v[12], dx); ff_add(v[13], -dx * ry); ff_add(v[14], dy); ff_add(v[15], dy * rx);
+                            ff_add(v[16], dx * ry * ry + dy * rx * rx);
+                        }
+                    }
+                    if (!(fm & 1)) g.x = 0.f;
+                    if (!(fm & 2)) g.y = 0.f;
+                    G[i] = g;
+                    const float Px = (fm & 1) ? 1.f / fmaxf(dg.x, 1.0e-12f) : 0.f;
+                    const float Py = (fm & 2) ? 1.f / fmaxf(dg.y, 1.0e-12f) : 0.f;
+                    const float yx = g.x - gp.x, yy = g.y - gp.y;
+                    const float Pg0 = Px * g.x, Pg1 = Py * g.y, Py0 = Px * yx, Py1 = Py * yy;
+                    ff_add(v[0], g.x * Pg0 + g.y * Pg1);
+                    ff_add(v[1], g.x * pp.x + g.y * pp.y);
+                    ff_add(v[2], g.x * Py0 + g.y * Py1);
+                    ff_add(v[3], yx * pp.x + yy * pp.y);
+                    ff_add(v[4], yx * Py0 + yy * Py1);
+                    ff_add(v[5], g.x * g.x + g.y * g.y);
+                }
+                float nm[1] = {0.f};
+                const int nmo[1] = {1};
+                double vs[NS];
+                float mo_[1];
+                block_reduce_mx<NT, NS, 1>(v, nm, nmo, vs, mo_, fred, dres, mres);
+                if constexpr (RIG) {
+                    if (tid == 0) {  // rigid_reduce_kernel, affine.py:456-473 (FP64)
+                        const int b = sg.rig0;
+                        const double a[9] = {vs[12], 0.0, vs[13], 0.0, vs[14], vs[15], vs[13], vs[15], vs[16]};
+                        const double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[6] * a[5]) +
+                                           a[2] * (a[3] * a[7] - a[6] * a[4]);
+                        double Hi[9] = {0};
+                        if (det != 0.0) {
+                            const double r = 1.0 / det;
+                            Hi[0] = (a[4] * a[8] - a[5] * a[7]) * r; Hi[1] = (a[2] * a[7] - a[1] * a[8]) * r;
+                            Hi[2] = (a[1] * a[5] - a[2] * a[4]) * r; Hi[3] = (a[5] * a[6] - a[3] * a[8]) * r;
+                            Hi[4] = (a[0] * a[8] - a[2] * a[6]) * r; Hi[5] = (a[2] * a[3] - a[0] * a[5]) * r;
+                            Hi[6] = (a[3] * a[7] - a[4] * a[6]) * r; Hi[7] = (a[1] * a[6] - a[0] * a[7]) * r;
+                            Hi[8] = (a[0] * a[4] - a[1] * a[3]) * r;
+                        }
+                        const double g[3] = {vs[6], vs[7], vs[8]}, y[3] = {vs[6] - vs[9], vs[7] - vs[10], vs[8] - vs[11]};
+                        double z[3], zy[3];
+                        for (int r = 0; r < 3; ++r) {
+                            z[r] = Hi[3 * r] * g[0] + Hi[3 * r + 1] * g[1] + Hi[3 * r + 2] * g[2];
+                            zy[r] = Hi[3 * r] * y[0] + Hi[3 * r + 1] * y[1] + Hi[3 * r + 2] * y[2];
+                        }
+                        for (int r = 0; r < 3; ++r) d.r_zq[3 * b + r] = z[r];
+                        s_zf[0][0] = (float)z[0]; s_zf[0][1] = (float)z[1]; s_zf[0][2] = (float)z[2];
+                        s_cs[0][0] = csx; s_cs[0][1] = csy;
+                        S.gPg += g[0] * z[0] + g[1] * z[1] + g[2] * z[2];
+                        S.g_Py += g[0] * zy[0] + g[1] * zy[1] + g[2] * zy[2];
+                        S.y_Py += y[0] * zy[0] + y[1] * zy[1] + y[2] * zy[2];
+                    }
+                }
+                b2(vs);
+            };
+            if (rig1) b1(std::true_type{}); else b1(std::false_type{});
+
+            // ---------------------------------------------- B3: direction + node curvature and caps
+            FF acc_pHp{0.f, 0.f}, acc_mpx{0.f, 0.f}, acc_mpy{0.f, 0.f};  // p^T H p; single rigid piece: sum m p
+            double acc_rare = 0.0;
+            float acc_pinf = 0.f, acc_clr = 1.0e30f, acc_alpha = (float)d.alpha_max;
+            {
+                const float bta = (float)S.beta;
+                for (int i = n0 + tid; i < n1; i += NT) {
+                    const uint8_t fm = d.free_mask[i];
+                    const float2 dx_ = XD[i];
+                    float px, py;
+                    const int ka = d.node_aff[i];
+                    if (ka >= 0) {
+                        const double *w = d.a_w + 3 * ka, *pq = d.a_pq + 6 * d.a_grp[ka];
+                        px = (float)(w[0] * pq[0] + w[1] * pq[1] + w[2] * pq[2]);
+                        py = (float)(w[0] * pq[3] + w[1] * pq[4] + w[2] * pq[5]);
+                    } else {
+                        const float2 g = G[i], dg = D[i], po = P[i];
+                        px = (fm & 1) ? -g.x / fmaxf(dg.x, 1.0e-12f) + bta * po.x : 0.f;
+                        py = (fm & 2) ? -g.y / fmaxf(dg.y, 1.0e-12f) + bta * po.y : 0.f;
+                        const int kr = d.node_rig[i];
+                        if (kr >= 0) {
+                            const int lb = d.r_grp[kr] - sg.rig0;
+                            float z0, z1, z2, csx, csy;
+                            if (lb < 8) {
+                                z0 = s_zf[lb][0]; z1 = s_zf[lb][1]; z2 = s_zf[lb][2]; csx = s_cs[lb][0]; csy = s_cs[lb][1];
+                            } else {
+                                const double *z = d.r_zq + 3 * (sg.rig0 + lb);
+                                const float2 cs = RCS[sg.rig0 + lb];
+                                z0 = (float)z[0]; z1 = (float)z[1]; z2 = (float)z[2]; csx = cs.x; csy = cs.y;
+                            }
+                            const float2 a0 = RARM[i];
+                            const float rx = a0.x + (dx_.x - csx), ry = a0.y + (dx_.y - csy);
+                            px -= z0 - z2 * ry;
+                            py -= z1 + z2 * rx;
+                        }
+                    }
+                    P[i] = make_float2(px, py);
+                    const float mi = M32[i];
+                    ff_add(acc_pHp, mi * (px * px + py * py));
+                    if (rig1 && d.node_rig[i] >= 0) { ff_add(acc_mpx, mi * px); ff_add(acc_mpy, mi * py); }
+                    acc_pinf = fmaxf(acc_pinf, sqrtf(px * px + py * py));
+                    const int bs = d.node_bslot[i];
+                    if (bs >= 0) {
+                        for (int k = 0; k < n_col; ++k) {
+                            const Col c = cols[k];
+                            if (c.kind == 4) {  // half-space: clearance, CCD, barrier and friction curvature
+                                const float nx = colf[k][0], ny = colf[k][1];
+                                const float dd = PHI0[(size_t)bs * n_col + k] + (nx * dx_.x + ny * dx_.y);
+                                const float gp = nx * px + ny * py;
+                                if (!(gp >= 0.f || dd <= 0.f)) acc_alpha = fminf(acc_alpha, feta * dd / (-gp));
+                                acc_clr = fminf(acc_clr, dd);
+                                if (dd <= 0.f || dd >= fdhat) continue;
+                                const float bp = barrier_bp<float>(dd, fdhat), bpp = barrier_bpp<float>(dd, fdhat);
+                                ff_add(acc_pHp, fh2 * fmaxf(fkappa * (bpp * gp * gp), 0.f));
+                                if (d.friction && (fm & 3)) {
+                                    const float f_n = fkappa * fabsf(bp);
+                                    const float vx = dx_.x * finv_dt, vy = dx_.y * finv_dt;
+                                    const float vn = vx * nx + vy * ny;
+                                    const float vtx = vx - vn * nx, vty = vy - vn * ny;
+                                    const float den = fmaxf(sqrtf(vtx * vtx + vty * vty), fepsv);
+                                    const float kt = fh2 * colmuf[k] * f_n * finv_dt / den;
+                                    const float pt = ((fm & 1) ? px : 0.f) * (-ny) + ((fm & 2) ? py : 0.f) * nx;
+                                    ff_add(acc_pHp, kt * pt * pt);
+                                }
+                                continue;
+                            }
+                            // curved colliders, FP64
+                            const double2 xi = xpos(i);
+                            double dd, nx, ny, dc = 1.0, gn = 1.0;
+                            SdfHit hh;
+                            if (c.kind == 0) {
+                                const double ex = xi.x - c.cx, ey = xi.y - c.cy;
+                                dc = sqrt(ex * ex + ey * ey);
+                                dd = dc - c.r; nx = ex / dc; ny = ey / dc;
+                                const double a = (double)px * px + (double)py * py;
+                                if (a >= 1.0e-24) {  // disc_ccd_kernel, kernels.py:344-371
+                                    const double bq = 2.0 * (ex * px + ey * py), cq = (ex * ex + ey * ey) - c.r * c.r;
+                                    const double disc = bq * bq - 4.0 * a * cq;
+                                    if (disc >= 0.0) {
+                                        const double sq = sqrt(disc), r1 = (-bq - sq) / (2.0 * a), r2 = (-bq + sq) / (2.0 * a);
+                                        double sv = BIG;
+                                        if (r1 > 0.0) sv = dmin(sv, r1);
+                                        if (r2 > 0.0) sv = dmin(sv, r2);
+                                        if (sv < BIG) acc_alpha = fminf(acc_alpha, (float)(d.ccd_eta * sv));
+                                    }
+                                }
+                            } else {
+                                hh = sdf_eval(c.kind, c.cx, c.cy, c.rx, c.ry, c.rref, xi.x, xi.y);
+                                dd = hh.d; nx = hh.gx; ny = hh.gy;
+                                gn = sqrt(nx * nx + ny * ny);
+                                const double gp = nx * px + ny * py;
+                                if (!(gp >= 0.0 || dd <= 0.0)) acc_alpha = fminf(acc_alpha, (float)(d.ccd_eta * dd / (-gp)));
+                            }
+                            acc_clr = fminf(acc_clr, (float)dd);
+                            if (dd <= 0.0 || dd >= dhat) continue;
+                            const float rd = (float)dd, rnx = (float)nx, rny = (float)ny;
+                            const float bp = barrier_bp<float>(rd, fdhat), bpp = barrier_bpp<float>(rd, fdhat);
+                            float val;
+                            if (c.kind == 0) {
+                                const float pn = px * rnx + py * rny;
+                                const float ptx = px - pn * rnx, pty = py - pn * rny;
+                                val = fkappa * (bpp * pn * pn + (bp / (float)dc) * (ptx * ptx + pty * pty));
+                            } else {
+                                const float gp = rnx * px + rny * py;
+                                const float Hp0 = (float)hh.H00 * px + (float)hh.H01 * py, Hp1 = (float)hh.H10 * px + (float)hh.H11 * py;
+                                val = fkappa * (bpp * gp * gp + bp * (px * Hp0 + py * Hp1));
+                            }
+                            ff_add(acc_pHp, fh2 * fmaxf(val, 0.f));
+                            if (d.friction && (fm & 3)) {
+                                const float ig = 1.f / fmaxf((float)gn, 1e-30f);
+                                const float nnx = rnx * ig, nny = rny * ig;
+                                const float f_n = fkappa * fabsf(bp) * (float)gn;
+                                const float vx = dx_.x * finv_dt, vy = dx_.y * finv_dt;
+                                const float vn = vx * nnx + vy * nny;
+                                const float vtx = vx - vn * nnx, vty = vy - vn * nny;
+                                const float den = fmaxf(sqrtf(vtx * vtx + vty * vty), fepsv);
+                                const float kt = fh2 * colmuf[k] * f_n * finv_dt / den;
+                                const float pt = ((fm & 1) ? px : 0.f) * (-nny) + ((fm & 2) ? py : 0.f) * nnx;
+                                ff_add(acc_pHp, kt * pt * pt);
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+
+            // ---------------------------------------------- B4: triangles (curvature + inversion cap)
+            {
+                const float shrink = (float)d.area_shrink;
+                for (int t = t0 + tid; t < t1; t += NT) {
+                    const int i0 = __ldg(d.tri + 3 * t), i1 = __ldg(d.tri + 3 * t + 1), i2 = __ldg(d.tri + 3 * t + 2);
+                    const float *ec = Ec + 9 * (size_t)t;
+                    const float G00 = ec[0], G01 = ec[1], G10 = ec[2], G11 = ec[3], c1 = ec[4];
+                    const float e1x = ec[5], e1y = ec[6], e2x = ec[7], e2y = ec[8];
+                    const float2 p0 = P[i0], p1 = P[i1], p2 = P[i2];
+                    const float q1x = p1.x - p0.x, q1y = p1.y - p0.y, q2x = p2.x - p0.x, q2y = p2.y - p0.y;
+                    const float4 B = Bm[t];
+                    const float A = Ar[t], mu = Mu[t], la = La[t];
+                    const float f00 = q1x * B.x + q2x * B.z, f01 = q1x * B.y + q2x * B.w;
+                    const float f10 = q1y * B.x + q2y * B.z, f11 = q1y * B.y + q2y * B.w;
+                    const float dd = f00 * f00 + f01 * f01 + f10 * f10 + f11 * f11;
+                    const float GdF = G00 * f00 + G01 * f01 + G10 * f10 + G11 * f11;
+                    const float M00 = f00 * G00 + f10 * G10, M01 = f00 * G01 + f10 * G11;
+                    const float M10 = f01 * G00 + f11 * G10, M11 = f01 * G01 + f11 * G11;
+                    const float tr = M00 * M00 + 2.f * M01 * M10 + M11 * M11;
+                    ff_add(acc_pHp, fh2 * fmaxf(A * (mu * dd + la * GdF * GdF - c1 * tr), 0.f));
+                    const float a0 = e1x * e2y - e1y * e2x;  // inversion_alpha_kernel, kernels.py:303-341
+                    const float a1 = (e1x * q2y - e1y * q2x) + (q1x * e2y - q1y * e2x);
+                    const float a2 = q1x * q2y - q1y * q2x;
+                    const float cc = a0 - shrink * a0;
+                    if (fabsf(a2) < 1.0e-24f) {
+                        if (fabsf(a1) > 1.0e-24f) {
+                            const float s = -cc / a1;
+                            if (s > 0.f) acc_alpha = fminf(acc_alpha, s);
+                        }
+                    } else {
+                        const float disc = a1 * a1 - 4.f * a2 * cc;
+                        if (disc >= 0.f) {
+                            const float sq = sqrtf(disc);
+                            const float r1 = (-a1 - sq) / (2.f * a2), r2 = (-a1 + sq) / (2.f * a2);
+                            if (r1 > 0.f) acc_alpha = fminf(acc_alpha, r1);
+                            if (r2 > 0.f) acc_alpha = fminf(acc_alpha, r2);
+                        }
+                    }
+                }
+                if (scene_rare) {
+                    for (int b = sg.aff0 + tid; b < sg.aff0 + sg.naff; b += NT) {  // affine_pHp_kernel
+                        const double *q = d.a_q + 6 * b, *pq = d.a_pq + 6 * b;
+                        const M2 dA{pq[1], pq[2], pq[4], pq[5]}, A{q[1], q[2], q[4], q[5]};
+                        acc_rare += h2 * dmax(ddot2(dA, nh_d2(A, dA, d.a_Mu[b], d.a_La[b])), 0.0);
+                    }
+                    if (scene_ipc) ipc_pairs(1, acc_rare, d.alpha_max);
+                    for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {  // Tendon.pHp
+                        const double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3];
+                        double dL = 0.0;
+                        for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
+                            if (d.t_tid[j] != k) continue;
+                            const int m = d.t_nxt[j];
+                            if (m < 0) continue;
+                            const int na = d.t_node[j], nb_ = d.t_node[m];
+                            const double2 xa = xpos(na), xb = xpos(nb_);
+                            const double tx = xb.x - xa.x, ty = xb.y - xa.y, ln = dmax(sqrt(tx * tx + ty * ty), 1.0e-12);
+                            const double sx = tx / ln, sy = ty / ln;
+                            const float2 pa = P[na], pb = P[nb_];
+                            const double dpx = (double)pb.x - (double)pa.x, dpy = (double)pb.y - (double)pa.y;
+                            const double along = dpx * sx + dpy * sy;
+                            dL += along;
+                            acc_rare += h2 * tau * ((dpx * dpx + dpy * dpy) - along * along) * (1.0 / ln);
+                        }
+                        acc_rare += h2 * keff * dL * dL;
+                    }
+                    // FP64 contributions of the rare terms joined into the compensated pair
+                    const float hi = (float)acc_rare;
+                    ff_add(acc_pHp, hi);
+                    ff_add(acc_pHp, (float)(acc_rare - (double)hi));
+                }
+            }
+            {
+                FF sv[3] = {acc_pHp, acc_mpx, acc_mpy};
+                float mv[3] = {acc_pinf, acc_clr, acc_alpha};
+                const int mops[3] = {1, 2, 2};
+                double so[3];
+                float mo[3];
+                block_reduce_mx<NT, 3, 3>(sv, mv, mops, so, mo, fred, dres, mres);
+                // ---------------------------------------------- B5: step length and convergence (FP64)
+                if (tid == 0) {
+                    const double ph = so[0], pinf = mo[0], clr = mo[1];
+                    double a = mo[2];
+                    if (scene_ipc) {
+                        a = dmin(a, tc_scan(d.alpha_max));
+                        if (pinf > 0.0) a = dmin(a, 0.45 * d.reach / pinf);
+                    }
+                    S.pHp = ph; S.p_inf = pinf; S.clr_min = clr;
+                    S.alpha = a;
+                    if (S.active) {
+                        bool done = false;
+                        if (d.gtol > 0.0) {
+                            if (it == 0) S.gn0 = S.gn2;
+                            else if (S.gn2 <= d.gtol * d.gtol * S.gn0) { S.active = 0; done = true; }
+                        }
+                        if (!done) {
+                            if (ph > 0.0) a = dmin(a, -S.gTp / ph);
+                            if (clr < near && pinf > 0.0) a = dmin(a, 0.5 * dhat / pinf);
+                            if (!(a == a)) { S.status = D2F_ENAN; S.active = 0; S.alpha = 0.0; }
+                            else if (a <= 0.0) { S.active = 0; S.alpha = 0.0; }
+                            else {
+                                S.alpha = a;
+                                if (d.tol_x > 0.0 && a * pinf < d.tol_x) { S.active = 0; S.iters += 1; }
+                                else {
+                                    const double dm = -a * S.gTp - 0.5 * a * a * ph;
+                                    if (it == 0) S.dE0 = dmax(dm, 1.0e-300);
+                                    else if (dm < d.eps * S.dE0) S.active = 0;
+                                    S.iters += 1;
+                                }
+                            }
+                        }
+                    }
+                    if (S.active) {
+                        for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
+                            for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
+                        S.motion += S.alpha * pinf;              // bound on any node's move
+                        if (rig1) {                              // centroid shift, sum m dx / M
+                            const double Mt = d.r_acc[3 * sg.rig0 + 2];
+                            S.csx += S.alpha * so[1] / Mt;
+                            S.csy += S.alpha * so[2] / Mt;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+
+            // ---------------------------------------------- D1: dx += alpha p (slaved nodes: J q - x_n)
+            {
+                const bool act = S.active != 0;
+                const float al = (float)S.alpha;
+                for (int i = n0 + tid; i < n1; i += NT) {
+                    const int ka = d.node_aff[i];
+                    if (ka >= 0) {
+                        const double *w = d.a_w + 3 * ka, *q = d.a_q + 6 * d.a_grp[ka];
+                        const double2 xn = Xn[i];
+                        XD[i] = make_float2((float)(w[0] * q[0] + w[1] * q[1] + w[2] * q[2] - xn.x),
+                                            (float)(w[0] * q[3] + w[1] * q[4] + w[2] * q[5] - xn.y));
+                    } else if (act) {
+                        const float2 pp = P[i], u = XD[i];
+                        XD[i] = make_float2(u.x + al * pp.x, u.y + al * pp.y);
+                    }
+                }
+                __syncthreads();
+            }
+        }
+
+        // ================================================================ commit (FP64)
+        for (int i = n0 + tid; i < n1; i += NT) {
+            const double2 xn = Xn[i];
+            const float2 u = XD[i];
+            const double2 xi = make_double2(xn.x + (double)u.x, xn.y + (double)u.y);
+            X[i] = xi;
+            Vv[i] = make_double2((xi.x - xn.x) * inv_dt, (xi.y - xn.y) * inv_dt);
+        }
+        if (tid == 0) {
+            d.iters[sc] = S.iters;
+            d.active[sc] = S.active;
+            d.status[sc] = S.status;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace d2f

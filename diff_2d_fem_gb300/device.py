@@ -40,7 +40,7 @@ class DeviceSolver:
     """Binds a problem to device memory and a libd2f handle. `precision`: "fp64" or
     "mixed". threads / blocks_per_sm: the scene-block launch shape (0 = library default)."""
 
-    def __init__(self, prob, precision="fp64", threads=256, blocks_per_sm=0, device="cuda", stream=None):
+    def __init__(self, prob, precision="fp64", threads=0, blocks_per_sm=0, device="cuda", stream=None):
         if torch is None:
             raise RuntimeError("PyTorch is required for device buffers")
         if not torch.cuda.is_available():
@@ -184,10 +184,10 @@ class DeviceSolver:
         self.v = T_("v", np.asarray(prob.get("v", np.zeros_like(x)), np.float64), f64)
         self.xn = T_("xn", np.zeros_like(x), f64)
         if self.mixed:
-            # the FP32 element routine works on displacements from the rest shape
+            # the FP32 iterations work on increments from the step start and on displacements
+            # from the rest shape (rest edge vectors per triangle)
             rest = np.asarray(prob.get("rest", x), np.float64)
             T_("xrest", rest, f64)
-            T_("xu", x - rest, f64)
             T_("Dm", np.concatenate([rest[tri[:, 1]] - rest[tri[:, 0]], rest[tri[:, 2]] - rest[tri[:, 0]]], 1), rdt)
         self.xhat = T_("xhat", np.zeros_like(x), f64)
         for nm in ("grad", "grad_prev", "p", "diagH", "diag_el"):
@@ -258,6 +258,11 @@ class DeviceSolver:
             T_("r_grp", rg["grp"], i32)
             T_("r_acc", np.zeros((n_rig, 3)), f64)
             T_("r_zq", np.zeros((n_rig, 3)), f64)
+        if self.mixed:
+            n_rig_ = len(rg["env"]) if rg is not None else 0
+            ncol_ = len(np.asarray(prob.get("colliders", np.zeros((0, 8)))).reshape(-1, 8))
+            nbytes = int(self.L.d2f_mixed_scratch_bytes(N, T, Nb, ncol_, n_rig_))
+            self._t["mscr"] = torch.zeros(nbytes, dtype=torch.uint8, device=self.dev)
         T_("iters", np.zeros(B), i32)
         T_("active", np.zeros(B), i32)
         T_("status", np.zeros(B), i32)

@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-VARIANTS = [(128, 4), (256, 1), (256, 2), (256, 3), (512, 1)]
+VARIANTS = [(32, 16), (64, 8), (128, 4), (256, 3)]
 _CACHE = {}
 
 

@@ -18,6 +18,7 @@
 #ifndef D2F_H
 #define D2F_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -66,7 +67,7 @@ typedef struct d2f_scene_desc {
     const d2f_seg *segs;         /* n_scenes */
     /* node state */
     double *x, *v, *xn, *xhat;   /* N x 2 */
-    double *xu;                  /* N x 2: x - rest (mixed precision; else NULL) */
+    double *xu;                  /* unused (NULL) */
     const double *xrest;         /* N x 2: rest positions (mixed precision; else NULL) */
     void *grad, *grad_prev, *p, *diagH, *diag_el; /* N x 2 real */
     const double *mass;          /* N */
@@ -86,6 +87,7 @@ typedef struct d2f_scene_desc {
     const void *Dm;              /* T x 4 real: rest edge vectors X1-X0, X2-X0 (mixed; else NULL) */
     void *escr;                  /* T x 12 real: per-corner gradient and diagonal */
     void *ecache;                /* T x 9 real: F^-T, la log J - mu, edge vectors */
+    void *mscr;                  /* mixed precision: per-step scratch of d2f_mixed_scratch_bytes() bytes; else NULL */
     /* boundary nodes and colliders */
     const int32_t *bnd;          /* Nb: node of each boundary slot */
     const double *colliders;     /* n_col x 8: kind, cx, cy, rx, ry, rref, r, mu */
@@ -122,7 +124,7 @@ typedef struct d2f_scene_desc {
     double ccd_eta, cg_guard, gtol;
     double ipc_mu, ipc_dhat, ipc_kappa, reach, gap, bc_floor, skin;
     int32_t iter_max, conv_check, friction, per_body;
-    int32_t threads;             /* threads per scene block: 128, 256 or 512 (0: 256) */
+    int32_t threads;             /* threads per scene block: 32, 64, 128 or 256 (0: 128) */
     int32_t blocks_per_sm;       /* resident scene blocks per SM the register budget targets
                                     (0: the library's default for that width) */
 } d2f_scene_desc;
@@ -160,6 +162,10 @@ int32_t d2f_destroy(d2f_solver *s);
 /* Message of the last error on this thread ("" if none). */
 const char *d2f_last_error(void);
 
+/* Bytes of the mixed-precision per-step scratch (d2f_scene_desc.mscr) for a batch of N
+ * nodes, T triangles, Nb boundary nodes, n_col colliders and n_rig rigid-mode pieces. */
+size_t d2f_mixed_scratch_bytes(int32_t N, int32_t T, int32_t Nb, int32_t n_col, int32_t n_rig);
+
 /* Number of kernels d2f_step launches per call (for launch accounting). */
 int32_t d2f_kernels_per_step(const d2f_solver *s);
 
@@ -169,7 +175,7 @@ int32_t d2f_kernels_per_step(const d2f_solver *s);
 /* One implicit step of every scene, like d2f_step, for callers that cannot allocate
  * device memory (a host that forbids cudaMalloc after start-up, a plugin handed plain
  * pointers by its host). No handle and no allocation: the caller passes the descriptor
- * with its inputs and outputs; the scratch fields (escr, ecache, cand, cand_tr, xref, work) are
+ * with its inputs and outputs; the scratch fields (escr, ecache, mscr, cand, cand_tr, xref, work) are
  * ignored and taken from a static device array of D2F_NOALLOC_SCRATCH_BYTES that every
  * GPU loading the library holds until exit. A batch needing more scratch than that is
  * refused with D2F_EINVAL and a message. The first call on a device looks up the array's

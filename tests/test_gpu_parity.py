@@ -56,6 +56,7 @@ def test_mixed_close_to_fp64_when_converged(name):
     prob, steps, _ = load_fixture(name)
     prob = dict(prob)
     prob["iter_max"] = 3000
+    prob["eps"] = 1e-13       # the default 1e-10 leaves ~sqrt(eps) of each step's motion
     r64 = _run_device(prob, steps, "fp64")
     rmx = _run_device(prob, steps, "mixed")
     for k, ((x64, _), (xmx, it)) in enumerate(zip(r64, rmx)):
