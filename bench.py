@@ -97,6 +97,17 @@ def algorithmic_bytes(prob, iters, mixed):
     return float((np.asarray(iters, np.float64) * per).sum())
 
 
+# DRAM traffic of the step kernel per scene-iteration: dram__bytes_read.sum +
+# dram__bytes_write.sum of one ncu capture of one step of 608 scenes of this workload (after
+# one warm-up step), divided by that step's scene-iterations. keyed by precision:
+# (bytes per scene-iteration, launch shape captured). A launch's traffic is this times its
+# scene-iterations (traffic grows with the iterations each scene runs).
+TRAFFIC_PER_SCENE_ITER = {
+    "mixed": ((50.444956672e9 + 29.283109632e9) / (608 * 240.19078947368422), "128x4"),
+    "fp64": ((98.965070336e9 + 59.728653568e9) / (608 * 239.94078947368422), "128x4"),
+}
+
+
 # ----------------------------------------------------------------------------- CPU baseline
 def cpu_sample(prob, state_x, state_v, n_threads, per_thread, seed=1):
     """The serial FP64 oracle on a bounded sample: n_threads threads, each advancing its own
@@ -293,6 +304,8 @@ def run_ours(args, rank, world):
     peaks, src = _peaks()
     hbm = float(peaks.get("hbm_gbs", HBM_FALLBACK_GBS))
     achieved = launch_bytes / (launch_ms / 1e3) / 1e9
+    tps, tshape = TRAFFIC_PER_SCENE_ITER[args.precision]
+    traffic = float(tps * np.sum(it_l))
     rec = {
         "metric": "batched scene-steps/s (implicit PNCG step)",
         "value": value, "unit": "scene-steps/s", "n_gpus": world, "steps": args.steps,
@@ -317,7 +330,9 @@ def run_ours(args, rank, world):
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": "scene-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                     "frac": achieved / hbm, "traffic": traffic, "peak_source": src,
+                     "traffic_source": f"ncu capture of 608 scenes ({tshape} launch shape), scaled by "
+                                       f"scene-iterations ({int(np.sum(it_l))} in this launch)",
                      "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": launch_ms},
         "cpu_baseline": {"value": cpu_val, "unit": "scene-steps/s", "cores": threads, "kind": "port",
                          "sample": cpu_desc},

@@ -48,7 +48,8 @@ class SceneDesc(C.Structure):
 
 
 EXPORTS = ("d2f_abi_version", "d2f_create", "d2f_step", "d2f_set_dt", "d2f_stats", "d2f_destroy",
-           "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc", "d2f_mixed_scratch_bytes")
+           "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc", "d2f_mixed_scratch_bytes",
+           "d2f_adjoint_solve", "d2f_adjoint_vjp")
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
@@ -85,6 +86,10 @@ def load(build_if_missing: bool = True):
     L.d2f_step_noalloc.restype = _I
     L.d2f_mixed_scratch_bytes.argtypes = [_I, _I, _I, _I, _I]
     L.d2f_mixed_scratch_bytes.restype = C.c_size_t
+    L.d2f_adjoint_solve.argtypes = [_P, _P, _P, _P, _P, _P, _D, _I, _P, _P, _P]
+    L.d2f_adjoint_solve.restype = _I
+    L.d2f_adjoint_vjp.argtypes = [_P, _P, _P, _P, _P, _P]
+    L.d2f_adjoint_vjp.restype = _I
     if L.d2f_abi_version() != D2F_ABI_VERSION:
         raise RuntimeError("libd2f.so ABI version mismatch; rebuild it")
     _LIB = L

@@ -2,7 +2,7 @@
 
     python -m diff_2d_fem_gb300.build
 
-Three translation units (FP64 kernels, mixed kernels, C ABI) compiled in parallel, one
+Four translation units (FP64 step kernels, mixed step kernels, C ABI, adjoint kernels) compiled in parallel, one
 -gencode (sm_103a), no CMake. The library lands in
 diff_2d_fem_gb300/_build/libd2f.so and is rebuilt when a source is newer than it.
 """
@@ -17,8 +17,8 @@ ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libd2f.so")
 CSRC = os.path.join(HERE, "csrc")
-SOURCES = [os.path.join(CSRC, f) for f in ("pncg_fp64.cu", "pncg_mixed.cu", "d2f_capi.cu")]
-DEPS = SOURCES + [os.path.join(CSRC, "pncg_kernel.cuh"), os.path.join(CSRC, "d2f_math.cuh"),
+SOURCES = [os.path.join(CSRC, f) for f in ("pncg_fp64.cu", "pncg_mixed.cu", "d2f_capi.cu", "adjoint.cu")]
+DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("pncg_kernel.cuh", "pncg_mixed_kernel.cuh", "d2f_math.cuh", "d2f_solver.h")] + [
                   os.path.join(ROOT, "include", "d2f.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -29,7 +29,7 @@ def nvcc():
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile the three translation units in parallel, link libd2f.so."""
+    """Compile the translation units in parallel, link libd2f.so."""
     os.makedirs(OUT_DIR, exist_ok=True)
     newest = max(os.path.getmtime(p) for p in DEPS + [__file__])
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:

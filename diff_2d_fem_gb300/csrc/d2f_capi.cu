@@ -7,18 +7,15 @@
 #include <stdio.h>
 #include <string.h>
 
-struct d2f_solver {
-    d2f_scene_desc d;
-    int grid;
-    int smem;
-};
+#include "d2f_solver.h"
 
-static thread_local char g_err[512];
+thread_local char g_err[512];
 
-static int fail(int code, const char *msg) {
+int d2f_fail(int code, const char *msg) {
     snprintf(g_err, sizeof g_err, "%s", msg);
     return code;
 }
+static int fail(int code, const char *msg) { return d2f_fail(code, msg); }
 
 // The built variant for (threads, blocks_per_sm): an exact match, else the first variant of
 // that width, else (128, 4).

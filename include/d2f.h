@@ -184,6 +184,38 @@ int32_t d2f_kernels_per_step(const d2f_solver *s);
  * No counterpart in the reference: its solver always owns its own buffers. */
 int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream);
 
+/* ---- adjoint of a converged step (FP64 solvers only) ----
+ *
+ * Solve, per scene, the transposed linearised step system at the converged positions x_lin
+ * (N x 2, device):
+ *     (M + h^2 (K_elastic + K_collider + K_tendon)) lam = rhs      on the free DOFs,
+ * with the collider contact gate frozen at x_lin and friction left out, by Jacobi-
+ * preconditioned CG run on the device, one thread block per scene. `rhs` (N x 2) is read on
+ * the free DOFs only; `lam` (N x 2) gets the solution, zero on the kinematic DOFs. `work`
+ * is 10 N doubles of scratch. `tension` (n_ten, device, or NULL = desc->t_Tcmd) is the
+ * tension of each tension-controlled tendon at this step. A scene stops when
+ * |r| <= rtol |rhs| or after max_iter iterations; per scene, `iters` (device, n_scenes)
+ * gets the iterations and `status` (device, n_scenes) 0 (converged), 1 (max_iter reached)
+ * or D2F_ENAN (the operator was not positive along a search direction). The handle's
+ * per-triangle scratch (escr, ecache) is overwritten: call between steps, not during one.
+ * Refused (D2F_EINVAL) for mixed-precision solvers, IPC contact between bodies and affine
+ * bodies, which the operator has no tangent for.
+ * Replaces AdjointPNCG2D.adjoint_solve (implicit/adjoint.py:339-369), whose MINRES runs on
+ * the host and crosses to the device twice per matrix-vector product. */
+int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs, double *lam, double *work,
+                          const double *tension, double rtol, int32_t max_iter, int32_t *iters, int32_t *status,
+                          void *stream);
+
+/* Vector-Jacobian products of one step's residual, accumulated for a solved lam:
+ *   dscale[t]   += -h^2 lam . f_t(x_lin)    (f_t: triangle t's elastic force at its current
+ *                                            mu, lam; the derivative with respect to a common
+ *                                            scale of the triangle's two moduli)
+ *   dtension[k]  = -h^2 lam . dL_k/dx       (L_k: length of tendon k; NULL to skip)
+ * Replaces AdjointPNCG2D.drho (implicit/adjoint.py:277-283, drho_kernel :164-178), which
+ * returns the same product pre-multiplied by the density map's (1 - Emin). */
+int32_t d2f_adjoint_vjp(d2f_solver *s, const double *x_lin, const double *lam, double *dscale, double *dtension,
+                        void *stream);
+
 #ifdef __cplusplus
 }
 #endif
