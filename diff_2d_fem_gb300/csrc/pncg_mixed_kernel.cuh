@@ -1,27 +1,31 @@
-// pncg_mixed_kernel.cuh — the mixed-precision implicit step: FP32 iterations on increments
-// from the step-start state, FP64 where the reference's accuracy argument needs it.
+// pncg_mixed_kernel.cuh — the mixed-precision implicit step: FP32 iterations on small offsets
+// from an FP64 base state, FP64 where the reference's accuracy argument needs it.
 //
 // GB300 executes FP64 at ~1/64 of its FP32 rate, so in this path an iteration performs
 // (almost) no FP64 instruction:
 //
-//   * positions: x = x_n + dx with x_n the FP64 state at the start of the step and dx an
-//     FP32 increment. Everything an iteration needs is formed from dx plus per-step
-//     quantities computed once in FP64:
-//       - triangles: F = I + H, H = (dU0 + dx-differences) B, dU0 = the FP64 edge
-//         differences of (x_n - X_rest) rounded once per step — so F is formed from FP64
-//         edge differences, and the first Piola stress is evaluated in the
-//         cancellation-free form mu((J-1)I + J H - cof H)/J + la log1p(J-1)(I + cof H)/J;
-//       - inertia: x - x_hat = dx - dt e^(-dt c) v;
-//       - half-space colliders: phi = phi0 + n.dx with phi0 = n.(x_n - c) in FP64 per step,
-//         so the barrier distance keeps FP64 accuracy near contact; other collider shapes,
-//         IPC pairs, tendons and affine bodies evaluate in FP64 from x_n + dx;
-//       - friction: slip velocity dx / dt;
-//       - rigid modes: arms r = (x_n - c_n) + dx - (c - c_n).
+//   * the base: positions x = x_b + r with x_b an FP64 base state and r an FP32 offset, and
+//     the gradient g = g0 + (g - g0) with g0 the elastic, tendon and external forces at x_b
+//     evaluated in FP64 and kept as a compensated FP32 pair. The base starts at x_n (the
+//     state at the start of the step) and is rebuilt every REBASE iterations (x_b += r,
+//     r = 0, g0 at the new x_b), so r and the increments shrink as the solve converges:
+//     neither the FP32 resolution of the positions nor the large, mutually cancelling forces
+//     of a loaded body bound how far it converges (iterative refinement);
+//   * triangles: F = I + Hn + K, Hn = dU0 B with dU0 the FP64 edge differences of
+//     (x_b - X_rest) rounded once per rebuild, K = (r-differences) B; the gradient takes the
+//     stress increment P(F) - P(Fn) in a form without cancellation, the diagonal and the
+//     curvature the stress at F;
+//   * inertia: x - x_hat = dx - dt e^(-dt c) v with dx = (x_b - x_n) + r in FP32;
+//   * half-space colliders: phi = phi0 + n.dx with phi0 = n.(x_n - c) in FP64 per step,
+//     so the barrier distance keeps FP64 accuracy near contact; other collider shapes,
+//     IPC pairs, tendons and affine bodies evaluate in FP64 from x_b + r;
+//   * friction: slip velocity dx / dt;
+//   * rigid modes: arms a = (x_n - c_n) + dx - (c - c_n).
 //   * dot products: each thread accumulates its FP32 products with compensated (TwoSum)
 //     FP32 pairs, warps merge the pairs, and the per-warp partials are summed in FP64. The
 //     Dai-Kou beta, the step length, the convergence ratio and the energy model stay FP64.
 //   * step caps (inversion, CCD, |p|, clearance) are FP32 minima/maxima.
-// At the end of the step x = x_n + dx and v = (x - x_n)/dt in FP64.
+// At the end of the step x = x_b + r and v = (x - x_n)/dt in FP64.
 #pragma once
 #include <type_traits>
 
@@ -106,7 +110,7 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
 
 // Byte layout of the mixed path's per-step scratch (d2f_scene_desc.mscr), 256-aligned parts.
 struct MixedLayout {
-    size_t xd, xhv, fh, rarm, m32, du0, phi0, rcs, dref, total;
+    size_t xd, xhv, g0, xbd, xr, db, rarm, m32, du0, phi0, rcs, dref, total;
 };
 __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, long n_col, long n_rig) {
     auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -114,7 +118,10 @@ __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, lon
     size_t o = 0;
     L.xd = o; o = up(o + (size_t)N * 8);
     L.xhv = o; o = up(o + (size_t)N * 8);
-    L.fh = o; o = up(o + (size_t)N * 8);
+    L.g0 = o; o = up(o + (size_t)N * 16);
+    L.xbd = o; o = up(o + (size_t)N * 16);
+    L.xr = o; o = up(o + (size_t)N * 8);
+    L.db = o; o = up(o + (size_t)N * 8);
     L.rarm = o; o = up(o + (size_t)N * 8);
     L.m32 = o; o = up(o + (size_t)N * 4);
     L.du0 = o; o = up(o + (size_t)T * 16);
@@ -124,6 +131,28 @@ __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, lon
     L.total = o;
     return L;
 }
+
+// d len / d x at eyelet node n of a tendon (prv / nxt: neighbouring eyelet entries or -1),
+// FP64 positions from pos(node)
+template <class PosF>
+__device__ __forceinline__ double2 tendon_dlen(PosF pos, const int32_t *t_node, int prv, int nxt, int n) {
+    double gx = 0.0, gy = 0.0;
+    const double2 xn = pos(n);
+    if (prv >= 0) {
+        const double2 xa = pos(t_node[prv]);
+        const double tx = xn.x - xa.x, ty = xn.y - xa.y, ln = dmax(sqrt(tx * tx + ty * ty), 1.0e-12);
+        gx += tx / ln; gy += ty / ln;
+    }
+    if (nxt >= 0) {
+        const double2 xb = pos(t_node[nxt]);
+        const double tx = xb.x - xn.x, ty = xb.y - xn.y, ln = dmax(sqrt(tx * tx + ty * ty), 1.0e-12);
+        gx -= tx / ln; gy -= ty / ln;
+    }
+    return make_double2(gx, gy);
+}
+
+// iterations between rebuilds of the FP64 gradient base
+constexpr int REBASE = 32;
 
 // ---------------------------------------------------------------------- the kernel
 template <int NT, int MINB>
@@ -174,10 +203,15 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     unsigned char *ms = static_cast<unsigned char *>(d.mscr);
     float2 *__restrict__ XD = reinterpret_cast<float2 *>(ms + ML.xd);     // x - x_n
     float2 *__restrict__ XHV = reinterpret_cast<float2 *>(ms + ML.xhv);   // x_hat - x_n
-    float2 *__restrict__ FH = reinterpret_cast<float2 *>(ms + ML.fh);     // h^2 f
+    float4 *__restrict__ G0 = reinterpret_cast<float4 *>(ms + ML.g0);     // step-start gradient, FP32 pair
+    double2 *__restrict__ G0d = reinterpret_cast<double2 *>(ms + ML.g0);  // the same, FP64 while it is built
+    double2 *__restrict__ Esc64 = reinterpret_cast<double2 *>(d.escr);    // per-corner FP64 forces (setup only)
     float2 *__restrict__ RARM = reinterpret_cast<float2 *>(ms + ML.rarm); // x_n - c_n (rigid pieces)
     float *__restrict__ M32 = reinterpret_cast<float *>(ms + ML.m32);
-    float4 *__restrict__ DU0 = reinterpret_cast<float4 *>(ms + ML.du0);   // step-start displacement edges
+    float4 *__restrict__ DU0 = reinterpret_cast<float4 *>(ms + ML.du0);   // displacement edges at the base x_b
+    double2 *__restrict__ XBd = reinterpret_cast<double2 *>(ms + ML.xbd); // base positions x_b (FP64)
+    float2 *__restrict__ XR = reinterpret_cast<float2 *>(ms + ML.xr);     // x - x_b
+    float2 *__restrict__ DB = reinterpret_cast<float2 *>(ms + ML.db);     // x_b - x_n
     float *__restrict__ PHI0 = reinterpret_cast<float *>(ms + ML.phi0);   // half-space distances at x_n
     float2 *__restrict__ DREF = reinterpret_cast<float2 *>(ms + ML.dref); // dx when the candidate list was built
     float2 *__restrict__ RCS = reinterpret_cast<float2 *>(ms + ML.rcs);   // rigid pieces: centroid shift
@@ -207,10 +241,108 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             colmuf[tid] = (float)colmu[tid];
         }
 
-        auto xpos = [&](int n) -> double2 {  // FP64 position
-            const double2 a = Xn[n];
-            const float2 b = XD[n];
+        auto xpos = [&](int n) -> double2 {  // FP64 position x_b + (x - x_b)
+            const double2 a = XBd[n];
+            const float2 b = XR[n];
             return make_double2(a.x + (double)b.x, a.y + (double)b.y);
+        };
+        auto xbpos = [&](int n) -> double2 { return XBd[n]; };  // FP64 position at the base x_b
+
+        // The base of the iteration: positions x = x_b + r with x_b in FP64 and the offset r in
+        // FP32, and the gradient g = g0 + (g - g0) with g0 = elastic force + tendon force
+        // - h^2 f_ext at x_b evaluated in FP64 and kept as a compensated FP32 pair, the
+        // increment formed from r in FP32. Rebuilt at the step start and every REBASE
+        // iterations (x_b += r, r = 0): the offsets and increments shrink as the solve
+        // converges, so neither the positions' FP32 resolution nor the large, mutually
+        // cancelling forces of a loaded body limit how far it converges (iterative refinement).
+        auto build_base = [&]() {
+            for (int i = n0 + tid; i < n1; i += NT) {
+                const double2 b = XBd[i], xn = Xn[i];
+                const float2 r = XR[i];
+                const double2 xb = make_double2(b.x + (double)r.x, b.y + (double)r.y);
+                XBd[i] = xb;
+                XR[i] = make_float2(0.f, 0.f);
+                const float2 db = make_float2((float)(xb.x - xn.x), (float)(xb.y - xn.y));
+                DB[i] = db;
+                XD[i] = db;
+            }
+            __syncthreads();
+            for (int t = t0 + tid; t < t1; t += NT) {
+                const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
+                const double2 a0 = XBd[i0], a1 = XBd[i1], a2 = XBd[i2], r0 = Xr[i0], r1 = Xr[i1], r2 = Xr[i2];
+                const double e1x = (a1.x - a0.x) - (r1.x - r0.x), e1y = (a1.y - a0.y) - (r1.y - r0.y);
+                const double e2x = (a2.x - a0.x) - (r2.x - r0.x), e2y = (a2.y - a0.y) - (r2.y - r0.y);
+                DU0[t] = make_float4((float)e1x, (float)e1y, (float)e2x, (float)e2y);
+                const float4 Bf = Bm[t];
+                const double bx = Bf.x, by = Bf.y, bz = Bf.z, bw = Bf.w;
+                const double H00 = e1x * bx + e2x * bz, H01 = e1x * by + e2x * bw;
+                const double H10 = e1y * bx + e2y * bz, H11 = e1y * by + e2y * bw;
+                const double dH = H00 * H11 - H01 * H10, Jm1 = (H00 + H11) + dH, J = 1.0 + Jm1;
+                const double logJ = J > 1.0e-6 ? log1p(Jm1) : log(1.0e-6);
+                const double iJ = J != 0.0 ? 1.0 / J : 0.0;
+                const double mu = Mu[t], la = La[t], ll = la * logJ, onepJ = 1.0 + J;
+                // cancellation-free first Piola stress of F = I + H
+                const double P00 = mu * ((H00 * onepJ + dH) * iJ) + ll * ((1.0 + H11) * iJ);
+                const double P01 = mu * ((J * H01 + H10) * iJ) + ll * (-H10 * iJ);
+                const double P10 = mu * ((J * H10 + H01) * iJ) + ll * (-H01 * iJ);
+                const double P11 = mu * ((H11 * onepJ + dH) * iJ) + ll * ((1.0 + H00) * iJ);
+                const double hA = h2 * (double)Ar[t];
+                const double g1x = hA * (P00 * bx + P01 * by), g1y = hA * (P10 * bx + P11 * by);
+                const double g2x = hA * (P00 * bz + P01 * bw), g2y = hA * (P10 * bz + P11 * bw);
+                Esc64[3 * t] = make_double2(-(g1x + g2x), -(g1y + g2y));
+                Esc64[3 * t + 1] = make_double2(g1x, g1y);
+                Esc64[3 * t + 2] = make_double2(g2x, g2y);
+            }
+            __syncthreads();
+            for (int i = n0 + tid; i < n1; i += NT) {
+                double gx = 0.0, gy = 0.0;
+                for (int k = __ldg(d.inc_ptr + i); k < __ldg(d.inc_ptr + i + 1); ++k) {
+                    const double2 c = Esc64[__ldg(d.inc + k)];
+                    gx += c.x; gy += c.y;
+                }
+                if (d.fext) {
+                    const double2 f = Fx[i];
+                    gx -= h2 * f.x; gy -= h2 * f.y;
+                }
+                G0d[i] = make_double2(gx, gy);
+            }
+            __syncthreads();
+            if (sg.nten > 0) {  // tendon force at x_b (Tendon.grad_diag, actuation.py:169-228)
+                for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
+                    double L = 0.0;
+                    for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
+                        if (d.t_tid[j] != k) continue;
+                        const int m = d.t_nxt[j];
+                        if (m < 0) continue;
+                        const double2 xa = xbpos(d.t_node[j]), xb = xbpos(d.t_node[m]);
+                        const double ex = xb.x - xa.x, ey = xb.y - xa.y;
+                        L += sqrt(ex * ex + ey * ey);
+                    }
+                    double tau;
+                    if (d.t_stiff[k] > 0.0) {
+                        const double ext = L - d.t_L0[k];
+                        tau = ext > 0.0 ? d.t_stiff[k] * ext : 0.0;
+                    } else {
+                        tau = dmax(d.t_Tcmd[k], 0.0);
+                    }
+                    d.t_state[4 * k + 1] = tau;  // tension at x_b, read by the increments
+                }
+                __syncthreads();
+                for (int j = sg.tent0 + tid; j < sg.tent0 + sg.ntent; j += NT) {
+                    const int n = d.t_node[j];
+                    const double tau = d.t_state[4 * d.t_tid[j] + 1];
+                    const double2 g = tendon_dlen(xbpos, d.t_node, d.t_prv[j], d.t_nxt[j], n);
+                    atomicAdd(&G0d[n].x, h2 * tau * g.x);
+                    atomicAdd(&G0d[n].y, h2 * tau * g.y);
+                }
+                __syncthreads();
+            }
+            for (int i = n0 + tid; i < n1; i += NT) {  // to a compensated FP32 pair, in place
+                const double2 g = G0d[i];
+                const float hx = (float)g.x, hy = (float)g.y;
+                G0[i] = make_float4(hx, hy, (float)(g.x - (double)hx), (float)(g.y - (double)hy));
+            }
+            __syncthreads();
         };
 
         // ================================================================ step setup (FP64, once per step)
@@ -218,12 +350,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             const double2 xi = X[i], vi = Vv[i];
             Xn[i] = xi;
             XD[i] = make_float2(0.f, 0.f);
+            XBd[i] = xi;
+            XR[i] = make_float2(0.f, 0.f);
             XHV[i] = make_float2((float)(dt * d.drag * vi.x), (float)(dt * d.drag * vi.y));
             M32[i] = (float)d.mass[i];
-            if (d.fext) {
-                const double2 f = Fx[i];
-                FH[i] = make_float2((float)(h2 * f.x), (float)(h2 * f.y));
-            }
             G[i] = make_float2(0.f, 0.f);
             P[i] = make_float2(0.f, 0.f);
         }
@@ -234,12 +364,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             S.motion = 0.0; S.csx = 0.0; S.csy = 0.0;
         }
         __syncthreads();
-        for (int t = t0 + tid; t < t1; t += NT) {  // displacement edges at x_n, FP64 then rounded once
-            const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
-            const double2 a0 = Xn[i0], a1 = Xn[i1], a2 = Xn[i2], r0 = Xr[i0], r1 = Xr[i1], r2 = Xr[i2];
-            DU0[t] = make_float4((float)((a1.x - a0.x) - (r1.x - r0.x)), (float)((a1.y - a0.y) - (r1.y - r0.y)),
-                                 (float)((a2.x - a0.x) - (r2.x - r0.x)), (float)((a2.y - a0.y) - (r2.y - r0.y)));
-        }
         for (int j = tid; j < nbl; j += NT) {  // half-space distances at x_n
             const double2 xb = Xn[d.bnd[sg.bnd0 + j]];
             for (int k = 0; k < n_col; ++k) {
@@ -252,6 +376,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int n = d.bc_idx[b];
                 const double2 tg = Tgt[b], xn = Xn[n];
                 XD[n] = make_float2((float)(tg.x - xn.x), (float)(tg.y - xn.y));
+                XBd[n] = tg;
             }
         }
         // rigid pieces: step-start centroid c_n (FP64) and the arms x_n - c_n (FP32)
@@ -276,6 +401,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             if (tid == 0) { d.r_acc[3 * b] = cx; d.r_acc[3 * b + 1] = cy; d.r_acc[3 * b + 2] = c[2]; }
         }
         __syncthreads();
+
+        build_base();
 
         // ---------------------------------------------------------------- contact candidates
         // As in the FP64 kernel, but the list is rebuilt at every step start (x_n changed) and
@@ -527,7 +654,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int n = d.bc_idx[b];
                 const double2 tg = Tgt[b], x = xpos(n), xn = Xn[n];
                 const double2 nx = alpha_s >= 1.0 ? tg : make_double2(x.x + alpha_s * (tg.x - x.x), x.y + alpha_s * (tg.y - x.y));
+                const double2 xb = XBd[n];
                 XD[n] = make_float2((float)(nx.x - xn.x), (float)(nx.y - xn.y));
+                XR[n] = make_float2((float)(nx.x - xb.x), (float)(nx.y - xb.y));
             }
             __syncthreads();
         };
@@ -550,17 +679,24 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             }
             if (!S.active && !S.pending) break;
             if (S.status != 0) break;
+            if (it > 0 && it % REBASE == 0) build_base();
 
             // ---------------------------------------------- A1: triangles (gradient + diagonal)
             for (int t = t0 + tid; t < t1; t += NT) {
                 const int i0 = __ldg(d.tri + 3 * t), i1 = __ldg(d.tri + 3 * t + 1), i2 = __ldg(d.tri + 3 * t + 2);
                 const float4 B = Bm[t], du = DU0[t], Dm = Dmr[t];
                 const float A = Ar[t], mu = Mu[t], la = La[t];
-                const float2 u0 = XD[i0], u1 = XD[i1], u2 = XD[i2];
-                const float d1x = du.x + (u1.x - u0.x), d1y = du.y + (u1.y - u0.y);
-                const float d2x = du.z + (u2.x - u0.x), d2y = du.w + (u2.y - u0.y);
-                const float H00 = d1x * B.x + d2x * B.z, H01 = d1x * B.y + d2x * B.w;
-                const float H10 = d1y * B.x + d2y * B.z, H11 = d1y * B.y + d2y * B.w;
+                const float2 u0 = XR[i0], u1 = XR[i1], u2 = XR[i2];
+                const float q1x = u1.x - u0.x, q1y = u1.y - u0.y;  // edges of x - x_b
+                const float q2x = u2.x - u0.x, q2y = u2.y - u0.y;
+                const float d1x = du.x + q1x, d1y = du.y + q1y;
+                const float d2x = du.z + q2x, d2y = du.w + q2y;
+                // displacement gradient Hn at the base x_b and its increment K (F = I + Hn + K)
+                const float n00 = du.x * B.x + du.z * B.z, n01 = du.x * B.y + du.z * B.w;
+                const float n10 = du.y * B.x + du.w * B.z, n11 = du.y * B.y + du.w * B.w;
+                const float K00 = q1x * B.x + q2x * B.z, K01 = q1x * B.y + q2x * B.w;
+                const float K10 = q1y * B.x + q2y * B.z, K11 = q1y * B.y + q2y * B.w;
+                const float H00 = n00 + K00, H01 = n01 + K01, H10 = n10 + K10, H11 = n11 + K11;
                 const float dH = H00 * H11 - H01 * H10;
                 const float Jm1 = (H00 + H11) + dH;
                 const float J = 1.f + Jm1;
@@ -568,11 +704,23 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const float iJ = J != 0.f ? 1.f / J : 0.f;
                 const float G00 = (1.f + H11) * iJ, G01 = -H10 * iJ, G10 = -H01 * iJ, G11 = (1.f + H00) * iJ;
                 const float c1 = la * logJ - mu;
-                const float onepJ = 1.f + J, ll = la * logJ;
-                const float P00 = mu * ((H00 * onepJ + dH) * iJ) + ll * G00;
-                const float P01 = mu * ((J * H01 + H10) * iJ) + ll * G01;
-                const float P10 = mu * ((J * H10 + H01) * iJ) + ll * G10;
-                const float P11 = mu * ((H11 * onepJ + dH) * iJ) + ll * G11;
+                // stress increment P(F) - P(Fn) from small quantities only:
+                //   mu K + la (log J - log Jn) F^-T + (la log Jn - mu) (F^-T - Fn^-T),
+                //   J - Jn = cof(Fn):K + det K,  F^-T - Fn^-T = (cof(K) Jn - cof(Fn) (J - Jn)) / (J Jn)
+                const float Jnm1 = (n00 + n11) + (n00 * n11 - n01 * n10), Jn = 1.f + Jnm1;
+                const float dJ = ((1.f + n11) * K00 - n10 * K01) + ((1.f + n00) * K11 - n01 * K10) +
+                                 (K00 * K11 - K01 * K10);
+                const float logJn = Jn > 1.0e-6f ? log1pf(Jnm1) : logf(1.0e-6f);
+                const float dlogJ = (J > 1.0e-6f && Jn > 1.0e-6f) ? log1pf(dJ / Jn) : logJ - logJn;
+                const float c1n = la * logJn - mu;
+                const float iJJ = (J != 0.f && Jn != 0.f) ? 1.f / (J * Jn) : 0.f;
+                const float dG00 = (K11 * Jn - (1.f + n11) * dJ) * iJJ, dG01 = (n10 * dJ - K10 * Jn) * iJJ;
+                const float dG10 = (n01 * dJ - K01 * Jn) * iJJ, dG11 = (K00 * Jn - (1.f + n00) * dJ) * iJJ;
+                const float ld = la * dlogJ;
+                const float P00 = mu * K00 + ld * G00 + c1n * dG00;
+                const float P01 = mu * K01 + ld * G01 + c1n * dG01;
+                const float P10 = mu * K10 + ld * G10 + c1n * dG10;
+                const float P11 = mu * K11 + ld * G11 + c1n * dG11;
                 const float hA = fh2 * A;
                 const float g1x = hA * (P00 * B.x + P01 * B.y), g1y = hA * (P10 * B.x + P11 * B.y);
                 const float g2x = hA * (P00 * B.z + P01 * B.w), g2y = hA * (P10 * B.z + P11 * B.w);
@@ -680,11 +828,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         }
                     }
                 }
-                if (d.fext) {
-                    const float2 f = FH[i];
-                    gx -= f.x; gy -= f.y;
-                }
-                G[i] = make_float2(gx, gy);
+                const float4 g0 = G0[i];  // step-start gradient (FP32 pair) + this iteration's increments
+                G[i] = make_float2(g0.x + (g0.z + gx), g0.y + (g0.w + gy));
                 D[i] = make_float2(dxx, dyy);
             }
             __syncthreads();
@@ -738,10 +883,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         gLx -= sx; gLy -= sy;
                         geox += (1.0 - sx * sx) * il; geoy += (1.0 - sy * sy) * il;
                     }
+                    // the force at x_b is in g0: add the increment since x_b
+                    const double taun = d.t_state[4 * k + 1];
+                    const double2 gn = tendon_dlen(xbpos, d.t_node, d.t_prv[j], d.t_nxt[j], n);
                     float *gp_ = reinterpret_cast<float *>(G + n);
                     float *dp_ = reinterpret_cast<float *>(D + n);
-                    atomicAdd(gp_, (float)(h2 * tau * gLx));
-                    atomicAdd(gp_ + 1, (float)(h2 * tau * gLy));
+                    atomicAdd(gp_, (float)(h2 * (tau * gLx - taun * gn.x)));
+                    atomicAdd(gp_ + 1, (float)(h2 * (tau * gLy - taun * gn.y)));
                     atomicAdd(dp_, (float)(h2 * (tau * geox + keff * gLx * gLx)));
                     atomicAdd(dp_ + 1, (float)(h2 * (tau * geoy + keff * gLy * gLy)));
                 }
@@ -1217,7 +1365,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 __syncthreads();
             }
 
-            // ---------------------------------------------- D1: dx += alpha p (slaved nodes: J q - x_n)
+            // ---------------------------------------------- D1: r += alpha p, dx = (x_b - x_n) + r (slaved nodes: J q)
             {
                 const bool act = S.active != 0;
                 const float al = (float)S.alpha;
@@ -1225,12 +1373,16 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     const int ka = d.node_aff[i];
                     if (ka >= 0) {
                         const double *w = d.a_w + 3 * ka, *q = d.a_q + 6 * d.a_grp[ka];
-                        const double2 xn = Xn[i];
-                        XD[i] = make_float2((float)(w[0] * q[0] + w[1] * q[1] + w[2] * q[2] - xn.x),
-                                            (float)(w[0] * q[3] + w[1] * q[4] + w[2] * q[5] - xn.y));
+                        const double2 xn = Xn[i], xb = XBd[i];
+                        const double jx = w[0] * q[0] + w[1] * q[1] + w[2] * q[2];
+                        const double jy = w[0] * q[3] + w[1] * q[4] + w[2] * q[5];
+                        XD[i] = make_float2((float)(jx - xn.x), (float)(jy - xn.y));
+                        XR[i] = make_float2((float)(jx - xb.x), (float)(jy - xb.y));
                     } else if (act) {
-                        const float2 pp = P[i], u = XD[i];
-                        XD[i] = make_float2(u.x + al * pp.x, u.y + al * pp.y);
+                        const float2 pp = P[i], r = XR[i], db = DB[i];
+                        const float2 rn = make_float2(r.x + al * pp.x, r.y + al * pp.y);
+                        XR[i] = rn;
+                        XD[i] = make_float2(db.x + rn.x, db.y + rn.y);
                     }
                 }
                 __syncthreads();
@@ -1240,8 +1392,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         // ================================================================ commit (FP64)
         for (int i = n0 + tid; i < n1; i += NT) {
             const double2 xn = Xn[i];
-            const float2 u = XD[i];
-            const double2 xi = make_double2(xn.x + (double)u.x, xn.y + (double)u.y);
+            const double2 xi = xpos(i);
             X[i] = xi;
             Vv[i] = make_double2((xi.x - xn.x) * inv_dt, (xi.y - xn.y) * inv_dt);
         }
