@@ -159,6 +159,63 @@ def run_reference(args, rank, world):
         "e2e": {"value": val, "unit": "scene-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+# ----------------------------------------------------------------------------- gradients
+def measure_grads(args, dev):
+    """grads/s of the differentiation workload: a batch of tendon-driven arms, the loss
+    sum_b |x_tip,b - target_b|^2 after `grad_steps` steps, its gradient with respect to every
+    element's modulus (per pixel: 1024 values an arm) and every step's tendon tension, by the
+    checkpointed adjoint (checkpoints every 10 steps, replay in between). One gradient = one
+    forward rollout + its backward pass, timed with CUDA events after one short warm-up
+    rollout; grads/s = arms x gradients / time. The forward steps and their replay run in
+    mixed precision, the adjoint solves in FP64 at those states."""
+    import torch
+    from diff_2d_fem_gb300 import workloads, ImplicitIntegrator
+    from diff_2d_fem_gb300.adjoint import Rollout
+    T = args.grad_steps
+    m, kw, dt, ex = workloads.tendon_arms(args.arms, seed=0, steps=T)
+    integ = ImplicitIntegrator(**kw)
+    s = integ.attach(m, dt)
+    B, nt = args.arms, int(s.desc.T)
+    x0 = s.x.detach().clone()
+    tip = torch.as_tensor(ex["tip"], device=dev)
+    tgt = torch.as_tensor(ex["target"], device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def grad_once(steps, ckpt):
+        ro = Rollout(s, steps=steps, record=[steps], checkpoint_every=ckpt, rtol=1e-9, max_iter=20000,
+                     forward_precision="mixed")
+        E = torch.ones(nt, dtype=torch.float64, device=dev, requires_grad=True)
+        ten = torch.as_tensor(ex["tension"][:steps], device=dev).clone().requires_grad_(True)
+        v0 = torch.zeros_like(x0)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        out = ro(E, ten, x0, v0)
+        e1.record(stream)
+        loss = ((out[0][tip] - tgt) ** 2).sum()
+        loss.backward()
+        e2.record(stream)
+        torch.cuda.synchronize(dev)
+        ro.close()
+        return ro, E.grad, ten.grad, e0.elapsed_time(e1), e1.elapsed_time(e2), float(loss.item())
+
+    grad_once(2, 1)                                           # warm-up: buffers, launch paths
+    ro, gE, gT, f_ms, b_ms, loss = grad_once(T, 10)
+    its = ro.info["adjoint_total_iters"]
+    return {"value": B / ((f_ms + b_ms) / 1e3), "unit": "grads/s",
+            "workload": f"tendon_arms x{B} (16x64 px of 0.5 mm, E log-U[0.2,1.5] MPa per pixel, "
+                        f"tendon on node row 2, piecewise-linear tension in [0,50] N/m), {T} steps, dt {dt}",
+            "gradient": f"dL/dE per element ({nt // B} per arm) and dL/dtension per step; "
+                        "checkpoints every 10 steps",
+            "dtype": "forward and replay mixed-f32/f64, adjoint CG f64",
+            "ms_per_grad_batch": f_ms + b_ms, "forward_ms": f_ms, "backward_ms": b_ms,
+            "adjoint_cg_iters_per_solve_mean": float(its.mean() / T),
+            "adjoint_worst_status": int(np.abs(ro.info["adjoint_worst_status"]).max()),
+            "forward_unconverged_scene_steps": int(ro.info["forward_unconverged_steps"].sum()),
+            "replay_mismatch": ro.info["replay_mismatch"],
+            "grad_finite": bool(torch.isfinite(gE).all().item() and torch.isfinite(gT).all().item()),
+            "loss": loss}
+
+
 # ----------------------------------------------------------------------------- GPU arm
 def run_ours(args, rank, world):
     import torch
@@ -290,6 +347,9 @@ def run_ours(args, rank, world):
     d2h = int(x_pin.numel() * 8)
     x_e2e = x_pin.numpy().copy()
     m._solver.close()
+    torch.cuda.empty_cache()
+
+    grads = None if args.no_grads else measure_grads(args, dev)
 
     if rank != 0:
         if dist:
@@ -336,6 +396,7 @@ def run_ours(args, rank, world):
                      "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": launch_ms},
         "cpu_baseline": {"value": cpu_val, "unit": "scene-steps/s", "cores": threads, "kind": "port",
                          "sample": cpu_desc},
+        "grads": grads,
     }
     print(json.dumps(rec))
     if dist:
@@ -353,6 +414,9 @@ def main():
     ap.add_argument("--threads", type=int, default=0, help="launch shape; 0 = autotune")
     ap.add_argument("--bps", type=int, default=0)
     ap.add_argument("--tune-sample", type=int, default=1024)
+    ap.add_argument("--arms", type=int, default=256, help="differentiation workload: arms per batch")
+    ap.add_argument("--grad-steps", type=int, default=100, help="differentiation workload: steps")
+    ap.add_argument("--no-grads", action="store_true", help="skip the grads/s measurement")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only warmup + steps of the step kernel (for ncu)")
     args = ap.parse_args()

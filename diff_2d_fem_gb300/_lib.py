@@ -86,7 +86,7 @@ def load(build_if_missing: bool = True):
     L.d2f_step_noalloc.restype = _I
     L.d2f_mixed_scratch_bytes.argtypes = [_I, _I, _I, _I, _I]
     L.d2f_mixed_scratch_bytes.restype = C.c_size_t
-    L.d2f_adjoint_solve.argtypes = [_P, _P, _P, _P, _P, _P, _D, _I, _P, _P, _P]
+    L.d2f_adjoint_solve.argtypes = [_P, _P, _P, _P, _P, _P, _D, _I, _I, _P, _P, _P]
     L.d2f_adjoint_solve.restype = _I
     L.d2f_adjoint_vjp.argtypes = [_P, _P, _P, _P, _P, _P]
     L.d2f_adjoint_vjp.restype = _I

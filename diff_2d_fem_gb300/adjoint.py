@@ -82,6 +82,7 @@ class AdjointPNCG2D:
         self.status = torch.zeros(self.B, dtype=torch.int32, device=self.dev)
         self.worst_status = torch.zeros(self.B, dtype=torch.int32, device=self.dev)
         self.max_iters = torch.zeros(self.B, dtype=torch.int32, device=self.dev)
+        self.total_iters = torch.zeros(self.B, dtype=torch.int64, device=self.dev)
         self.solves = 0
 
     @property
@@ -111,24 +112,30 @@ class AdjointPNCG2D:
     def _x(self, x):
         return torch.as_tensor(x, dtype=torch.float64, device=self.dev).reshape(self.N, 2).contiguous()
 
-    def adjoint_solve(self, xk, rhs, rtol=1e-12, maxiter=20000, tension=None):
-        """Solve H(x_k) lam = rhs on the free DOFs for every scene (one launch). Returns lam
-        (N, 2), a device tensor; per-scene iterations and status in self.iters / self.status
-        (0 converged, 1 maxiter reached, -4 operator not positive along a direction), the
-        worst over all solves so far in self.worst_status / self.max_iters."""
+    def adjoint_solve(self, xk, rhs, rtol=1e-12, maxiter=20000, tension=None, guess=None):
+        """Solve H(x_k) lam = rhs on the free DOFs for every scene (one launch), from `guess`
+        (N, 2) if given, else from zero. Returns lam (N, 2), a device tensor; per-scene
+        iterations and status in self.iters / self.status (0 converged, 1 maxiter reached,
+        -4 operator not positive along a direction), the worst over all solves so far in
+        self.worst_status / self.max_iters, the sum of iterations in self.total_iters."""
         xk, rhs = self._x(xk), self._x(rhs)
-        lam = torch.empty((self.N, 2), dtype=torch.float64, device=self.dev)
+        if guess is not None:
+            lam = self._x(guess).clone()
+        else:
+            lam = torch.empty((self.N, 2), dtype=torch.float64, device=self.dev)
         tp = None
         if tension is not None:
             tp = C.c_void_p(tension.data_ptr())
         _lib.check(self.s.L.d2f_adjoint_solve(self.s.h, C.c_void_p(xk.data_ptr()), C.c_void_p(rhs.data_ptr()),
                                               C.c_void_p(lam.data_ptr()), C.c_void_p(self._work.data_ptr()), tp,
-                                              float(rtol), int(maxiter), C.c_void_p(self.iters.data_ptr()),
+                                              float(rtol), int(maxiter), int(guess is not None),
+                                              C.c_void_p(self.iters.data_ptr()),
                                               C.c_void_p(self.status.data_ptr()), self.s._stream_ptr()),
                    "d2f_adjoint_solve")
         worse = (self.status.abs() > self.worst_status.abs())
         self.worst_status.copy_(torch.where(worse, self.status, self.worst_status))
         torch.maximum(self.max_iters, self.iters, out=self.max_iters)
+        self.total_iters += self.iters.to(torch.int64)
         self.solves += 1
         return lam
 
@@ -147,7 +154,7 @@ class AdjointPNCG2D:
         self.vjp(xk, lam, d)
         return d / self.E * (1.0 - self.Emin)
 
-    def transient_adjoint(self, xs, seed, drag=None, rtol=1e-12, maxiter=20000):
+    def transient_adjoint(self, xs, seed, drag=None, rtol=1e-12, maxiter=20000, warm_start=True):
         """implicit/adjoint.py:371-399. xs = [x_0 .. x_T] (the forward states, arrays or
         tensors (N, 2)), seed = {k: dJ/dx_k (N, 2)}. Returns dJ/drho (n_tri,) as a device
         tensor, accumulated over the trajectory."""
@@ -161,7 +168,8 @@ class AdjointPNCG2D:
             rhs = (1.0 + dr) * m2 * lam1 - dr * m2 * lam2
             if k in seed:
                 rhs = rhs + self._x(seed[k])
-            lam = self.adjoint_solve(xs[k], rhs, rtol=rtol, maxiter=maxiter)
+            lam = self.adjoint_solve(xs[k], rhs, rtol=rtol, maxiter=maxiter,
+                                     guess=lam1 if (warm_start and k < T) else None)
             self.vjp(xs[k], lam, g)
             lam2, lam1 = lam1, lam
         return g / self.E * (1.0 - self.Emin)
@@ -192,12 +200,27 @@ class Rollout:
     None when the model has no tendon. x0, v0: (N, 2) initial state. `targets`, if given, is
     (steps, N, 2) kinematic targets per step (not differentiated; held DOFs carry no
     gradient). After a call, `info` has the forward's per-step convergence and the adjoint
-    solves' worst status."""
+    solves' worst status.
+
+    forward_precision="mixed" runs the forward steps and their replay with the mixed-precision
+    step (a second solver on the same problem) and linearises the FP64 adjoint at those states;
+    the replay then reproduces the forward to FP32 rounding of its tendon atomics instead of bit
+    for bit."""
 
     def __init__(self, solver, steps, record=None, checkpoint_every=8, rtol=1e-12, max_iter=20000,
-                 targets=None, Emin=1e-3):
+                 targets=None, Emin=1e-3, warm_start=True, forward_precision="fp64"):
         self.adj = AdjointPNCG2D(solver, Emin=Emin)
         self.s = self.adj.s
+        if forward_precision not in ("fp64", "mixed"):
+            raise ValueError("forward_precision must be 'fp64' or 'mixed'")
+        if forward_precision == "mixed":
+            from .device import DeviceSolver
+            self.fs = DeviceSolver(self.s.prob, precision="mixed", threads=self.s.desc.threads,
+                                   blocks_per_sm=self.s.desc.blocks_per_sm, device=self.s.dev, stream=self.s.stream)
+            self._fmu0 = self.fs.tensor("mu").clone()
+            self._flam0 = self.fs.tensor("lam").clone()
+        else:
+            self.fs = self.s
         self.steps = int(steps)
         if self.steps < 1:
             raise ValueError("steps must be >= 1")
@@ -206,6 +229,7 @@ class Rollout:
             raise ValueError("recorded steps must lie in 1..steps")
         self.K = max(1, int(checkpoint_every))
         self.rtol, self.max_iter = float(rtol), int(max_iter)
+        self.warm_start = bool(warm_start)
         self.targets = targets
         td = self.s.td
         self.n_ten = 0 if td is None else len(td["t2env"])
@@ -222,22 +246,32 @@ class Rollout:
 
     # ---- helpers
     def _set_step_commands(self, k, tension):
-        """Commands of step k (0-based)."""
+        """Commands of step k (0-based), on the forward solver."""
         if self.n_ten:
-            self.s.tensor("t_Tcmd").copy_(tension[k][self.ten_order])
+            self.fs.tensor("t_Tcmd").copy_(tension[k][self.ten_order])
         if self.targets is not None:
-            self.s.set_targets(np.asarray(self.targets[k]))
+            self.fs.set_targets(np.asarray(self.targets[k]))
 
     def _load_state(self, x, v):
-        self.s.x.copy_(x)
-        self.s.v.copy_(v)
+        self.fs.x.copy_(x)
+        self.fs.v.copy_(v)
+
+    def _set_modulus(self, E):
+        self.adj.set_modulus(E)
+        if self.fs is not self.s:
+            self.fs.tensor("mu").copy_(self._fmu0 * E.to(self._fmu0.dtype))
+            self.fs.tensor("lam").copy_(self._flam0 * E.to(self._flam0.dtype))
+
+    def close(self):
+        if self.fs is not self.s:
+            self.fs.close()
 
     def _forward(self, E, tension, x0, v0):
-        s, dev = self.s, self.s.dev
+        s, dev = self.fs, self.s.dev
         f64 = torch.float64
         self._E = E.detach().to(dev, f64).contiguous()
         self._tension = tension.detach().to(dev, f64).reshape(self.steps, self.n_ten).contiguous()
-        self.adj.set_modulus(self._E)
+        self._set_modulus(self._E)
         x = x0.detach().to(dev, f64).reshape(s.N, 2)
         v = v0.detach().to(dev, f64).reshape(s.N, 2)
         self._ckpt = {0: (x.clone(), v.clone())}
@@ -260,7 +294,7 @@ class Rollout:
         self.info = dict(forward_unconverged_steps=unconv.cpu().numpy(), forward_error=bad.cpu().numpy())
 
     def _backward(self, g_out):
-        s, adj, dev = self.s, self.adj, self.s.dev
+        s, adj, dev = self.fs, self.adj, self.s.dev
         f64 = torch.float64
         N, K = s.N, self.K
         g = {k: g_out[i].to(dev, f64).contiguous() for i, k in enumerate(self.record)}
@@ -273,7 +307,8 @@ class Rollout:
         dT_dev = torch.zeros((self.steps, max(self.n_ten, 1)), dtype=f64, device=dev)
         adj.worst_status.zero_()
         adj.max_iters.zero_()
-        adj.set_modulus(self._E)
+        adj.total_iters.zero_()
+        self._set_modulus(self._E)
         replay_mismatch = 0.0
         for c in reversed(range(0, self.steps, K)):
             e = min(c + K, self.steps)
@@ -291,7 +326,9 @@ class Rollout:
                 if k in g:
                     rhs = rhs + g[k]
                 tens = self._tension[k - 1][self.ten_order].contiguous() if self.n_ten else None
-                lam = adj.adjoint_solve(xk, rhs, rtol=self.rtol, maxiter=self.max_iter, tension=tens)
+                warm = self.warm_start and k < self.steps
+                lam = adj.adjoint_solve(xk, rhs, rtol=self.rtol, maxiter=self.max_iter, tension=tens,
+                                        guess=lam1 if warm else None)
                 adj.vjp(xk, lam, dscale, dT_dev[k - 1] if self.n_ten else None)
                 lam2, lam1 = lam1, lam
         self._load_state(*self._final)
@@ -304,5 +341,6 @@ class Rollout:
         dx0 = (m2 * lam1 - dr * m2 * lam2) * adj.free
         dv0 = (h * dr) * m2 * lam1 * adj.free
         self.info.update(adjoint_worst_status=adj.worst_status.cpu().numpy(),
-                         adjoint_max_iters=adj.max_iters.cpu().numpy(), replay_mismatch=replay_mismatch)
+                         adjoint_max_iters=adj.max_iters.cpu().numpy(),
+                         adjoint_total_iters=adj.total_iters.cpu().numpy(), replay_mismatch=replay_mismatch)
         return dE, dT, dx0, dv0

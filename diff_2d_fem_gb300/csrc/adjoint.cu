@@ -80,7 +80,8 @@ template <int NT>
 __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_scene_desc d, const double *__restrict__ xl,
                                                  const double *__restrict__ rhs, double *__restrict__ lam,
                                                  double *__restrict__ work, const double *__restrict__ tens, double rtol,
-                                                 int max_iter, int *__restrict__ iters_out, int *__restrict__ status_out) {
+                                                 int max_iter, int warm, int *__restrict__ iters_out,
+                                                 int *__restrict__ status_out) {
     constexpr int NW = NT / 32;
     __shared__ double red[NW * 4 + 4];
     __shared__ double s_col[MAXC][8];
@@ -101,8 +102,8 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
     const double *__restrict__ Ar = reinterpret_cast<const double *>(d.area);
     const double *__restrict__ Mu = reinterpret_cast<const double *>(d.mu);
     const double *__restrict__ La = reinterpret_cast<const double *>(d.lam);
-    double4_32a *__restrict__ Esc = reinterpret_cast<double4_32a *>(d.escr);   // .x .y: K v per corner; .z .w: diagonal
-    double *__restrict__ Ec = reinterpret_cast<double *>(d.ecache);   // F^-T, la log J - mu
+    double4_32a *__restrict__ Esc = reinterpret_cast<double4_32a *>(d.escr);  // .x .y: K v per corner; .z .w: diagonal
+    double *__restrict__ Ec = reinterpret_cast<double *>(d.ecache);          // F^-T, la log J - mu
     const double *__restrict__ TC = tens ? tens : d.t_Tcmd;
     if (tid < d.n_col && tid < MAXC)
         for (int q = 0; q < 8; ++q) s_col[tid][q] = d.colliders[8 * tid + q];
@@ -114,6 +115,83 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
         if (sc >= d.n_scenes) break;
         const d2f_seg sg = d.segs[sc];
         const int n0 = sg.node0, n1 = sg.node0 + sg.nn, t0 = sg.tri0, t1 = sg.tri0 + sg.nt;
+
+        // AP = (M + h^2 (K_elastic + K_collider + K_tendon)) V for this scene, all DOFs
+        auto hvp = [&](const double2 *__restrict__ V) {
+            // element pass: corner shares of h^2 K_elastic V (hvp_elastic_kernel, implicit/adjoint.py:69-84)
+            for (int t = t0 + tid; t < t1; t += NT) {
+                const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
+                const double *ec = Ec + 9 * (size_t)t;
+                const double G00 = ec[0], G01 = ec[1], G10 = ec[2], G11 = ec[3], c1 = ec[4];
+                const double2 p0 = V[i0], p1 = V[i1], p2 = V[i2];
+                const double4_32a B = Bm[t];
+                const double q1x = p1.x - p0.x, q1y = p1.y - p0.y, q2x = p2.x - p0.x, q2y = p2.y - p0.y;
+                const double f00 = q1x * B.x + q2x * B.z, f01 = q1x * B.y + q2x * B.w;
+                const double f10 = q1y * B.x + q2y * B.z, f11 = q1y * B.y + q2y * B.w;
+                const double mu = Mu[t], la = La[t];
+                const double GdF = G00 * f00 + G01 * f01 + G10 * f10 + G11 * f11;
+                // d2Psi/dF2 [dF] = mu dF + la (G:dF) G - (la log J - mu) G dF^T G
+                const double T00 = G00 * f00 + G01 * f01, T01 = G00 * f10 + G01 * f11;
+                const double T10 = G10 * f00 + G11 * f01, T11 = G10 * f10 + G11 * f11;
+                const double W00 = T00 * G00 + T01 * G10, W01 = T00 * G01 + T01 * G11;
+                const double W10 = T10 * G00 + T11 * G10, W11 = T10 * G01 + T11 * G11;
+                const double dP00 = mu * f00 + la * GdF * G00 - c1 * W00, dP01 = mu * f01 + la * GdF * G01 - c1 * W01;
+                const double dP10 = mu * f10 + la * GdF * G10 - c1 * W10, dP11 = mu * f11 + la * GdF * G11 - c1 * W11;
+                const double hA = h2 * Ar[t];
+                const double h1x = hA * (dP00 * B.x + dP01 * B.y), h1y = hA * (dP10 * B.x + dP11 * B.y);
+                const double h2x = hA * (dP00 * B.z + dP01 * B.w), h2y = hA * (dP10 * B.z + dP11 * B.w);
+                double4_32a *e = Esc + 3 * t;
+                e[0].x = -(h1x + h2x); e[0].y = -(h1y + h2y);
+                e[1].x = h1x; e[1].y = h1y;
+                e[2].x = h2x; e[2].y = h2y;
+            }
+            __syncthreads();
+            // node pass: inertia + gathered corners (ascending triangle) + frozen collider barrier
+            for (int i = n0 + tid; i < n1; i += NT) {
+                const double2 pi = V[i];
+                const double m = d.mass[i];
+                double ax = m * pi.x, ay = m * pi.y;
+                for (int k = d.inc_ptr[i]; k < d.inc_ptr[i + 1]; ++k) {
+                    const double4_32a c = Esc[d.inc[k]];
+                    ax += c.x; ay += c.y;
+                }
+                if (d.node_bslot[i] >= 0) {
+                    const double2 xi = XL[i];
+                    for (int k = 0; k < d.n_col; ++k) {
+                        double h00, h01, h11;
+                        collider_hessian(s_col[k], (int)s_col[k][0], xi.x, xi.y, d.dhat, d.kappa, h00, h01, h11);
+                        ax += h2 * (h00 * pi.x + h01 * pi.y);
+                        ay += h2 * (h01 * pi.x + h11 * pi.y);
+                    }
+                }
+                AP[i] = make_double2(ax, ay);
+            }
+            __syncthreads();
+            if (sg.nten > 0) {
+                // tendon (tension-controlled): geometric stiffness T/len (I - d d^T) per segment,
+                // the term of pHp_tendon_kernel (implicit/actuation.py:229-248)
+                for (int j = sg.tent0 + tid; j < sg.tent0 + sg.ntent; j += NT) {
+                    const int n = d.t_node[j], k = d.t_tid[j];
+                    const double tau = dmax(TC[k], 0.0);
+                    double ax = 0.0, ay = 0.0;
+                    const double2 xn = XL[n], pn = V[n];
+                    const int nb[2] = {d.t_prv[j], d.t_nxt[j]};
+                    for (int s2 = 0; s2 < 2; ++s2) {
+                        if (nb[s2] < 0) continue;
+                        const int o = d.t_node[nb[s2]];
+                        const double2 xo = XL[o], po = V[o];
+                        const double tx = xn.x - xo.x, ty = xn.y - xo.y, ln = dmax(sqrt(tx * tx + ty * ty), 1.0e-12);
+                        const double sx = tx / ln, sy = ty / ln;
+                        const double dx = pn.x - po.x, dy = pn.y - po.y, al = dx * sx + dy * sy;
+                        ax += tau / ln * (dx - al * sx);
+                        ay += tau / ln * (dy - al * sy);
+                    }
+                    atomicAdd(&AP[n].x, h2 * ax);
+                    atomicAdd(&AP[n].y, h2 * ay);
+                }
+                __syncthreads();
+            }
+        };
 
         // ---- tangent at x_lin: F^-T and (la log J - mu) per triangle, the Jacobi diagonal per corner
         for (int t = t0 + tid; t < t1; t += NT) {
@@ -139,8 +217,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
         }
         if (tid == 0) { s_stop = 0; s_status = 0; }
         __syncthreads();
-        // ---- preconditioner, r = b on the free DOFs, z = P r, p = z, lam = 0
-        double acc[2] = {0.0, 0.0};
+        // ---- the Jacobi preconditioner; the initial guess (0, or lam as given with warm)
         for (int i = n0 + tid; i < n1; i += NT) {
             const uint8_t fm = d.free_mask[i];
             const double m = d.mass[i];
@@ -157,99 +234,41 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                     dx += h2 * dmax(h00, 0.0); dy += h2 * dmax(h11, 0.0);
                 }
             }
-            const double2 b = B2[i];
-            const double ix = (fm & 1) ? 1.0 / dx : 0.0, iy = (fm & 2) ? 1.0 / dy : 0.0;
-            DI[i] = make_double2(ix, iy);
-            const double rx = (fm & 1) ? b.x : 0.0, ry = (fm & 2) ? b.y : 0.0;
+            DI[i] = make_double2((fm & 1) ? 1.0 / dx : 0.0, (fm & 2) ? 1.0 / dy : 0.0);
+            double2 l0 = make_double2(0.0, 0.0);
+            if (warm) {
+                const double2 l = LAM[i];
+                l0 = make_double2((fm & 1) ? l.x : 0.0, (fm & 2) ? l.y : 0.0);
+            }
+            LAM[i] = l0;
+            P[i] = l0;
+        }
+        __syncthreads();
+        if (warm) hvp(P);  // A lam0
+        // r = b - A lam0 on the free DOFs, z = D^-1 r, p = z
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int i = n0 + tid; i < n1; i += NT) {
+            const uint8_t fm = d.free_mask[i];
+            const double2 b = B2[i], di = DI[i];
+            const double2 a = warm ? AP[i] : make_double2(0.0, 0.0);
+            const double rx = (fm & 1) ? b.x - a.x : 0.0, ry = (fm & 2) ? b.y - a.y : 0.0;
             R[i] = make_double2(rx, ry);
-            const double zx = ix * rx, zy = iy * ry;
+            const double zx = di.x * rx, zy = di.y * ry;
             Z[i] = make_double2(zx, zy);
             P[i] = make_double2(zx, zy);
-            LAM[i] = make_double2(0.0, 0.0);
             acc[0] += rx * zx + ry * zy;
             acc[1] += rx * rx + ry * ry;
+            acc[2] += ((fm & 1) ? b.x * b.x : 0.0) + ((fm & 2) ? b.y * b.y : 0.0);
         }
-        bsum<NT, 2>(acc, red);
-        const double bb = acc[1];
+        bsum<NT, 3>(acc, red);
+        const double bb = acc[2];
         if (tid == 0) s_rz = acc[0];
         __syncthreads();
         int it = 0;
-        double rr = bb;
+        double rr = acc[1];
         for (; it < max_iter; ++it) {
             if (!(rr > rtol * rtol * bb) || s_stop) break;
-            // ---- element pass: corner shares of h^2 K_elastic p (hvp_elastic_kernel, implicit/adjoint.py:69-84)
-            for (int t = t0 + tid; t < t1; t += NT) {
-                const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
-                const double *ec = Ec + 9 * (size_t)t;
-                const double G00 = ec[0], G01 = ec[1], G10 = ec[2], G11 = ec[3], c1 = ec[4];
-                const double2 p0 = P[i0], p1 = P[i1], p2 = P[i2];
-                const double4_32a B = Bm[t];
-                const double q1x = p1.x - p0.x, q1y = p1.y - p0.y, q2x = p2.x - p0.x, q2y = p2.y - p0.y;
-                const double f00 = q1x * B.x + q2x * B.z, f01 = q1x * B.y + q2x * B.w;
-                const double f10 = q1y * B.x + q2y * B.z, f11 = q1y * B.y + q2y * B.w;
-                const double mu = Mu[t], la = La[t];
-                const double GdF = G00 * f00 + G01 * f01 + G10 * f10 + G11 * f11;
-                // G dF^T G
-                const double T00 = G00 * f00 + G01 * f01, T01 = G00 * f10 + G01 * f11;
-                const double T10 = G10 * f00 + G11 * f01, T11 = G10 * f10 + G11 * f11;
-                const double W00 = T00 * G00 + T01 * G10, W01 = T00 * G01 + T01 * G11;
-                const double W10 = T10 * G00 + T11 * G10, W11 = T10 * G01 + T11 * G11;
-                const double dP00 = mu * f00 + la * GdF * G00 - c1 * W00, dP01 = mu * f01 + la * GdF * G01 - c1 * W01;
-                const double dP10 = mu * f10 + la * GdF * G10 - c1 * W10, dP11 = mu * f11 + la * GdF * G11 - c1 * W11;
-                const double hA = h2 * Ar[t];
-                const double h1x = hA * (dP00 * B.x + dP01 * B.y), h1y = hA * (dP10 * B.x + dP11 * B.y);
-                const double h2x = hA * (dP00 * B.z + dP01 * B.w), h2y = hA * (dP10 * B.z + dP11 * B.w);
-                double4_32a *e = Esc + 3 * t;
-                e[0].x = -(h1x + h2x); e[0].y = -(h1y + h2y);
-                e[1].x = h1x; e[1].y = h1y;
-                e[2].x = h2x; e[2].y = h2y;
-            }
-            __syncthreads();
-            // ---- node pass: A p = M p + gathered K p + frozen collider barrier
-            for (int i = n0 + tid; i < n1; i += NT) {
-                const double2 pi = P[i];
-                const double m = d.mass[i];
-                double ax = m * pi.x, ay = m * pi.y;
-                for (int k = d.inc_ptr[i]; k < d.inc_ptr[i + 1]; ++k) {
-                    const double4_32a c = Esc[d.inc[k]];
-                    ax += c.x; ay += c.y;
-                }
-                if (d.node_bslot[i] >= 0) {
-                    const double2 xi = XL[i];
-                    for (int k = 0; k < d.n_col; ++k) {
-                        double h00, h01, h11;
-                        collider_hessian(s_col[k], (int)s_col[k][0], xi.x, xi.y, d.dhat, d.kappa, h00, h01, h11);
-                        ax += h2 * (h00 * pi.x + h01 * pi.y);
-                        ay += h2 * (h01 * pi.x + h11 * pi.y);
-                    }
-                }
-                AP[i] = make_double2(ax, ay);
-            }
-            __syncthreads();
-            if (sg.nten > 0) {
-                // tendon: geometric stiffness T/len (I - d d^T) per segment, plus k dL dL^T while
-                // taut (length-controlled); the same terms as pHp_tendon_kernel (implicit/actuation.py:229-256)
-                for (int j = sg.tent0 + tid; j < sg.tent0 + sg.ntent; j += NT) {
-                    const int n = d.t_node[j], k = d.t_tid[j];
-                    double tau = dmax(TC[k], 0.0);
-                    double ax = 0.0, ay = 0.0;
-                    const double2 xn = XL[n], pn = P[n];
-                    const int nb[2] = {d.t_prv[j], d.t_nxt[j]};
-                    for (int s2 = 0; s2 < 2; ++s2) {
-                        if (nb[s2] < 0) continue;
-                        const int o = d.t_node[nb[s2]];
-                        const double2 xo = XL[o], po = P[o];
-                        const double tx = xn.x - xo.x, ty = xn.y - xo.y, ln = dmax(sqrt(tx * tx + ty * ty), 1.0e-12);
-                        const double sx = tx / ln, sy = ty / ln;
-                        const double dx = pn.x - po.x, dy = pn.y - po.y, al = dx * sx + dy * sy;
-                        ax += tau / ln * (dx - al * sx);
-                        ay += tau / ln * (dy - al * sy);
-                    }
-                    atomicAdd(&AP[n].x, h2 * ax);
-                    atomicAdd(&AP[n].y, h2 * ay);
-                }
-                __syncthreads();
-            }
+            hvp(P);
             // ---- alpha = rz / p.Ap
             double pa[1] = {0.0};
             for (int i = n0 + tid; i < n1; i += NT) {
@@ -259,7 +278,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
             }
             bsum<NT, 1>(pa, red);
             if (tid == 0) {
-                if (!(pa[0] > 0.0)) { s_stop = 1; s_status = D2F_ENAN; }   // not positive definite along p
+                if (!(pa[0] > 0.0)) { s_stop = 1; s_status = D2F_ENAN; }  // not positive definite along p
                 s_alpha = pa[0] > 0.0 ? s_rz / pa[0] : 0.0;
             }
             __syncthreads();
@@ -362,8 +381,8 @@ __global__ void vjp_tension_kernel(const __grid_constant__ d2f_scene_desc d, con
 extern "C" {
 
 int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs, double *lam, double *work,
-                          const double *tension, double rtol, int32_t max_iter, int32_t *iters, int32_t *status,
-                          void *stream) {
+                          const double *tension, double rtol, int32_t max_iter, int32_t warm_start, int32_t *iters,
+                          int32_t *status, void *stream) {
     g_err[0] = 0;
     if (!s || !x_lin || !rhs || !lam || !work || !iters || !status)
         return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: null argument");
@@ -374,9 +393,19 @@ int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs,
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(s->d.work, 0, 4 * sizeof(int32_t), st) != cudaSuccess)
         return d2f_fail(D2F_ECUDA, "d2f_adjoint_solve: cudaMemsetAsync failed");
-    int grid = s->grid;
-    d2f::adj::pcg_kernel<128><<<grid > 0 ? grid : 1, 128, 0, st>>>(s->d, x_lin, rhs, lam, work, tension, rtol, max_iter,
-                                                                  iters, status);
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return d2f_fail(D2F_ECUDA, "d2f_adjoint_solve: no CUDA device");
+    // few scenes: 256 threads a scene, one block per SM at most; else 128 threads, 4 per SM
+    const bool wide = d2f_default_threads(s->d) >= 256;
+    int grid = nsm * (wide ? 1 : 4);
+    if (grid > s->d.n_scenes) grid = s->d.n_scenes;
+    if (wide)
+        d2f::adj::pcg_kernel<256><<<grid, 256, 0, st>>>(s->d, x_lin, rhs, lam, work, tension, rtol, max_iter,
+                                                       warm_start ? 1 : 0, iters, status);
+    else
+        d2f::adj::pcg_kernel<128><<<grid, 128, 0, st>>>(s->d, x_lin, rhs, lam, work, tension, rtol, max_iter,
+                                                       warm_start ? 1 : 0, iters, status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         snprintf(g_err, sizeof g_err, "d2f_adjoint_solve: launch failed: %s", cudaGetErrorString(e));

@@ -31,6 +31,16 @@ static void pick_variant(int nt, int bps, int *vnt, int *vminb) {
     *vminb = 4;
 }
 
+// Threads per scene block when the caller leaves it to the library: 256 when the batch has
+// at most two scenes per SM (few blocks: each needs more threads to hide latency), else 128.
+int d2f_default_threads(const d2f_scene_desc &d) {
+    if (d.threads) return d.threads;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 128;
+    return d.n_scenes <= 2 * nsm ? 256 : 128;
+}
+
 static int occupancy(const d2f_scene_desc &d, int smem, int vnt, int vminb) {
     return d.precision == D2F_MIXED ? d2f::occupancy_mixed(vnt, vminb, smem) : d2f::occupancy_fp64(vnt, vminb, smem);
 }
@@ -89,7 +99,7 @@ static int launch_shape(const d2f_scene_desc &d, int *grid, int *smem) {
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return fail(D2F_ECUDA, "d2f: no CUDA device");
     int vnt, vminb;
-    pick_variant(d.threads ? d.threads : 128, d.blocks_per_sm, &vnt, &vminb);
+    pick_variant(d2f_default_threads(d), d.blocks_per_sm, &vnt, &vminb);
     const int occ = occupancy(d, *smem, vnt, vminb);
     const int bps = d.blocks_per_sm > 0 ? (d.blocks_per_sm < occ ? d.blocks_per_sm : occ) : occ;
     *grid = nsm * bps;
@@ -99,7 +109,7 @@ static int launch_shape(const d2f_scene_desc &d, int *grid, int *smem) {
 
 static cudaError_t launch(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
     int vnt, vminb;
-    pick_variant(d.threads ? d.threads : 128, d.blocks_per_sm, &vnt, &vminb);
+    pick_variant(d2f_default_threads(d), d.blocks_per_sm, &vnt, &vminb);
     return d.precision == D2F_MIXED ? d2f::launch_mixed(vnt, vminb, d, grid, smem, st)
                                     : d2f::launch_fp64(vnt, vminb, d, grid, smem, st);
 }

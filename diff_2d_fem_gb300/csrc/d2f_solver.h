@@ -10,3 +10,4 @@ struct d2f_solver {
 
 extern thread_local char g_err[512];
 int d2f_fail(int code, const char *msg);
+int d2f_default_threads(const d2f_scene_desc &d);

@@ -1166,7 +1166,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
 // Launch shapes the library is built with: (threads per scene block, minimum resident
 // blocks per SM the register budget is fitted to). d2f_scene_desc.threads / blocks_per_sm
 // select one; the autotuner (tune.py) measures them.
-#define D2F_VARIANTS(X) X(32, 16) X(64, 8) X(128, 4) X(256, 3)
+#define D2F_VARIANTS(X) X(32, 16) X(64, 8) X(128, 4) X(256, 2) X(256, 3)
 
 namespace d2f {
 // one translation unit per precision instantiates the variants (pncg_fp64.cu, pncg_mixed.cu)

@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-VARIANTS = [(32, 16), (64, 8), (128, 4), (256, 3)]
+VARIANTS = [(32, 16), (64, 8), (128, 4), (256, 2), (256, 3)]
 _CACHE = {}
 
 

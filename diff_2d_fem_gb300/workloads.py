@@ -6,6 +6,10 @@
                          W ~ U{32..128} pixels of 0.75 mm, per-pixel E log-uniform in
                          [0.1, 2] MPa, ground mu ~ U[0.3, 0.9] per scene, top-edge pressure
                          ~ U[0, 5] kPa): the batching configuration
+  tendon_arms()          a batch of soft arms (16 x 64 pixels of 0.5 mm) pinned at one end
+                         and bent by a tension-controlled tendon, per-pixel E log-uniform
+                         in [0.2, 1.5] MPa, a piecewise-linear tension schedule and a target
+                         point per arm: the differentiation configuration
 
 Each returns (model, integrator kwargs, dt). No dataset is involved: the scenes are drawn
 from numpy.random.default_rng(seed) with the stated distributions.
@@ -60,3 +64,49 @@ def rectangles_on_ground(n_scenes=4096, seed=0, px=0.75e-3, gtol=1e-6):
     m._fext = f
     m._ctrl_version += 1
     return m, dict(gtol=gtol), 2e-3
+
+
+def tension_schedule(rng, n_scenes, steps=100, knots=6, lo=0.0, hi=50.0):
+    """(steps, n_scenes) piecewise-linear tension schedules: `knots` values U[lo, hi] per
+    scene at evenly spaced steps, linear in between."""
+    kk = np.linspace(0.0, steps - 1, knots)
+    vals = rng.uniform(lo, hi, (n_scenes, knots))
+    t = np.arange(steps, dtype=np.float64)
+    return np.stack([np.interp(t, kk, vals[i]) for i in range(n_scenes)], 1)
+
+
+def tendon_arms(n_scenes=256, seed=0, px=0.5e-3, steps=100):
+    """The differentiation configuration: n_scenes soft arms, each a 16 x 64-pixel mask
+    (8 mm x 32 mm) pinned at its first node column, per-pixel E log-uniform in [0.2, 1.5] MPa
+    (nu 0.40, density 1100), a tension-controlled tendon through the nodes of node row 2
+    (counted from the bottom), a `steps`-step piecewise-linear tension schedule in [0, 50] N/m
+    and a target point for the tip node (the tendon's last eyelet) within 4 mm of its rest
+    position. No gravity, no contact.
+
+    Returns (model, integrator kwargs, dt, extras), extras = dict(handles, E_pixels
+    (n, 16, 64), tension (steps, n), tip (n,) node indices, target (n, 2), tendons (n,))."""
+    rng = np.random.default_rng(seed)
+    H, W = 16, 64
+    m = Model()
+    hs, Es = [], []
+    for i in range(n_scenes):
+        E = np.exp(rng.uniform(np.log(2.0e5), np.log(1.5e6), (H, W)))
+        Es.append(E)
+        hs.append(m.add_soft_body(np.ones((H, W), np.uint8), physical_size=(W * px, H * px),
+                                  center=(0.5 * W * px, 0.5 * H * px), E=E, nu=0.40, density=1100.0,
+                                  env_id=i))
+    m.finalize()
+    tips, tendons, targets = [], [], []
+    for i, h in enumerate(hs):
+        X = m.rest_x(h)
+        m.set_kinematic_constraint(h, np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0])
+        row = np.where(np.abs(X[:, 1] - (X[:, 1].min() + 2 * px)) < 1e-9)[0]
+        row = row[np.argsort(X[row, 0])]
+        tendons.append(m.add_tendon(h, nodes=row))
+        tip = int(m.body_nodes(h)[row[-1]])
+        tips.append(tip)
+        targets.append(m.me.rest_pos[tip] + rng.uniform(-4e-3, 4e-3, 2))
+    tension = tension_schedule(rng, n_scenes, steps)
+    kw = dict(self_collision=False, friction=False, precision="fp64")
+    return m, kw, 2e-3, dict(handles=hs, E_pixels=np.stack(Es), tension=tension, tip=np.asarray(tips),
+                            target=np.asarray(targets), tendons=np.asarray(tendons))

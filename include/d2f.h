@@ -124,7 +124,8 @@ typedef struct d2f_scene_desc {
     double ccd_eta, cg_guard, gtol;
     double ipc_mu, ipc_dhat, ipc_kappa, reach, gap, bc_floor, skin;
     int32_t iter_max, conv_check, friction, per_body;
-    int32_t threads;             /* threads per scene block: 32, 64, 128 or 256 (0: 128) */
+    int32_t threads;             /* threads per scene block: 32, 64, 128 or 256 (0: 256 for at most two
+                                    scenes per SM, else 128) */
     int32_t blocks_per_sm;       /* resident scene blocks per SM the register budget targets
                                     (0: the library's default for that width) */
 } d2f_scene_desc;
@@ -191,7 +192,9 @@ int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream);
  *     (M + h^2 (K_elastic + K_collider + K_tendon)) lam = rhs      on the free DOFs,
  * with the collider contact gate frozen at x_lin and friction left out, by Jacobi-
  * preconditioned CG run on the device, one thread block per scene. `rhs` (N x 2) is read on
- * the free DOFs only; `lam` (N x 2) gets the solution, zero on the kinematic DOFs. `work`
+ * the free DOFs only; `lam` (N x 2) gets the solution, zero on the kinematic DOFs; with
+ * warm_start != 0 the CG starts from the `lam` passed in (e.g. the next step's adjoint,
+ * which a step's adjoint is close to), else from zero. `work`
  * is 10 N doubles of scratch. `tension` (n_ten, device, or NULL = desc->t_Tcmd) is the
  * tension of each tension-controlled tendon at this step. A scene stops when
  * |r| <= rtol |rhs| or after max_iter iterations; per scene, `iters` (device, n_scenes)
@@ -203,8 +206,8 @@ int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream);
  * Replaces AdjointPNCG2D.adjoint_solve (implicit/adjoint.py:339-369), whose MINRES runs on
  * the host and crosses to the device twice per matrix-vector product. */
 int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs, double *lam, double *work,
-                          const double *tension, double rtol, int32_t max_iter, int32_t *iters, int32_t *status,
-                          void *stream);
+                          const double *tension, double rtol, int32_t max_iter, int32_t warm_start, int32_t *iters,
+                          int32_t *status, void *stream);
 
 /* Vector-Jacobian products of one step's residual, accumulated for a solved lam:
  *   dscale[t]   += -h^2 lam . f_t(x_lin)    (f_t: triangle t's elastic force at its current

@@ -193,3 +193,86 @@ def test_adjoint_refuses_what_it_has_no_tangent_for():
     with pytest.raises(ValueError):
         AdjointPNCG2D(m)
     m.close()
+
+
+def test_tendon_arm_central_differences_32_entries():
+    """The differentiation configuration on one arm: 100 steps at dt 2e-3, loss = squared
+    distance of the tip to a target. 32 seeded entries — 24 pixel moduli, 8 step tensions —
+    each perturbed by +/- h relative in copies of the arm inside one batch of 65 scenes;
+    central differences against the adjoint gradient of the base copy to 1e-4, relative to
+    the entry (or to 1 % of the largest checked entry, for the entries smaller than that).
+    h = 1e-3: at h = 1e-6 the differences are dominated by the forward solve's convergence
+    floor (positions to ~1e-12 relative), not by the gradient; the truncation error of
+    central differences at 1e-3 is O(h^2) ~ 1e-6 relative."""
+    torch = _torch()
+    from diff_2d_fem_gb300 import workloads, scene, ImplicitIntegrator
+    from diff_2d_fem_gb300.adjoint import Rollout
+    T, h = 100, 1e-3
+    m, kw, dt, ex = workloads.tendon_arms(1, seed=5, steps=T)
+    base = scene.solver_problem(m, ImplicitIntegrator(**kw), dt)
+    base["eps"], base["iter_max"], base["tol_x"] = 0.0, 1000, 0.0     # fully converged steps
+    N1, T1 = np.asarray(base["x"]).shape[0], len(base["tri"])
+    rng = np.random.default_rng(11)
+    quad = np.asarray(m.me.tri_quad)                                   # triangle -> pixel
+    pix = rng.choice(np.unique(quad), 24, replace=False)
+    steps_k = np.sort(rng.choice(np.arange(T), 8, replace=False))
+    ten1 = ex["tension"][:, 0]
+    nb = 1 + 2 * 32
+    prob = tile_problem(base, nb)
+    E = np.ones((nb, T1))
+    ten = np.tile(ten1[:, None], (1, nb))
+    for j, p in enumerate(pix):
+        E[1 + 2 * j, quad == p] = 1 + h
+        E[2 + 2 * j, quad == p] = 1 - h
+    for j, k in enumerate(steps_k):
+        c = 1 + 2 * (24 + j)
+        ten[k, c], ten[k, c + 1] = ten1[k] * (1 + h), ten1[k] * (1 - h)
+    s = _device_solver(prob)
+    dev = s.dev
+    ro = Rollout(s, steps=T, checkpoint_every=10, rtol=1e-14, max_iter=50000)
+    Et = torch.tensor(E.reshape(-1), device=dev, requires_grad=True)
+    Tt = torch.tensor(ten, device=dev, requires_grad=True)
+    x0 = torch.tensor(np.asarray(prob["x"]), device=dev)
+    v0 = torch.zeros_like(x0)
+    out = ro(Et, Tt, x0, v0)[0].reshape(nb, N1, 2)
+    tip = int(ex["tip"][0])
+    L = ((out[:, tip] - torch.as_tensor(ex["target"][0], device=dev)) ** 2).sum(dim=1)
+    L.sum().backward()
+    assert int(np.abs(ro.info["adjoint_worst_status"]).max()) == 0
+    Lh = L.detach().cpu().numpy()
+    gE = Et.grad.reshape(nb, T1)[0].cpu().numpy()
+    gT = Tt.grad[:, 0].cpu().numpy()
+    fd = np.array([(Lh[1 + 2 * j] - Lh[2 + 2 * j]) / (2 * h) for j in range(32)])
+    adj = np.concatenate([[gE[quad == p].sum() for p in pix], gT[steps_k] * ten1[steps_k]])
+    err = np.abs(fd - adj) / np.maximum(np.abs(adj), 1e-2 * np.abs(adj).max())
+    assert err.max() < 1e-4, (err.max(), fd[err.argmax()], adj[err.argmax()], np.abs(adj).max())
+    s.close()
+
+
+def test_rollout_with_mixed_forward_matches_fp64_forward():
+    """The same gradients with the forward and its replay in mixed precision (the FP64 adjoint
+    linearised at the mixed states): within 1e-6 of the all-FP64 rollout's on the tendon
+    cantilever, converged steps."""
+    torch = _torch()
+    from diff_2d_fem_gb300.adjoint import Rollout
+    prob = _tendon()
+    prob["iter_max"], prob["eps"] = 3000, 0.0
+    T = 4
+    rng = np.random.default_rng(2)
+    E = 0.8 + 0.4 * rng.random(len(prob["mu"]))
+    tens = np.array([[5.0 + 5.0 * k] for k in range(T)])
+    w = rng.standard_normal((np.asarray(prob["x"]).shape[0], 2))
+    grads = []
+    for fp in ("fp64", "mixed"):
+        s = _device_solver(prob)
+        ro = Rollout(s, steps=T, checkpoint_every=2, rtol=1e-14, forward_precision=fp)
+        Et = torch.tensor(E, device=s.dev, requires_grad=True)
+        Tt = torch.tensor(tens, device=s.dev, requires_grad=True)
+        x0 = torch.tensor(np.asarray(prob["x"]), device=s.dev)
+        out = ro(Et, Tt, x0, torch.zeros_like(x0))
+        (out[0] * torch.as_tensor(w, device=s.dev)).sum().backward()
+        grads.append((Et.grad.cpu().numpy(), Tt.grad.cpu().numpy()))
+        ro.close()
+        s.close()
+    assert rel_err(grads[1][0], grads[0][0]) < 1e-6
+    assert rel_err(grads[1][1], grads[0][1]) < 1e-6
