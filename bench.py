@@ -134,6 +134,17 @@ def cpu_sample(prob, state_x, state_v, n_threads, per_thread, seed=1):
     return n / dt, f"{n} of {B} scenes x 1 step, {len(solvers)} threads x {per_thread} scenes, {dt:.1f} s"
 
 
+def _reference_status():
+    """Whether the reference installed under baseline/_ref imports here (it needs warp-lang)."""
+    ref = os.path.join(os.path.dirname(os.path.abspath(__file__)), "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref, "Diff_2D_FEM")):
+        return "reference not installed under baseline/_ref"
+    import importlib.util
+    if importlib.util.find_spec("warp") is None:
+        return "reference installed under baseline/_ref but not importable (warp-lang absent on this box)"
+    return "warp-lang present, but the reference's CPU path is not wired into this arm"
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -154,8 +165,8 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)", "config": {"workload": f"rectangles_on_ground x{args.scenes}", "dt": dt},
         "cpu_baseline": {"value": val, "unit": "scene-steps/s", "cores": threads, "kind": "port",
-                         "sample": desc + "; reference CPU path unavailable (warp-lang not installed), "
-                                          "timing its serial C restatement"},
+                         "sample": desc + "; " + _reference_status() + ", so this times the oracle port "
+                                          "(the reference's step restated serially in C)"},
         "e2e": {"value": val, "unit": "scene-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
