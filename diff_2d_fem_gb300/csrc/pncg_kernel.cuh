@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
     __shared__ double red[NW * 20 + 20];
     __shared__ int sc_next;
     __shared__ int s_wcnt[NW];
+    __shared__ unsigned s_wmask[NW];
     __shared__ double s_H6[6][6], s_L6[6][6];
     __shared__ double colmu[MAX_COL];
     extern __shared__ float2 pos32[];  // boundary positions for the candidate-list rebuild
@@ -435,16 +436,35 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
         // The reference's serial order for the ACCD cap: each edge reads the cap once, as the
         // edges before it left it, and its pairs lower it (ipc_contact.py:211, 241). Replayed
         // by one thread over the ordered candidate list from the per-pair profiles.
-        auto tc_scan = [&](double m0) -> double {
+        auto tc_scan = [&](double m0) -> double {  // every thread calls; the result is thread 0's
+            // A pair whose profile threshold T is >= m0 leaves the running minimum untouched at
+            // any cap <= m0 (accd_profile: accd(m) = m for m <= T), so only the pairs with
+            // T < m0 are replayed — found by warp ballots in candidate order, walked in that
+            // order by thread 0 with the same per-edge reset: the result equals the full serial
+            // replay.
             double m = m0, t_c = m0;
             int prevk = -1;
             const int nc = S.ncand;
-#pragma unroll 4
-            for (int c = 0; c < nc; ++c) {
-                const int k = (int)((unsigned)d.cand[sg.cand0 + c] >> 16);
-                const double2 pr = Ctr[sg.cand0 + c];
-                if (k != prevk) { t_c = m; prevk = k; }
-                m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+            for (int base = 0; base < nc; base += NT) {
+                const int c = base + tid;
+                const bool rel = c < nc && Ctr[sg.cand0 + c].x < m0;
+                const unsigned bal = __ballot_sync(0xffffffffu, rel);
+                if ((tid & 31) == 0) s_wmask[tid >> 5] = bal;
+                __syncthreads();
+                if (tid == 0) {
+                    for (int w = 0; w < NW; ++w) {
+                        unsigned msk = s_wmask[w];
+                        while (msk) {
+                            const int cc = base + w * 32 + (__ffs(msk) - 1);
+                            msk &= msk - 1;
+                            const int k = (int)((unsigned)d.cand[sg.cand0 + cc] >> 16);
+                            const double2 pr = Ctr[sg.cand0 + cc];
+                            if (k != prevk) { t_c = m; prevk = k; }
+                            m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+                        }
+                    }
+                }
+                __syncthreads();
             }
             return m;
         };
@@ -463,8 +483,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             double v[1] = {qi};
             const int ops[1] = {1};
             block_reduce<NT, 1>(v, ops, red);
+            const double a_tc = tc_scan(1.0);
             if (tid == 0) {
-                double a_s = tc_scan(1.0);
+                double a_s = a_tc;
                 if (v[0] > 0.0) a_s = dmin(a_s, 0.45 * d.reach / v[0]);
                 S.alpha_s = a_s;
             }
@@ -1076,12 +1097,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 double v[4] = {acc_pHp, acc_pinf, acc_clr, acc_alpha};
                 const int ops[4] = {0, 1, 2, 2};
                 block_reduce<NT, 4>(v, ops, red);
+                const double a_ccd = scene_ipc ? tc_scan(d.alpha_max) : 0.0;   // ACCD, reference order
                 // ---------------------------------------------- B5: step length and convergence
                 if (tid == 0) {
                     const double ph = v[0], pinf = v[1], clr = v[2];
                     double a = v[3];
                     if (scene_ipc) {
-                        a = dmin(a, tc_scan(d.alpha_max));                       // ACCD, reference order
+                        a = dmin(a, a_ccd);
                         if (pinf > 0.0) a = dmin(a, 0.45 * d.reach / pinf);      // ipc_far_cap_kernel
                     }
                     S.pHp = ph; S.p_inf = pinf; S.clr_min = clr;

@@ -166,6 +166,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     __shared__ float mres[8];
     __shared__ int sc_next;
     __shared__ int s_wcnt[NW];
+    __shared__ unsigned s_wmask[NW];
     __shared__ double s_H6[6][6], s_L6[6][6];
     __shared__ double colmu[MAX_COL];
     __shared__ float s_zf[8][3], s_cs[8][2];  // rigid-mode correction of up to 8 pieces, FP32
@@ -616,16 +617,35 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 }
             }
         };
-        auto tc_scan = [&](double m0) -> double {
+        auto tc_scan = [&](double m0) -> double {  // every thread calls; the result is thread 0's
+            // A pair whose profile threshold T is >= m0 leaves the running minimum untouched at
+            // any cap <= m0 (accd_profile: accd(m) = m for m <= T), so only the pairs with
+            // T < m0 are replayed — found by warp ballots in candidate order, walked in that
+            // order by thread 0 with the same per-edge reset: the result equals the full serial
+            // replay.
             double m = m0, t_c = m0;
             int prevk = -1;
             const int nc = S.ncand;
-#pragma unroll 4
-            for (int c = 0; c < nc; ++c) {
-                const int k = (int)((unsigned)d.cand[sg.cand0 + c] >> 16);
-                const double2 pr = Ctr[sg.cand0 + c];
-                if (k != prevk) { t_c = m; prevk = k; }
-                m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+            for (int base = 0; base < nc; base += NT) {
+                const int c = base + tid;
+                const bool rel = c < nc && Ctr[sg.cand0 + c].x < m0;
+                const unsigned bal = __ballot_sync(0xffffffffu, rel);
+                if ((tid & 31) == 0) s_wmask[tid >> 5] = bal;
+                __syncthreads();
+                if (tid == 0) {
+                    for (int w = 0; w < NW; ++w) {
+                        unsigned msk = s_wmask[w];
+                        while (msk) {
+                            const int cc = base + w * 32 + (__ffs(msk) - 1);
+                            msk &= msk - 1;
+                            const int k = (int)((unsigned)d.cand[sg.cand0 + cc] >> 16);
+                            const double2 pr = Ctr[sg.cand0 + cc];
+                            if (k != prevk) { t_c = m; prevk = k; }
+                            m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+                        }
+                    }
+                }
+                __syncthreads();
             }
             return m;
         };
@@ -641,8 +661,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             double v[1] = {qi};
             const int ops[1] = {1};
             block_reduce<NT, 1>(v, ops, red);
+            const double a_tc = tc_scan(1.0);
             if (tid == 0) {
-                double a_s = tc_scan(1.0);
+                double a_s = a_tc;
                 if (v[0] > 0.0) a_s = dmin(a_s, 0.45 * d.reach / v[0]);
                 S.alpha_s = a_s;
                 S.q_inf = v[0];
@@ -1318,12 +1339,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 double so[3];
                 float mo[3];
                 block_reduce_mx<NT, 3, 3>(sv, mv, mops, so, mo, fred, dres, mres);
+                const double a_ccd = scene_ipc ? tc_scan(d.alpha_max) : 0.0;
                 // ---------------------------------------------- B5: step length and convergence (FP64)
                 if (tid == 0) {
                     const double ph = so[0], pinf = mo[0], clr = mo[1];
                     double a = mo[2];
                     if (scene_ipc) {
-                        a = dmin(a, tc_scan(d.alpha_max));
+                        a = dmin(a, a_ccd);
                         if (pinf > 0.0) a = dmin(a, 0.45 * d.reach / pinf);
                     }
                     S.pHp = ph; S.p_inf = pinf; S.clr_min = clr;
