@@ -99,6 +99,7 @@ struct SceneSh {
     double alpha, pHp, gTp, beta, p_inf, clr_min, dE0, gn0, q_inf, alpha_s, dispmax;
     double gPg, g_p, g_Py, y_p, y_Py, gn2;
     double motion, csx, csy, mpx, mpy;  // mixed path: motion since the candidate build, centroid shift
+    double dmin_c;                      // smallest candidate-pair distance at the list build (conservative)
     int active, pending, iters, ncand, count, status, rebuild;
 };
 
@@ -215,6 +216,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
         // Node-edge pairs of this scene within reach + skin, rebuilt when a boundary node has
         // moved skin/2 from where the list was built: the pairs closer than `reach` at any
         // later position are then all in the list (each of the three points moves < skin/2).
+        // true while every candidate pair is provably out of reach: its distance at the list
+        // build (dmin_c, conservative) minus twice the largest node move since then; the pair
+        // passes and the ACCD replay would find nothing and are skipped (same result)
+        bool ipc_far = false;
         auto ipc_refresh = [&](bool force) {
             double dm = 0.0;
             for (int j = tid; j < nbl; j += NT) {
@@ -225,7 +230,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             double v[1] = {dm};
             const int ops[1] = {1};
             block_reduce<NT, 1>(v, ops, red);
-            if (!(force || S.rebuild || 2.0 * v[0] >= d.skin)) return;
+            if (!(force || S.rebuild || 2.0 * v[0] >= d.skin)) {
+                ipc_far = S.dmin_c - 2.0 * v[0] >= d.reach;
+                return;
+            }
             // rebuild
             double2 anchor = X[d.bnd[sg.bnd0]];
             for (int j = tid; j < nbl; j += NT) {
@@ -238,6 +246,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             const float rad = (float)(d.reach + d.skin);
             const float slack = 1.0e-5f * rad;
             const long npair = (long)sg.ne * nbl;
+            float dmn = 3.0e38f;
             // ordered stream compaction: the list comes out sorted by (edge, boundary slot),
             // the order in which the reference visits the pairs
             for (long base = 0; base < npair; base += NT) {
@@ -259,8 +268,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                         float t = (wx * abx + wy * aby) / fmaxf(abx * abx + aby * aby, 1e-30f);
                         t = fminf(fmaxf(t, 0.f), 1.f);
                         const float dx = wx - t * abx, dy = wy - t * aby;
-                        keep = sqrtf(dx * dx + dy * dy) <= rad + slack &&
+                        const float dd = sqrtf(dx * dx + dy * dy);
+                        keep = dd <= rad + slack &&
                                !excluded(d, sg.bnd0 + j, d.ela[ge]) && !excluded(d, sg.bnd0 + j, d.elb[ge]);
+                        if (keep) dmn = fminf(dmn, dd);
                     }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, keep);
@@ -277,12 +288,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 if (tid == 0) S.count += tot;         // read after the next chunk's first barrier
             }
             __syncthreads();
+            double vm[1] = {(double)dmn};
+            const int opm[1] = {2};
+            block_reduce<NT, 1>(vm, opm, red);
             if (tid == 0) {
                 if (S.count > sg.ncap) { S.status = D2F_ECAP; S.ncand = sg.ncap; }
                 else S.ncand = S.count;
                 S.rebuild = 0;
+                S.dmin_c = vm[0] - 1.0e-4 * (double)rad;  // FP32 rounding of the build distances
             }
             __syncthreads();
+            ipc_far = S.dmin_c >= d.reach;
         };
 
         // IPC pair evaluation (ipc_pair_kernel + _pair, ipc_contact.py:130-296), FP64.
@@ -295,6 +311,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             return make_double2(t.x - x.x, t.y - x.y);
         };
         auto ipc_pairs = [&](int mode, double &acc_pHp, double t_c) {
+            if (ipc_far) return;  // every pair out of reach: no term, no cap
             const double idhat = d.ipc_dhat, ikappa = d.ipc_kappa, reach = d.reach, gap = d.gap;
             const double dlo = 1.0e-9 * idhat, onset = 0.02 * idhat;
             const double mu_s = d.friction ? d.ipc_mu : 0.0;
@@ -437,6 +454,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
         // edges before it left it, and its pairs lower it (ipc_contact.py:211, 241). Replayed
         // by one thread over the ordered candidate list from the per-pair profiles.
         auto tc_scan = [&](double m0) -> double {  // every thread calls; the result is thread 0's
+            if (ipc_far) return m0;  // no pair in reach: every profile is (inf, inf)
             // A pair whose profile threshold T is >= m0 leaves the running minimum untouched at
             // any cap <= m0 (accd_profile: accd(m) = m for m <= T), so only the pairs with
             // T < m0 are replayed — found by warp ballots in candidate order, walked in that

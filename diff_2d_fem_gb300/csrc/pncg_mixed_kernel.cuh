@@ -408,11 +408,18 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         // ---------------------------------------------------------------- contact candidates
         // As in the FP64 kernel, but the list is rebuilt at every step start (x_n changed) and
         // its validity inside a step is the FP32 motion dx - dx_ref of the boundary nodes.
+        // true while every candidate pair is provably out of reach: its distance at the list
+        // build (dmin_c, conservative) minus twice the largest node move since then; the pair
+        // passes and the ACCD replay would find nothing and are skipped (same result)
+        bool ipc_far = false;
         auto ipc_refresh = [&]() {
             // rebuild when the nodes may have moved skin/2 since the last build: every node
             // moves at most alpha |p|_inf per iteration (alpha_s q_inf per sweep), summed in
             // S.motion — a bound, so no reduction over the nodes is needed
-            if (!(S.rebuild || 2.0 * S.motion >= d.skin)) return;
+            if (!(S.rebuild || 2.0 * S.motion >= d.skin)) {
+                ipc_far = S.dmin_c - 2.0 * S.motion >= d.reach;
+                return;
+            }
             __syncthreads();
             const double2 anchor = xpos(d.bnd[sg.bnd0]);
             for (int j = tid; j < nbl; j += NT) {
@@ -426,6 +433,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             const float rad = (float)(d.reach + d.skin);
             const float slack = 1.0e-5f * rad;
             const long npair = (long)sg.ne * nbl;
+            float dmn = 3.0e38f;
             for (long base = 0; base < npair; base += NT) {
                 const long q = base + tid;
                 bool keep = false;
@@ -444,8 +452,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         float t = (wx * abx + wy * aby) / fmaxf(abx * abx + aby * aby, 1e-30f);
                         t = fminf(fmaxf(t, 0.f), 1.f);
                         const float dx = wx - t * abx, dy = wy - t * aby;
-                        keep = sqrtf(dx * dx + dy * dy) <= rad + slack &&
+                        const float dd = sqrtf(dx * dx + dy * dy);
+                        keep = dd <= rad + slack &&
                                !excluded(d, sg.bnd0 + j, d.ela[ge]) && !excluded(d, sg.bnd0 + j, d.elb[ge]);
+                        if (keep) dmn = fminf(dmn, dd);
                     }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, keep);
@@ -462,13 +472,18 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 if (tid == 0) S.count += tot;
             }
             __syncthreads();
+            double vm[1] = {(double)dmn};
+            const int opm[1] = {2};
+            block_reduce<NT, 1>(vm, opm, red);
             if (tid == 0) {
                 if (S.count > sg.ncap) { S.status = D2F_ECAP; S.ncand = sg.ncap; }
                 else S.ncand = S.count;
                 S.rebuild = 0;
                 S.motion = 0.0;
+                S.dmin_c = vm[0] - 1.0e-4 * (double)rad;  // FP32 rounding of the build distances
             }
             __syncthreads();
+            ipc_far = S.dmin_c >= d.reach;
         };
 
         auto kin_dir = [&](int n) -> double2 {
@@ -479,6 +494,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         };
         // IPC pairs (ipc_pair_kernel + _pair, ipc_contact.py:130-296) in FP64 at x_n + dx
         auto ipc_pairs = [&](int mode, double &acc_pHp, double t_c) {
+            if (ipc_far) return;  // every pair out of reach: no term, no cap
             const double idhat = d.ipc_dhat, ikappa = d.ipc_kappa, reach = d.reach, gap = d.gap;
             const double dlo = 1.0e-9 * idhat, onset = 0.02 * idhat;
             const double mu_s = d.friction ? d.ipc_mu : 0.0;
@@ -618,6 +634,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             }
         };
         auto tc_scan = [&](double m0) -> double {  // every thread calls; the result is thread 0's
+            if (ipc_far) return m0;  // no pair in reach: every profile is (inf, inf)
             // A pair whose profile threshold T is >= m0 leaves the running minimum untouched at
             // any cap <= m0 (accd_profile: accd(m) = m for m <= T), so only the pairs with
             // T < m0 are replayed — found by warp ballots in candidate order, walked in that
