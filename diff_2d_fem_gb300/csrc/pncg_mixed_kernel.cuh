@@ -194,12 +194,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     const float *__restrict__ Mu = reinterpret_cast<const float *>(d.mu);
     const float *__restrict__ La = reinterpret_cast<const float *>(d.lam);
     float4 *__restrict__ Esc = reinterpret_cast<float4 *>(d.escr);
-    float *__restrict__ Ec = reinterpret_cast<float *>(d.ecache);
     const double2 *__restrict__ Fx = reinterpret_cast<const double2 *>(d.fext);
     const double2 *__restrict__ Tgt = reinterpret_cast<const double2 *>(d.bc_target);
     double2 *__restrict__ Ctr = reinterpret_cast<double2 *>(d.cand_tr);
     const double2 *__restrict__ Xr = reinterpret_cast<const double2 *>(d.xrest);
-    const float4 *__restrict__ Dmr = reinterpret_cast<const float4 *>(d.Dm);
     const MixedLayout ML = mixed_layout(d.N, d.T, d.Nb, d.n_col, d.n_rig);
     unsigned char *ms = static_cast<unsigned char *>(d.mscr);
     float2 *__restrict__ XD = reinterpret_cast<float2 *>(ms + ML.xd);     // x - x_n
@@ -722,7 +720,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             // ---------------------------------------------- A1: triangles (gradient + diagonal)
             for (int t = t0 + tid; t < t1; t += NT) {
                 const int i0 = __ldg(d.tri + 3 * t), i1 = __ldg(d.tri + 3 * t + 1), i2 = __ldg(d.tri + 3 * t + 2);
-                const float4 B = Bm[t], du = DU0[t], Dm = Dmr[t];
+                const float4 B = Bm[t], du = DU0[t];
                 const float A = Ar[t], mu = Mu[t], la = La[t];
                 const float2 u0 = XR[i0], u1 = XR[i1], u2 = XR[i2];
                 const float q1x = u1.x - u0.x, q1y = u1.y - u0.y;  // edges of x - x_b
@@ -777,9 +775,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 Esc[3 * t] = make_float4(-(g1x + g2x), -(g1y + g2y), d0x, d0y);
                 Esc[3 * t + 1] = make_float4(g1x, g1y, d1x_, d1y_);
                 Esc[3 * t + 2] = make_float4(g2x, g2y, d2x_, d2y_);
-                float *ec = Ec + 9 * (size_t)t;
-                ec[0] = G00; ec[1] = G01; ec[2] = G10; ec[3] = G11; ec[4] = c1;
-                ec[5] = Dm.x + d1x; ec[6] = Dm.y + d1y; ec[7] = Dm.z + d2x; ec[8] = Dm.w + d2y;
             }
             __syncthreads();
 
@@ -1283,13 +1278,26 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const float shrink = (float)d.area_shrink;
                 for (int t = t0 + tid; t < t1; t += NT) {
                     const int i0 = __ldg(d.tri + 3 * t), i1 = __ldg(d.tri + 3 * t + 1), i2 = __ldg(d.tri + 3 * t + 2);
-                    const float *ec = Ec + 9 * (size_t)t;
-                    const float G00 = ec[0], G01 = ec[1], G10 = ec[2], G11 = ec[3], c1 = ec[4];
-                    const float e1x = ec[5], e1y = ec[6], e2x = ec[7], e2y = ec[8];
                     const float2 p0 = P[i0], p1 = P[i1], p2 = P[i2];
-                    const float q1x = p1.x - p0.x, q1y = p1.y - p0.y, q2x = p2.x - p0.x, q2y = p2.y - p0.y;
-                    const float4 B = Bm[t];
+                    const float2 u0 = XR[i0], u1 = XR[i1], u2 = XR[i2];
+                    const float4 B = Bm[t], du = DU0[t];
                     const float A = Ar[t], mu = Mu[t], la = La[t];
+                    // F^-T and la log J - mu at x, formed again here rather than cached by the
+                    // gradient pass (36 bytes a triangle less to write and read each iteration)
+                    const float d1x = du.x + (u1.x - u0.x), d1y = du.y + (u1.y - u0.y);
+                    const float d2x = du.z + (u2.x - u0.x), d2y = du.w + (u2.y - u0.y);
+                    const float H00 = d1x * B.x + d2x * B.z, H01 = d1x * B.y + d2x * B.w;
+                    const float H10 = d1y * B.x + d2y * B.z, H11 = d1y * B.y + d2y * B.w;
+                    const float dH = H00 * H11 - H01 * H10, Jm1 = (H00 + H11) + dH, J = 1.f + Jm1;
+                    const float logJ = J > 1.0e-6f ? log1pf(Jm1) : logf(1.0e-6f);
+                    const float iJ = J != 0.f ? 1.f / J : 0.f;
+                    const float G00 = (1.f + H11) * iJ, G01 = -H10 * iJ, G10 = -H01 * iJ, G11 = (1.f + H00) * iJ;
+                    const float c1 = la * logJ - mu;
+                    // current edge vectors: rest edges (the columns of B^-1) + displacement edges
+                    const float idet = 1.f / (B.x * B.w - B.y * B.z);
+                    const float e1x = B.w * idet + d1x, e1y = -B.z * idet + d1y;
+                    const float e2x = -B.y * idet + d2x, e2y = B.x * idet + d2y;
+                    const float q1x = p1.x - p0.x, q1y = p1.y - p0.y, q2x = p2.x - p0.x, q2y = p2.y - p0.y;
                     const float f00 = q1x * B.x + q2x * B.z, f01 = q1x * B.y + q2x * B.w;
                     const float f10 = q1y * B.x + q2y * B.z, f11 = q1y * B.y + q2y * B.w;
                     const float dd = f00 * f00 + f01 * f01 + f10 * f10 + f11 * f11;
