@@ -53,9 +53,9 @@ __device__ __forceinline__ FF ff_merge(FF a, FF b) {
     return FF{hi, lo - (hi - s)};
 }
 
-// Block reduction: NS compensated sums (returned as FP64) and NM FP32 extrema
-// (ops 1 = max, 2 = min). Deterministic. `fred` holds NW*(2*NS+NM) floats, `dres` NS doubles,
-// `mres` NM floats.
+// Block reduction: NS compensated sums (returned as FP64) and NM FP32 reductions
+// (ops 0 = plain sum, 1 = max, 2 = min). Deterministic. `fred` holds NW*(2*NS+NM) floats,
+// `dres` NS doubles, `mres` NM floats.
 template <int NT, int NS, int NM>
 __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], const int (&mops)[NM],
                                                 double (&out_s)[NS], float (&out_m)[NM], float *fred,
@@ -72,7 +72,7 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
 #pragma unroll
         for (int k = 0; k < NM; ++k) {
             const float b = __shfl_down_sync(0xffffffffu, m[k], o);
-            m[k] = mops[k] == 1 ? fmaxf(m[k], b) : fminf(m[k], b);
+            m[k] = mops[k] == 1 ? fmaxf(m[k], b) : mops[k] == 2 ? fminf(m[k], b) : m[k] + b;
         }
     }
     if (lane == 0) {
@@ -95,7 +95,7 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
             float a = fred[2 * NS + j];
             for (int q = 1; q < NW; ++q) {
                 const float b = fred[q * (2 * NS + NM) + 2 * NS + j];
-                a = mops[j] == 1 ? fmaxf(a, b) : fminf(a, b);
+                a = mops[j] == 1 ? fmaxf(a, b) : mops[j] == 2 ? fminf(a, b) : a + b;
             }
             mres[j] = a;
         }
@@ -110,7 +110,7 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
 
 // Byte layout of the mixed path's per-step scratch (d2f_scene_desc.mscr), 256-aligned parts.
 struct MixedLayout {
-    size_t xd, xhv, g0, xbd, xr, db, rarm, m32, du0, phi0, rcs, dref, total;
+    size_t xd, xhv, g0, gd, xbd, xr, db, rarm, m32, du0, phi0, rcs, dref, total;
 };
 __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, long n_col, long n_rig) {
     auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -119,6 +119,7 @@ __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, lon
     L.xd = o; o = up(o + (size_t)N * 8);
     L.xhv = o; o = up(o + (size_t)N * 8);
     L.g0 = o; o = up(o + (size_t)N * 16);
+    L.gd = o; o = up(o + (size_t)N * 16);
     L.xbd = o; o = up(o + (size_t)N * 16);
     L.xr = o; o = up(o + (size_t)N * 8);
     L.db = o; o = up(o + (size_t)N * 8);
@@ -193,7 +194,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     const float *__restrict__ Ar = reinterpret_cast<const float *>(d.area);
     const float *__restrict__ Mu = reinterpret_cast<const float *>(d.mu);
     const float *__restrict__ La = reinterpret_cast<const float *>(d.lam);
-    float4 *__restrict__ Esc = reinterpret_cast<float4 *>(d.escr);
     const double2 *__restrict__ Fx = reinterpret_cast<const double2 *>(d.fext);
     const double2 *__restrict__ Tgt = reinterpret_cast<const double2 *>(d.bc_target);
     double2 *__restrict__ Ctr = reinterpret_cast<double2 *>(d.cand_tr);
@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     float2 *__restrict__ XHV = reinterpret_cast<float2 *>(ms + ML.xhv);   // x_hat - x_n
     float4 *__restrict__ G0 = reinterpret_cast<float4 *>(ms + ML.g0);     // step-start gradient, FP32 pair
     double2 *__restrict__ G0d = reinterpret_cast<double2 *>(ms + ML.g0);  // the same, FP64 while it is built
-    double2 *__restrict__ Esc64 = reinterpret_cast<double2 *>(d.escr);    // per-corner FP64 forces (setup only)
+    double2 *__restrict__ Esc64 = reinterpret_cast<double2 *>(d.escr);    // per-corner FP64 forces (base builds)
+    float4 *__restrict__ GD = reinterpret_cast<float4 *>(ms + ML.gd);     // per node: elastic gradient + diagonal sums
     float2 *__restrict__ RARM = reinterpret_cast<float2 *>(ms + ML.rarm); // x_n - c_n (rigid pieces)
     float *__restrict__ M32 = reinterpret_cast<float *>(ms + ML.m32);
     float4 *__restrict__ DU0 = reinterpret_cast<float4 *>(ms + ML.du0);   // displacement edges at the base x_b
@@ -351,6 +352,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             XD[i] = make_float2(0.f, 0.f);
             XBd[i] = xi;
             XR[i] = make_float2(0.f, 0.f);
+            GD[i] = make_float4(0.f, 0.f, 0.f, 0.f);
             XHV[i] = make_float2((float)(dt * d.drag * vi.x), (float)(dt * d.drag * vi.y));
             M32[i] = (float)d.mass[i];
             G[i] = make_float2(0.f, 0.f);
@@ -772,9 +774,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 dg(b0x, b0y, d0x, d0y);
                 dg(B.x, B.y, d1x_, d1y_);
                 dg(B.z, B.w, d2x_, d2y_);
-                Esc[3 * t] = make_float4(-(g1x + g2x), -(g1y + g2y), d0x, d0y);
-                Esc[3 * t + 1] = make_float4(g1x, g1y, d1x_, d1y_);
-                Esc[3 * t + 2] = make_float4(g2x, g2y, d2x_, d2y_);
+                // accumulate at the nodes (vector atomics; the order of the FP32 sums is not fixed)
+                atomicAdd(GD + i0, make_float4(-(g1x + g2x), -(g1y + g2y), d0x, d0y));
+                atomicAdd(GD + i1, make_float4(g1x, g1y, d1x_, d1y_));
+                atomicAdd(GD + i2, make_float4(g2x, g2y, d2x_, d2y_));
             }
             __syncthreads();
 
@@ -788,21 +791,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 float gy = (fm & 2) ? m * (dx_.y - hv.y) : 0.f;
                 float dxx = m, dyy = m;
                 {
-                    const int4 ca = __ldg(reinterpret_cast<const int4 *>(d.inc8) + 2 * i);
-                    const int4 cb = __ldg(reinterpret_cast<const int4 *>(d.inc8) + 2 * i + 1);
-                    const int cs[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
-                    float4 cv[8];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        if (cs[q] >= 0) cv[q] = Esc[cs[q]];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        if (cs[q] >= 0) { gx += cv[q].x; gy += cv[q].y; dxx += cv[q].z; dyy += cv[q].w; }
-                    const int k0 = __ldg(d.inc_ptr + i) + 8, k1 = __ldg(d.inc_ptr + i + 1);
-                    for (int k = k0; k < k1; ++k) {
-                        const float4 c = Esc[__ldg(d.inc + k)];
-                        gx += c.x; gy += c.y; dxx += c.z; dyy += c.w;
-                    }
+                    const float4 c = GD[i];  // the elastic sums of this iteration; reset for the next
+                    GD[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    gx += c.x; gy += c.y; dxx += c.z; dyy += c.w;
                 }
                 if (scene_rig) Del[i] = make_float2(dxx, dyy);
                 const int bs = d.node_bslot[i];
@@ -1073,11 +1064,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 __syncthreads();
             };
             auto b1 = [&](auto rig_tag) {
+                // the five Dai-Kou dots and |g|^2 as compensated sums; the rigid piece's
+                // projections (they shape the preconditioner only) as plain FP32 sums
                 constexpr bool RIG = decltype(rig_tag)::value;
-                constexpr int NS = RIG ? 17 : 6;
+                constexpr int NS = 6, NM = RIG ? 12 : 1;
                 FF v[NS];
 #pragma unroll
                 for (int q = 0; q < NS; ++q) v[q] = FF{0.f, 0.f};
+                float r[NM];
+                int rops[NM];
+#pragma unroll
+                for (int q = 0; q < NM; ++q) { r[q] = 0.f; rops[q] = q == 0 ? 1 : 0; }
                 const float csx = (float)S.csx, csy = (float)S.csy;
                 for (int i = n0 + tid; i < n1; i += NT) {
                     const uint8_t fm = d.free_mask[i];
@@ -1089,10 +1086,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                             const float rx = a0.x + (u.x - csx), ry = a0.y + (u.y - csy);
                             const float m = M32[i];
                             const float dx = fmaxf(dg.x - de.x, 0.f) + m, dy = fmaxf(dg.y - de.y, 0.f) + m;
-                            ff_add(v[6], g.x); ff_add(v[7], g.y); ff_add(v[8], rx * g.y - ry * g.x);
-                            ff_add(v[9], gp.x); ff_add(v[10], gp.y); ff_add(v[11], rx * gp.y - ry * gp.x);
-                            ff_add(v[12], dx); ff_add(v[13], -dx * ry); ff_add(v[14], dy); ff_add(v[15], dy * rx);
-                            ff_add(v[16], dx * ry * ry + dy * rx * rx);
+                            r[1] += g.x; r[2] += g.y; r[3] += rx * g.y - ry * g.x;
+                            r[4] += gp.x; r[5] += gp.y; r[6] += rx * gp.y - ry * gp.x;
+                            r[7] += dx; r[8] += -dx * ry; r[9] += dy; r[10] += dy * rx;
+                            r[11] += dx * ry * ry + dy * rx * rx;
                         }
                     }
                     if (!(fm & 1)) g.x = 0.f;
@@ -1109,15 +1106,15 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     ff_add(v[4], yx * Py0 + yy * Py1);
                     ff_add(v[5], g.x * g.x + g.y * g.y);
                 }
-                float nm[1] = {0.f};
-                const int nmo[1] = {1};
                 double vs[NS];
-                float mo_[1];
-                block_reduce_mx<NT, NS, 1>(v, nm, nmo, vs, mo_, fred, dres, mres);
+                float mo_[NM];
+                block_reduce_mx<NT, NS, NM>(v, r, rops, vs, mo_, fred, dres, mres);
                 if constexpr (RIG) {
                     if (tid == 0) {  // rigid_reduce_kernel, affine.py:456-473 (FP64)
                         const int b = sg.rig0;
-                        const double a[9] = {vs[12], 0.0, vs[13], 0.0, vs[14], vs[15], vs[13], vs[15], vs[16]};
+                        double rv[17];
+                        for (int q = 6; q < 17; ++q) rv[q] = (double)mo_[q - 5];
+                        const double a[9] = {rv[12], 0.0, rv[13], 0.0, rv[14], rv[15], rv[13], rv[15], rv[16]};
                         const double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[6] * a[5]) +
                                            a[2] * (a[3] * a[7] - a[6] * a[4]);
                         double Hi[9] = {0};
@@ -1129,7 +1126,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                             Hi[6] = (a[3] * a[7] - a[4] * a[6]) * r; Hi[7] = (a[1] * a[6] - a[0] * a[7]) * r;
                             Hi[8] = (a[0] * a[4] - a[1] * a[3]) * r;
                         }
-                        const double g[3] = {vs[6], vs[7], vs[8]}, y[3] = {vs[6] - vs[9], vs[7] - vs[10], vs[8] - vs[11]};
+                        const double g[3] = {rv[6], rv[7], rv[8]}, y[3] = {rv[6] - rv[9], rv[7] - rv[10], rv[8] - rv[11]};
                         double z[3], zy[3];
                         for (int r = 0; r < 3; ++r) {
                             z[r] = Hi[3 * r] * g[0] + Hi[3 * r + 1] * g[1] + Hi[3 * r + 2] * g[2];
