@@ -110,23 +110,23 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
 
 // Byte layout of the mixed path's per-step scratch (d2f_scene_desc.mscr), 256-aligned parts.
 struct MixedLayout {
-    size_t xd, xhv, g0, gd, xbd, xr, db, rarm, m32, du0, phi0, rcs, dref, total;
+    size_t xd, hvm, g0, gd, xbd, xr, db, rarm, ninfo, du0, phi0, rcs, dref, total;
 };
 __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, long n_col, long n_rig) {
     auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
     MixedLayout L;
     size_t o = 0;
     L.xd = o; o = up(o + (size_t)N * 8);
-    L.xhv = o; o = up(o + (size_t)N * 8);
+    L.hvm = o; o = up(o + (size_t)N * 16);
     L.g0 = o; o = up(o + (size_t)N * 16);
     L.gd = o; o = up(o + (size_t)N * 16);
     L.xbd = o; o = up(o + (size_t)N * 16);
     L.xr = o; o = up(o + (size_t)N * 8);
     L.db = o; o = up(o + (size_t)N * 8);
     L.rarm = o; o = up(o + (size_t)N * 8);
-    L.m32 = o; o = up(o + (size_t)N * 4);
+    L.ninfo = o; o = up(o + (size_t)N * 8);
     L.du0 = o; o = up(o + (size_t)T * 16);
-    L.phi0 = o; o = up(o + (size_t)Nb * (n_col > 0 ? n_col : 1) * 4);
+    L.phi0 = o; o = up(o + (size_t)N * (n_col > 0 ? n_col : 1) * 4);
     L.rcs = o; o = up(o + (size_t)(n_rig > 0 ? n_rig : 1) * 8);
     L.dref = o; o = up(o + (size_t)(Nb > 0 ? Nb : 1) * 8);
     L.total = o;
@@ -154,6 +154,8 @@ __device__ __forceinline__ double2 tendon_dlen(PosF pos, const int32_t *t_node, 
 
 // iterations between rebuilds of the FP64 gradient base
 constexpr int REBASE = 32;
+// packed per-node flags (NINFO.x): bits 0-1 free mask, then these, bits 4-7 the rigid piece
+constexpr int NI_AFF = 4, NI_RIG = 8;
 
 // ---------------------------------------------------------------------- the kernel
 template <int NT, int MINB>
@@ -201,18 +203,18 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     const MixedLayout ML = mixed_layout(d.N, d.T, d.Nb, d.n_col, d.n_rig);
     unsigned char *ms = static_cast<unsigned char *>(d.mscr);
     float2 *__restrict__ XD = reinterpret_cast<float2 *>(ms + ML.xd);     // x - x_n
-    float2 *__restrict__ XHV = reinterpret_cast<float2 *>(ms + ML.xhv);   // x_hat - x_n
+    float4 *__restrict__ HVM = reinterpret_cast<float4 *>(ms + ML.hvm);   // x_hat - x_n, mass
     float4 *__restrict__ G0 = reinterpret_cast<float4 *>(ms + ML.g0);     // step-start gradient, FP32 pair
     double2 *__restrict__ G0d = reinterpret_cast<double2 *>(ms + ML.g0);  // the same, FP64 while it is built
     double2 *__restrict__ Esc64 = reinterpret_cast<double2 *>(d.escr);    // per-corner FP64 forces (base builds)
     float4 *__restrict__ GD = reinterpret_cast<float4 *>(ms + ML.gd);     // per node: elastic gradient + diagonal sums
     float2 *__restrict__ RARM = reinterpret_cast<float2 *>(ms + ML.rarm); // x_n - c_n (rigid pieces)
-    float *__restrict__ M32 = reinterpret_cast<float *>(ms + ML.m32);
+    int2 *__restrict__ NINFO = reinterpret_cast<int2 *>(ms + ML.ninfo);  // node flags, boundary slot
     float4 *__restrict__ DU0 = reinterpret_cast<float4 *>(ms + ML.du0);   // displacement edges at the base x_b
     double2 *__restrict__ XBd = reinterpret_cast<double2 *>(ms + ML.xbd); // base positions x_b (FP64)
     float2 *__restrict__ XR = reinterpret_cast<float2 *>(ms + ML.xr);     // x - x_b
     float2 *__restrict__ DB = reinterpret_cast<float2 *>(ms + ML.db);     // x_b - x_n
-    float *__restrict__ PHI0 = reinterpret_cast<float *>(ms + ML.phi0);   // half-space distances at x_n
+    float *__restrict__ PHI0 = reinterpret_cast<float *>(ms + ML.phi0);   // half-space distances at x_n, per node
     float2 *__restrict__ DREF = reinterpret_cast<float2 *>(ms + ML.dref); // dx when the candidate list was built
     float2 *__restrict__ RCS = reinterpret_cast<float2 *>(ms + ML.rcs);   // rigid pieces: centroid shift
 
@@ -353,8 +355,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             XBd[i] = xi;
             XR[i] = make_float2(0.f, 0.f);
             GD[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-            XHV[i] = make_float2((float)(dt * d.drag * vi.x), (float)(dt * d.drag * vi.y));
-            M32[i] = (float)d.mass[i];
+            HVM[i] = make_float4((float)(dt * d.drag * vi.x), (float)(dt * d.drag * vi.y), (float)d.mass[i], 0.f);
+            {  // packed static node info: bits 0-1 free mask, 2 affine, 3 rigid, 4-7 rigid piece (15: look up)
+                int f = d.free_mask[i];
+                if (d.node_aff[i] >= 0) f |= NI_AFF;
+                const int kr = d.node_rig[i];
+                if (kr >= 0) {
+                    const int lb = d.r_grp[kr] - sg.rig0;
+                    f |= NI_RIG | ((lb < 15 ? lb : 15) << 4);
+                }
+                NINFO[i] = make_int2(f, d.node_bslot[i]);
+            }
             G[i] = make_float2(0.f, 0.f);
             P[i] = make_float2(0.f, 0.f);
         }
@@ -369,7 +380,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             const double2 xb = Xn[d.bnd[sg.bnd0 + j]];
             for (int k = 0; k < n_col; ++k) {
                 const Col c = cols[k];
-                if (c.kind == 4) PHI0[(size_t)(sg.bnd0 + j) * n_col + k] = (float)(c.rx * (xb.x - c.cx) + c.ry * (xb.y - c.cy));
+                if (c.kind == 4) PHI0[(size_t)d.bnd[sg.bnd0 + j] * n_col + k] = (float)(c.rx * (xb.x - c.cx) + c.ry * (xb.y - c.cy));
             }
         }
         if (!scene_ipc) {  // apply_bc_kernel, kernels.py:53-59: x = target
@@ -784,9 +795,12 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             // ---------------------------------------------- A2: nodes (gather, colliders, friction, force)
             for (int i = n0 + tid; i < n1; i += NT) {
                 Gp[i] = G[i];
-                const float2 dx_ = XD[i], hv = XHV[i];
-                const float m = M32[i];
-                const uint8_t fm = d.free_mask[i];
+                const float2 dx_ = XD[i];
+                const float4 hvm = HVM[i];
+                const int2 inf = NINFO[i];
+                const float2 hv = make_float2(hvm.x, hvm.y);
+                const float m = hvm.z;
+                const int fm = inf.x & 3;
                 float gx = (fm & 1) ? m * (dx_.x - hv.x) : 0.f;
                 float gy = (fm & 2) ? m * (dx_.y - hv.y) : 0.f;
                 float dxx = m, dyy = m;
@@ -796,14 +810,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     gx += c.x; gy += c.y; dxx += c.z; dyy += c.w;
                 }
                 if (scene_rig) Del[i] = make_float2(dxx, dyy);
-                const int bs = d.node_bslot[i];
-                if (bs >= 0) {
+                if (inf.y >= 0) {
                     for (int k = 0; k < n_col; ++k) {
                         const Col c = cols[k];
                         float dd, nx, ny, tang = 0.f, H00 = 0.f, H11 = 0.f, gn = 1.f;
                         if (c.kind == 4) {  // half-space: phi0 (FP64 per step) + n.dx
                             nx = colf[k][0]; ny = colf[k][1];
-                            dd = PHI0[(size_t)bs * n_col + k] + (nx * dx_.x + ny * dx_.y);
+                            dd = PHI0[(size_t)i * n_col + k] + (nx * dx_.x + ny * dx_.y);
                         } else {           // curved colliders in FP64
                             const double2 xi = xpos(i);
                             double ddd, nnx, nny, dc = 1.0;
@@ -962,7 +975,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
                     if (d.r_grp[k] != b) continue;
                     const int i = d.r_node[k];
-                    const float m = M32[i];
+                    const float m = HVM[i].z;
                     const float2 u = XD[i];
                     ff_add(cs2[0], m * u.x);
                     ff_add(cs2[1], m * u.y);
@@ -983,7 +996,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     const float2 a0 = RARM[i], u = XD[i];
                     const float rx = a0.x + (u.x - csx), ry = a0.y + (u.y - csy);
                     const float2 g = G[i], gp = Gp[i], dg = D[i], de = Del[i];
-                    const float m = M32[i];
+                    const float m = HVM[i].z;
                     const float dx = fmaxf(dg.x - de.x, 0.f) + m, dy = fmaxf(dg.y - de.y, 0.f) + m;
                     ff_add(v[0], g.x); ff_add(v[1], g.y); ff_add(v[2], rx * g.y - ry * g.x);
                     ff_add(v[3], gp.x); ff_add(v[4], gp.y); ff_add(v[5], rx * gp.y - ry * gp.x);
@@ -1077,14 +1090,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 for (int q = 0; q < NM; ++q) { r[q] = 0.f; rops[q] = q == 0 ? 1 : 0; }
                 const float csx = (float)S.csx, csy = (float)S.csy;
                 for (int i = n0 + tid; i < n1; i += NT) {
-                    const uint8_t fm = d.free_mask[i];
+                    const int inf = NINFO[i].x, fm = inf & 3;
                     float2 g = G[i];
                     const float2 dg = D[i], gp = Gp[i], pp = P[i];
                     if constexpr (RIG) {
-                        if (d.node_rig[i] >= 0) {  // a free node: the mask does not change g
+                        if (inf & NI_RIG) {  // a free node: the mask does not change g
                             const float2 a0 = RARM[i], u = XD[i], de = Del[i];
                             const float rx = a0.x + (u.x - csx), ry = a0.y + (u.y - csy);
-                            const float m = M32[i];
+                            const float m = HVM[i].z;
                             const float dx = fmaxf(dg.x - de.x, 0.f) + m, dy = fmaxf(dg.y - de.y, 0.f) + m;
                             r[1] += g.x; r[2] += g.y; r[3] += rx * g.y - ry * g.x;
                             r[4] += gp.x; r[5] += gp.y; r[6] += rx * gp.y - ry * gp.x;
@@ -1151,11 +1164,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             {
                 const float bta = (float)S.beta;
                 for (int i = n0 + tid; i < n1; i += NT) {
-                    const uint8_t fm = d.free_mask[i];
+                    const int2 inf = NINFO[i];
+                    const int fm = inf.x & 3;
                     const float2 dx_ = XD[i];
+                    const float mi = HVM[i].z;
                     float px, py;
-                    const int ka = d.node_aff[i];
-                    if (ka >= 0) {
+                    if (inf.x & NI_AFF) {
+                        const int ka = d.node_aff[i];
                         const double *w = d.a_w + 3 * ka, *pq = d.a_pq + 6 * d.a_grp[ka];
                         px = (float)(w[0] * pq[0] + w[1] * pq[1] + w[2] * pq[2]);
                         py = (float)(w[0] * pq[3] + w[1] * pq[4] + w[2] * pq[5]);
@@ -1163,9 +1178,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         const float2 g = G[i], dg = D[i], po = P[i];
                         px = (fm & 1) ? -g.x / fmaxf(dg.x, 1.0e-12f) + bta * po.x : 0.f;
                         py = (fm & 2) ? -g.y / fmaxf(dg.y, 1.0e-12f) + bta * po.y : 0.f;
-                        const int kr = d.node_rig[i];
-                        if (kr >= 0) {
-                            const int lb = d.r_grp[kr] - sg.rig0;
+                        if (inf.x & NI_RIG) {
+                            int lb = (inf.x >> 4) & 15;
+                            if (lb == 15) lb = d.r_grp[d.node_rig[i]] - sg.rig0;
                             float z0, z1, z2, csx, csy;
                             if (lb < 8) {
                                 z0 = s_zf[lb][0]; z1 = s_zf[lb][1]; z2 = s_zf[lb][2]; csx = s_cs[lb][0]; csy = s_cs[lb][1];
@@ -1181,17 +1196,15 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         }
                     }
                     P[i] = make_float2(px, py);
-                    const float mi = M32[i];
                     ff_add(acc_pHp, mi * (px * px + py * py));
-                    if (rig1 && d.node_rig[i] >= 0) { ff_add(acc_mpx, mi * px); ff_add(acc_mpy, mi * py); }
+                    if (rig1 && (inf.x & NI_RIG)) { ff_add(acc_mpx, mi * px); ff_add(acc_mpy, mi * py); }
                     acc_pinf = fmaxf(acc_pinf, sqrtf(px * px + py * py));
-                    const int bs = d.node_bslot[i];
-                    if (bs >= 0) {
+                    if (inf.y >= 0) {
                         for (int k = 0; k < n_col; ++k) {
                             const Col c = cols[k];
                             if (c.kind == 4) {  // half-space: clearance, CCD, barrier and friction curvature
                                 const float nx = colf[k][0], ny = colf[k][1];
-                                const float dd = PHI0[(size_t)bs * n_col + k] + (nx * dx_.x + ny * dx_.y);
+                                const float dd = PHI0[(size_t)i * n_col + k] + (nx * dx_.x + ny * dx_.y);
                                 const float gp = nx * px + ny * py;
                                 if (!(gp >= 0.f || dd <= 0.f)) acc_alpha = fminf(acc_alpha, feta * dd / (-gp));
                                 acc_clr = fminf(acc_clr, dd);
@@ -1414,8 +1427,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const bool act = S.active != 0;
                 const float al = (float)S.alpha;
                 for (int i = n0 + tid; i < n1; i += NT) {
-                    const int ka = d.node_aff[i];
-                    if (ka >= 0) {
+                    if (NINFO[i].x & NI_AFF) {
+                        const int ka = d.node_aff[i];
                         const double *w = d.a_w + 3 * ka, *q = d.a_q + 6 * d.a_grp[ka];
                         const double2 xn = Xn[i], xb = XBd[i];
                         const double jx = w[0] * q[0] + w[1] * q[1] + w[2] * q[2];
