@@ -7,7 +7,7 @@ template <int NT, int MINB>
 static cudaError_t launch_v(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
     auto k = pncg_mixed_kernel<NT, MINB>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    k<<<grid, NT, smem, st>>>(d);
+    k<<<grid, NT, smem, st>>>(d, mixed_ptrs(d));
     return cudaGetLastError();
 }
 

@@ -158,8 +158,38 @@ constexpr int REBASE = 32;
 constexpr int NI_AFF = 4, NI_RIG = 8;
 
 // ---------------------------------------------------------------------- the kernel
+// Device pointers of the per-step scratch parts (host-computed from d2f_scene_desc.mscr).
+struct MixedPtrs {
+    float2 *xd, *rarm, *xr, *db, *dref, *rcs;
+    float4 *hvm, *g0, *gd, *du0;
+    double2 *g0d, *xbd;
+    int2 *ninfo;
+    float *phi0;
+};
+inline MixedPtrs mixed_ptrs(const d2f_scene_desc &d) {
+    const MixedLayout L = mixed_layout(d.N, d.T, d.Nb, d.n_col, d.n_rig);
+    unsigned char *ms = static_cast<unsigned char *>(d.mscr);
+    MixedPtrs p;
+    p.xd = reinterpret_cast<float2 *>(ms + L.xd);
+    p.rarm = reinterpret_cast<float2 *>(ms + L.rarm);
+    p.xr = reinterpret_cast<float2 *>(ms + L.xr);
+    p.db = reinterpret_cast<float2 *>(ms + L.db);
+    p.dref = reinterpret_cast<float2 *>(ms + L.dref);
+    p.rcs = reinterpret_cast<float2 *>(ms + L.rcs);
+    p.hvm = reinterpret_cast<float4 *>(ms + L.hvm);
+    p.g0 = reinterpret_cast<float4 *>(ms + L.g0);
+    p.gd = reinterpret_cast<float4 *>(ms + L.gd);
+    p.du0 = reinterpret_cast<float4 *>(ms + L.du0);
+    p.g0d = reinterpret_cast<double2 *>(ms + L.g0);
+    p.xbd = reinterpret_cast<double2 *>(ms + L.xbd);
+    p.ninfo = reinterpret_cast<int2 *>(ms + L.ninfo);
+    p.phi0 = reinterpret_cast<float *>(ms + L.phi0);
+    return p;
+}
+
 template <int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_constant__ d2f_scene_desc d) {
+__global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_constant__ d2f_scene_desc d,
+                                                              const __grid_constant__ MixedPtrs mp) {
     constexpr int NW = NT / 32;
     __shared__ SceneSh S;
     __shared__ Col cols[MAX_COL];
@@ -200,23 +230,23 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     const double2 *__restrict__ Tgt = reinterpret_cast<const double2 *>(d.bc_target);
     double2 *__restrict__ Ctr = reinterpret_cast<double2 *>(d.cand_tr);
     const double2 *__restrict__ Xr = reinterpret_cast<const double2 *>(d.xrest);
-    const MixedLayout ML = mixed_layout(d.N, d.T, d.Nb, d.n_col, d.n_rig);
-    unsigned char *ms = static_cast<unsigned char *>(d.mscr);
-    float2 *__restrict__ XD = reinterpret_cast<float2 *>(ms + ML.xd);     // x - x_n
-    float4 *__restrict__ HVM = reinterpret_cast<float4 *>(ms + ML.hvm);   // x_hat - x_n, mass
-    float4 *__restrict__ G0 = reinterpret_cast<float4 *>(ms + ML.g0);     // step-start gradient, FP32 pair
-    double2 *__restrict__ G0d = reinterpret_cast<double2 *>(ms + ML.g0);  // the same, FP64 while it is built
-    double2 *__restrict__ Esc64 = reinterpret_cast<double2 *>(d.escr);    // per-corner FP64 forces (base builds)
-    float4 *__restrict__ GD = reinterpret_cast<float4 *>(ms + ML.gd);     // per node: elastic gradient + diagonal sums
-    float2 *__restrict__ RARM = reinterpret_cast<float2 *>(ms + ML.rarm); // x_n - c_n (rigid pieces)
-    int2 *__restrict__ NINFO = reinterpret_cast<int2 *>(ms + ML.ninfo);  // node flags, boundary slot
-    float4 *__restrict__ DU0 = reinterpret_cast<float4 *>(ms + ML.du0);   // displacement edges at the base x_b
-    double2 *__restrict__ XBd = reinterpret_cast<double2 *>(ms + ML.xbd); // base positions x_b (FP64)
-    float2 *__restrict__ XR = reinterpret_cast<float2 *>(ms + ML.xr);     // x - x_b
-    float2 *__restrict__ DB = reinterpret_cast<float2 *>(ms + ML.db);     // x_b - x_n
-    float *__restrict__ PHI0 = reinterpret_cast<float *>(ms + ML.phi0);   // half-space distances at x_n, per node
-    float2 *__restrict__ DREF = reinterpret_cast<float2 *>(ms + ML.dref); // dx when the candidate list was built
-    float2 *__restrict__ RCS = reinterpret_cast<float2 *>(ms + ML.rcs);   // rigid pieces: centroid shift
+    // the per-step scratch arrays: pointers from the parameter space (constant bank), not
+    // registers
+    float2 *__restrict__ XD = mp.xd;       // x - x_n
+    float4 *__restrict__ HVM = mp.hvm;     // x_hat - x_n, mass
+    float4 *__restrict__ G0 = mp.g0;       // step-start gradient, FP32 pair
+    double2 *__restrict__ G0d = mp.g0d;    // the same, FP64 while it is built
+    double2 *__restrict__ Esc64 = reinterpret_cast<double2 *>(d.escr);  // per-corner FP64 forces (base builds)
+    float4 *__restrict__ GD = mp.gd;       // per node: elastic gradient + diagonal sums
+    float2 *__restrict__ RARM = mp.rarm;   // x_n - c_n (rigid pieces)
+    int2 *__restrict__ NINFO = mp.ninfo;   // node flags, boundary slot
+    float4 *__restrict__ DU0 = mp.du0;     // displacement edges at the base x_b
+    double2 *__restrict__ XBd = mp.xbd;    // base positions x_b (FP64)
+    float2 *__restrict__ XR = mp.xr;       // x - x_b
+    float2 *__restrict__ DB = mp.db;       // x_b - x_n
+    float *__restrict__ PHI0 = mp.phi0;    // half-space distances at x_n, per node
+    float2 *__restrict__ DREF = mp.dref;   // dx when the candidate list was built
+    float2 *__restrict__ RCS = mp.rcs;     // rigid pieces: centroid shift
 
     if (tid < n_col && tid < MAX_COL) {
         const double *c = d.colliders + 8 * tid;
