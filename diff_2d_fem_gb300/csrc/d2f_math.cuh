@@ -57,7 +57,7 @@ __device__ __forceinline__ double seg_closest(double px, double py, double ax, d
 }
 
 // kinds: 0 disc, 1 ellipse, 2 rounded box, 3 rounded triangle, 4 half-space
-__device__ inline SdfHit sdf_eval(int kind, double cx, double cy, double rx, double ry, double rref,
+static __device__ __noinline__ SdfHit sdf_eval(int kind, double cx, double cy, double rx, double ry, double rref,
                                   double x, double y) {
     SdfHit h{0, 0, 0, 0, 0, 0, 0};
     if (kind == 4) {  // half-space: phi = n . (x - c), flat
@@ -183,7 +183,7 @@ __device__ inline double accd(double px, double py, double ax, double ay, double
 // step that would have crossed the gap, or the last one taken), +inf when it reached t_c0 or
 // nothing moves. The reference reads the cap once per edge, after the edges before it have
 // lowered it (ipc_contact.py:211, 241); this lets the caller replay that order exactly.
-__device__ inline double accd_profile(double px, double py, double ax, double ay, double bx, double by,
+static __device__ __noinline__ double accd_profile(double px, double py, double ax, double ay, double bx, double by,
                                       double dpx, double dpy, double dax, double day, double dbx, double dby,
                                       double g, double t_c0, double &T) {
     double mx = (dpx + dax + dbx) / 3.0, my = (dpy + day + dby) / 3.0;
@@ -231,7 +231,7 @@ __device__ __forceinline__ M2 nh_d2(M2 F, M2 dF, double mu, double la) {
 __device__ __forceinline__ double ddot2(M2 A, M2 B) { return A.a * B.a + A.b * B.b + A.c * B.c + A.d * B.d; }
 
 // ---- 6x6 block: reduced Hessian, Cholesky with diagonal fallback, solve; affine.py:60-147
-__device__ inline void reduced_hessian(M2 A, double Mu, double La, double h2, const double *Hs, double (*H)[6]) {
+static __device__ __noinline__ void reduced_hessian(M2 A, double Mu, double La, double h2, const double *Hs, double (*H)[6]) {
     // Hs: x block then y block, 6 unique entries each: 00 01 02 11 12 22
     const int u[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     for (int r = 0; r < 6; ++r)
@@ -261,7 +261,7 @@ __device__ inline void reduced_hessian(M2 A, double Mu, double La, double h2, co
     }
 }
 
-__device__ inline void chol6(const double (*H)[6], double (*L)[6]) {
+static __device__ __noinline__ void chol6(const double (*H)[6], double (*L)[6]) {
     for (int r = 0; r < 6; ++r)
         for (int c = 0; c < 6; ++c) L[r][c] = 0.0;
     bool ok = true;
@@ -286,7 +286,7 @@ __device__ inline void chol6(const double (*H)[6], double (*L)[6]) {
     }
 }
 
-__device__ inline void chol6_solve(const double (*L)[6], const double *b, double *x) {
+static __device__ __noinline__ void chol6_solve(const double (*L)[6], const double *b, double *x) {
     double y[6];
     for (int i = 0; i < 6; ++i) {
         double s = b[i];
