@@ -105,7 +105,9 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
     for (int k = 0; k < NS; ++k) out_s[k] = dres[k];
 #pragma unroll
     for (int k = 0; k < NM; ++k) out_m[k] = mres[k];
-    __syncthreads();
+    // no barrier here: a later call writes `fred` only after its threads passed this call's
+    // second barrier (every read of `fred` is before it), and `dres` / `mres` only after its own
+    // first barrier, which every thread reaches after reading this call's results
 }
 
 // Byte layout of the mixed path's per-step scratch (d2f_scene_desc.mscr), 256-aligned parts.
@@ -153,7 +155,7 @@ __device__ __forceinline__ double2 tendon_dlen(PosF pos, const int32_t *t_node, 
 }
 
 // iterations between rebuilds of the FP64 gradient base
-constexpr int REBASE = 32;
+constexpr int REBASE = 64;
 // packed per-node flags (NINFO.x): bits 0-1 free mask, then these, bits 4-7 the rigid piece
 constexpr int NI_AFF = 4, NI_RIG = 8;
 
