@@ -6,6 +6,9 @@
                          W ~ U{32..128} pixels of 0.75 mm, per-pixel E log-uniform in
                          [0.1, 2] MPa, ground mu ~ U[0.3, 0.9] per scene, top-edge pressure
                          ~ U[0, 5] kPa): the batching configuration
+  pads_and_block()       a contact-heavy batch: a soft pad pushed by a kinematic jaw squeezes
+                         an affine rigid block against a second, static pad (IPC contact
+                         between bodies with per-scene friction)
   tendon_arms()          a batch of soft arms (16 x 64 pixels of 0.5 mm) pinned at one end
                          and bent by a tension-controlled tendon, per-pixel E log-uniform
                          in [0.2, 1.5] MPa, a piecewise-linear tension schedule and a target
@@ -110,3 +113,48 @@ def tendon_arms(n_scenes=256, seed=0, px=0.5e-3, steps=100):
     kw = dict(self_collision=False, friction=False, precision="fp64")
     return m, kw, 2e-3, dict(handles=hs, E_pixels=np.stack(Es), tension=tension, tip=np.asarray(tips),
                             target=np.asarray(targets), tendons=np.asarray(tendons))
+
+
+def pads_and_block(n_scenes=512, seed=0, steps=150, jaw_speed=0.01):
+    """The contact-heavy configuration: per scene, a 40 x 40-pixel soft pad (0.5 mm pixels,
+    20 mm, E 0.3 MPa, nu 0.45) whose outer column is a kinematic jaw translating at 10 mm/s,
+    a 16 x 16-pixel affine block (1 mm pixels, 16 mm, density 600, the model's 1 GPa rigid
+    modulus) 0.3 mm from it, and a second pad held still 0.3 mm beyond the block; the block's
+    height offset is U[-2, 2] mm, the body friction per scene U[0.4, 0.8], d-hat 0.1 mm,
+    gravity on. Returns (model, integrator kwargs, dt, extras) with extras = dict(command)
+    where command(k) sets the jaw targets of step k (0-based)."""
+    rng = np.random.default_rng(seed)
+    m = Model()
+    m.dhat = 1.0e-4
+    gap, half_b, pad = 0.3e-3, 8.0e-3, 20.0e-3
+    off = rng.uniform(-2.0e-3, 2.0e-3, n_scenes)
+    mu = rng.uniform(0.4, 0.8, n_scenes)
+    left, right = [], []
+    for i in range(n_scenes):
+        cy = 0.5 * pad
+        left.append(m.add_soft_body(np.ones((40, 40), np.uint8), physical_size=(pad, pad),
+                                    center=(-(half_b + gap + 0.5 * pad), cy), E=0.3e6, nu=0.45,
+                                    density=1100.0, env_id=i, mu=float(mu[i])))
+        m.add_affine_body(np.ones((16, 16), np.uint8), physical_size=(2 * half_b, 2 * half_b),
+                          center=(0.0, cy + off[i]), density=600.0, env_id=i, mu=float(mu[i]))
+        right.append(m.add_soft_body(np.ones((40, 40), np.uint8), physical_size=(pad, pad),
+                                     center=(half_b + gap + 0.5 * pad, cy), E=0.3e6, nu=0.45,
+                                     density=1100.0, env_id=i, mu=float(mu[i])))
+    m.finalize()
+    m.gravity = (0.0, -9.81)
+    jaws = []
+    for hl, hr in zip(left, right):
+        X = m.rest_x(hl)
+        jl = np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0]
+        m.set_kinematic_constraint(hl, jl)
+        Y = m.rest_x(hr)
+        m.set_kinematic_constraint(hr, np.where(Y[:, 0] > Y[:, 0].max() - 1e-9)[0])
+        jaws.append((hl, X, jl))
+    dt = 1.0e-3
+
+    def command(k):
+        for hl, X, jl in jaws:
+            tgt = X.copy()
+            tgt[jl, 0] += jaw_speed * dt * (k + 1)
+            m.set_kinematic_target(hl, tgt)
+    return m, {}, dt, dict(command=command, steps=steps, offset=off, mu=mu)

@@ -80,6 +80,8 @@ def lib():
         _LIB.d2o_step.restype = C.c_int
         _LIB.d2o_energy.argtypes = [C.POINTER(_Solver), _PD]
         _LIB.d2o_energy.restype = None
+        _LIB.d2o_ipc_energy.argtypes = [C.POINTER(_Solver), _PD]
+        _LIB.d2o_ipc_energy.restype = None
     return _LIB
 
 
@@ -255,6 +257,17 @@ class OracleSolver:
     def energy(self):
         out = np.zeros(self.B)
         self._lib.d2o_energy(C.byref(self.s), out.ctypes.data_as(_PD))
+        return out
+
+    def ipc_energy(self, x=None, xn=None):
+        """The IPC contact energy per environment (barrier + lagged friction) at x, slip from
+        xn; x and xn default to the solver's current state."""
+        if x is not None:
+            self.state["x"][:] = np.asarray(x, np.float64).reshape(-1, 2)
+        if xn is not None:
+            self.state["xn"][:] = np.asarray(xn, np.float64).reshape(-1, 2)
+        out = np.zeros(self.B)
+        self._lib.d2o_ipc_energy(C.byref(self.s), out.ctypes.data_as(_PD))
         return out
 
     @property

@@ -1224,6 +1224,14 @@ static void energy_into(d2o_solver *s, double *E) {
     if (s->n_tendon) tendon_energy(s, E);
 }
 void d2o_energy(d2o_solver *s, double *buf) { energy_into(s, buf); }
+/* the IPC contact term alone (IPCContact.energy, ipc_contact.py:414-429): barrier and lagged
+   friction between bodies at s->x, friction slip measured from s->xn; per environment */
+void d2o_ipc_energy(d2o_solver *s, double *buf) {
+    for (int e = 0; e < s->B; ++e) buf[e] = 0.0;
+    if (!s->has_ipc) return;
+    ipc_launch L = ipc_base(s, 2, s->p, buf, s->clr_min, s->alpha);
+    ipc_pair(&L);
+}
 
 /* ------------------------------------------------------------------ the loop, solver.py:252-425 */
 static void iterate(d2o_solver *s) {

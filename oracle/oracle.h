@@ -88,6 +88,7 @@ int d2o_step(d2o_solver *s);
 
 /* Per-env total energy (PNCG2DSolver._energy_into) into s->Ener. */
 void d2o_energy(d2o_solver *s, double *buf);
+void d2o_ipc_energy(d2o_solver *s, double *buf);
 
 /* Number of floating-point operations the element pass of one iteration would perform
  * is not counted here; see the Python side. */

@@ -1,0 +1,114 @@
+"""The contact-heavy configuration (a soft pad pushed by a kinematic jaw squeezes an affine
+block against a second pad; IPC contact between bodies with per-scene friction).
+
+At the configuration's iteration budget (129, the reference's CFL rule) no step converges,
+and contact with friction amplifies any difference: two FP64 implementations that differ
+only in summation order (CUDA and the serial oracle) separate from 5e-15 (step 1) to 1e-9
+(step 9) and 5e-4 (step 25) of the coordinates. So the FP64 path is checked against the
+oracle over the first steps and on one step from a shared state with contact active, and the
+mixed path against FP64 on one converged step from that state.
+"""
+import warnings
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(n, seed):
+    from diff_2d_fem_gb300 import workloads, scene, ImplicitIntegrator
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")              # mixed pixel sizes, as configured
+        m, kw, dt, ex = workloads.pads_and_block(n, seed=seed)
+    ex["command"](0)
+    prob = scene.solver_problem(m, ImplicitIntegrator(**kw), dt)
+    prob["rest"] = np.asarray(m.me.rest_pos, np.float64)
+    return m, prob, ex
+
+
+def _targets(m):
+    return np.asarray(m._targets, np.float64)
+
+
+def test_fp64_matches_oracle_first_steps():
+    """One scene, the configured budget, 7 steps: within 1e-9 of the oracle every step."""
+    from diff_2d_fem_gb300.device import DeviceSolver
+    m, prob, ex = _scene(1, seed=3)
+    s = DeviceSolver(prob, precision="fp64")
+    o = oracle.OracleSolver(prob)
+    bc = np.asarray(prob["bc_idx"])
+    for k in range(7):
+        ex["command"](k)
+        tg = _targets(m)
+        s.set_targets(tg)
+        o.set_bc_target(tg[bc])
+        s.step()
+        o.step()
+        _, _, st = s.stats()
+        assert (st == 0).all()
+        assert rel_err(s.get_x(), o.x) < 1e-9, k
+    s.close()
+
+
+def _contact_state():
+    """The state after 24 steps of one scene (block gripped, contact active)."""
+    from diff_2d_fem_gb300.device import DeviceSolver
+    m, prob, ex = _scene(1, seed=3)
+    s = DeviceSolver(prob, precision="fp64")
+    for k in range(24):
+        ex["command"](k)
+        s.set_targets(_targets(m))
+        s.step()
+    x, v, q = s.get_x(), s.get_v(), s.get_affine_q()
+    s.close()
+    p2 = dict(prob)
+    p2["x"], p2["v"] = x, v
+    p2["affine"] = dict(prob["affine"], q=q)
+    ex["command"](24)
+    return p2, _targets(m), x
+
+
+def _one_step(prob, tg, precision):
+    from diff_2d_fem_gb300.device import DeviceSolver
+    sd = DeviceSolver(prob, precision=precision)
+    sd.set_targets(tg)
+    sd.step()
+    _, _, st = sd.stats()
+    assert (st == 0).all(), precision
+    x = sd.get_x()
+    sd.close()
+    return x
+
+
+def test_step_in_contact_matches_oracle():
+    """From the in-contact state, one step at the configured budget (129 iterations): the
+    FP64 path within 1e-8 of the oracle, relative to the coordinates."""
+    p2, tg, _ = _contact_state()
+    x64 = _one_step(p2, tg, "fp64")
+    o = oracle.OracleSolver(p2)
+    o.set_bc_target(tg[np.asarray(p2["bc_idx"])])
+    o.step()
+    assert rel_err(x64, o.x) < 1e-8
+
+
+def test_converged_step_in_contact_mixed_matches_fp64():
+    """From the in-contact state, one step run (nearly) to convergence: 20000 iterations (the
+    1 GPa block squeezed between 0.3 MPa pads is so ill-conditioned that 4000 iterations still
+    leave 3e-5 and 20000 leave 2e-9 of the 60000-iteration answer, against which mixed and FP64
+    agree to 2.5e-11). The mixed path within 1e-8 of the FP64 path, relative to the
+    coordinates, and the IPC contact energies (oracle-evaluated) within 1e-6 relative: the
+    barrier energy varies like (position change) / (gap ~ 1e-5 m), far faster than positions."""
+    p2, tg, x0 = _contact_state()
+    p2["iter_max"], p2["eps"] = 20000, 0.0
+    x64 = _one_step(p2, tg, "fp64")
+    xmx = _one_step(p2, tg, "mixed")
+    assert rel_err(xmx, x64) < 1e-8
+    o = oracle.OracleSolver(p2)
+    e64 = o.ipc_energy(x64, x0)[0]
+    emx = o.ipc_energy(xmx, x0)[0]
+    assert e64 > 0.0
+    assert abs(emx - e64) / e64 < 1e-6
