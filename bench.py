@@ -103,8 +103,8 @@ def algorithmic_bytes(prob, iters, mixed):
 # (bytes per scene-iteration, launch shape captured). A launch's traffic is this times its
 # scene-iterations (traffic grows with the iterations each scene runs).
 TRAFFIC_PER_SCENE_ITER = {
-    "mixed": ((50.444956672e9 + 29.283109632e9) / (608 * 240.19078947368422), "128x4"),
-    "fp64": ((98.965070336e9 + 59.728653568e9) / (608 * 239.94078947368422), "128x4"),
+    "mixed": ((8.505456896e9 + 5.764890880e9) / (608 * 239.94736842105263), "256x3"),
+    "fp64": ((76.904082432e9 + 59.028497920e9) / (608 * 239.94078947368422), "256x2"),
 }
 
 
