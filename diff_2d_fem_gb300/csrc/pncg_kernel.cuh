@@ -389,6 +389,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                             atomicAdd(dp_, R(ch[q] * hx));
                             atomicAdd(dp_ + 1, R(ch[q] * hy));
                         }
+                    } else if (mode == 2) {  // energy: barrier + lagged friction (ipc_contact.py:414-429)
+                        const double asl = epsv / inv_dt, au = dabs(ut);
+                        const double f0 = au < asl ? au * au / (2.0 * asl) : au - 0.5 * asl;
+                        acc_pHp += coef * h2 * (ikappa * barrier_b<double>(dist, idhat) + mu_p * f_n * f0);
                     } else {
                         double bpp = barrier_bpp<double>(dist, idhat);
                         R2 u0 = P[ip], u1 = P[ia], u2 = P[ib];
@@ -489,6 +493,92 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
 
         // kinematic sweep (IPCContact._sweep, ipc_contact.py:456-463 with bc_motion /
         // ccd mode 3 / far cap / bc_advance, :299-331)
+        // The scene's step energy at X, FP64, every term (energy_into, solver.py:453-498):
+        // inertia and elastic (kernels.py:445-468), collider barriers and lagged friction
+        // (core/sdf.py:174-181, 274-294; kernels.py:483-513), external force
+        // (actuation.py:43-50), affine bodies (affine.py:237-246), IPC (ipc_contact.py:414-429)
+        // and tendons (actuation.py:259-268). Every thread calls; every thread gets the sum.
+        auto scene_energy = [&]() -> double {
+            double e = 0.0;
+            for (int i = n0 + tid; i < n1; i += NT) {
+                const double2 xi = X[i], xh = Xh[i];
+                const double ux = xi.x - xh.x, uy = xi.y - xh.y;
+                e += 0.5 * d.mass[i] * (ux * ux + uy * uy);
+                if (d.fext) {
+                    const double2 f = Fx[i], xn = Xn[i];
+                    e += -h2 * (f.x * (xi.x - xn.x) + f.y * (xi.y - xn.y));
+                }
+            }
+            for (int t = t0 + tid; t < t1; t += NT) {
+                const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
+                const double2 x0 = X[i0], x1 = X[i1], x2 = X[i2];
+                const R4 B = Bm[t];
+                const double e1x = x1.x - x0.x, e1y = x1.y - x0.y, e2x = x2.x - x0.x, e2y = x2.y - x0.y;
+                const double F00 = e1x * B.x + e2x * B.z, F01 = e1x * B.y + e2x * B.w;
+                const double F10 = e1y * B.x + e2y * B.z, F11 = e1y * B.y + e2y * B.w;
+                const double J = F00 * F11 - F10 * F01, logJ = log(dmax(J, 1.0e-6));
+                const double I2 = F00 * F00 + F01 * F01 + F10 * F10 + F11 * F11;
+                const double mu = Mu[t], la = La[t];
+                e += h2 * double(Ar[t]) * (0.5 * mu * (I2 - 2.0) - mu * logJ + 0.5 * la * logJ * logJ);
+            }
+            for (int j = tid; j < nbl; j += NT) {
+                const int n = d.bnd[sg.bnd0 + j];
+                const double2 xi = X[n];
+                const uint8_t fm = d.free_mask[n];
+                for (int k = 0; k < n_col; ++k) {
+                    const Col c = cols[k];
+                    double dd, nx, ny, gn = 1.0;
+                    if (c.kind == 0) {
+                        const double ex = xi.x - c.cx, ey = xi.y - c.cy, dc = sqrt(ex * ex + ey * ey);
+                        dd = dc - c.r; nx = ex / dc; ny = ey / dc;
+                    } else {
+                        const SdfHit hh = sdf_eval(c.kind, c.cx, c.cy, c.rx, c.ry, c.rref, xi.x, xi.y);
+                        dd = hh.d;
+                        gn = sqrt(hh.gx * hh.gx + hh.gy * hh.gy);
+                        nx = hh.gx / dmax(gn, 1.0e-30); ny = hh.gy / dmax(gn, 1.0e-30);
+                    }
+                    if (dd <= 0.0 || dd >= dhat) continue;
+                    e += h2 * kappa * barrier_b<double>(dd, dhat);
+                    if (d.friction && (fm & 3)) {
+                        const double2 xni = Xn[n];
+                        const double f_n = kappa * dabs(barrier_bp<double>(dd, dhat)) * gn;
+                        const double vx = (xi.x - xni.x) * inv_dt, vy = (xi.y - xni.y) * inv_dt;
+                        const double vn = vx * nx + vy * ny;
+                        const double vtx = vx - vn * nx, vty = vy - vn * ny;
+                        const double ut = sqrt(vtx * vtx + vty * vty) / inv_dt, a = epsv / inv_dt;
+                        const double f0 = ut < a ? ut * ut / (2.0 * a) : ut - a * 0.5;
+                        e += h2 * colmu[k] * f_n * f0;
+                    }
+                }
+            }
+            for (int b = sg.aff0 + tid; b < sg.aff0 + sg.naff; b += NT) {
+                const double *q = d.a_q + 6 * b;
+                const M2 A{q[1], q[2], q[4], q[5]};
+                const double logJ = log(dmax(det2(A), 1.0e-6));
+                e += h2 * (0.5 * d.a_Mu[b] * (ddot2(A, A) - 2.0) - d.a_Mu[b] * logJ + 0.5 * d.a_La[b] * logJ * logJ);
+            }
+            if (scene_ipc) ipc_pairs(2, e, 0.0);
+            for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
+                double L = 0.0;
+                for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
+                    if (d.t_tid[j] != k || d.t_nxt[j] < 0) continue;
+                    const double2 xa = X[d.t_node[j]], xb = X[d.t_node[d.t_nxt[j]]];
+                    const double ex = xb.x - xa.x, ey = xb.y - xa.y;
+                    L += sqrt(ex * ex + ey * ey);
+                }
+                if (d.t_stiff[k] > 0.0) {
+                    const double ext = L - d.t_L0[k];
+                    if (ext > 0.0) e += 0.5 * h2 * d.t_stiff[k] * ext * ext;
+                } else {
+                    e += h2 * dmax(d.t_Tcmd[k], 0.0) * L;
+                }
+            }
+            double v[1] = {e};
+            const int ops[1] = {0};
+            block_reduce<NT, 1>(v, ops, red);
+            return v[0];
+        };
+
         auto sweep = [&]() {
             ipc_refresh(false);
             double qi = 0.0;
@@ -1159,8 +1249,35 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 __syncthreads();
             }
 
-            // ---------------------------------------------- D1: update x (update_x_kernel + expand)
-            {
+            // ---------------------------------------------- D1: update x (update_x_kernel + expand),
+            // or the backtracking line search (solver.py:397-425)
+            if (d.line_search) {
+                // E0 at x, then n_backtrack trial points x0 + alpha p, alpha halved while the
+                // energy exceeds E0 + ls_tol (|E0| + 1) (ls_halve_kernel, solver.py:63-73)
+                double2 *__restrict__ X0 = reinterpret_cast<double2 *>(d.xu);
+                const double E0 = scene_energy();
+                for (int i = n0 + tid; i < n1; i += NT) X0[i] = X[i];
+                __syncthreads();
+                auto trial = [&]() {  // set_x_from_x0_kernel, solver.py:52-60
+                    if (S.active) {
+                        const double al = S.alpha;
+                        for (int i = n0 + tid; i < n1; i += NT) {
+                            const R2 pp = P[i];
+                            const double2 x0 = X0[i];
+                            X[i] = make_double2(x0.x + al * double(pp.x), x0.y + al * double(pp.y));
+                        }
+                    }
+                    __syncthreads();
+                };
+                for (int bt = 0; bt < d.n_backtrack; ++bt) {
+                    trial();
+                    if (scene_ipc) ipc_refresh(false);
+                    const double E = scene_energy();
+                    if (tid == 0 && S.active && E > E0 + d.ls_tol * (dabs(E0) + 1.0)) S.alpha *= 0.5;
+                    __syncthreads();
+                }
+                trial();
+            } else {
                 const bool act = S.active != 0;
                 const double al = S.alpha;
                 for (int i = n0 + tid; i < n1; i += NT) {

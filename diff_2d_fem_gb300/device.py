@@ -290,7 +290,13 @@ class DeviceSolver:
         d.threads = int(threads or 0)
         d.blocks_per_sm = int(blocks_per_sm or 0)
         if int(sc.get("line_search", 0)):
-            raise NotImplementedError("the energy line search runs on the CPU oracle only in this build")
+            if self.mixed:
+                raise NotImplementedError("the energy line search runs in FP64 only (precision='fp64')")
+            if n_aff:
+                raise NotImplementedError("the energy line search with affine bodies is not in this build")
+            self._t["xu"] = torch.zeros((N, 2), dtype=torch.float64, device=self.dev)
+            d.xu = self._t["xu"].data_ptr()
+            d.line_search, d.n_backtrack, d.ls_tol = 1, int(sc.get("n_bt", 4)), float(sc.get("ls_tol", 1e-7))
         h = C.c_void_p()
         torch.cuda.synchronize(self.dev)
         _lib.check(self.L.d2f_create(C.byref(d), C.byref(h)), "d2f_create")

@@ -9,6 +9,8 @@
   pads_and_block()       a contact-heavy batch: a soft pad pushed by a kinematic jaw squeezes
                          an affine rigid block against a second, static pad (IPC contact
                          between bodies with per-scene friction)
+  slab_with_holes()      the large-scene configuration: a 256 x 1024-pixel soft slab with 200
+                         circular holes resting on the ground, 32 affine discs dropped on it
   tendon_arms()          a batch of soft arms (16 x 64 pixels of 0.5 mm) pinned at one end
                          and bent by a tension-controlled tendon, per-pixel E log-uniform
                          in [0.2, 1.5] MPa, a piecewise-linear tension schedule and a target
@@ -158,3 +160,53 @@ def pads_and_block(n_scenes=512, seed=0, steps=150, jaw_speed=0.01):
             tgt[jl, 0] += jaw_speed * dt * (k + 1)
             m.set_kinematic_target(hl, tgt)
     return m, {}, dt, dict(command=command, steps=steps, offset=off, mu=mu)
+
+
+def _disc_mask(r):
+    """A (2r, 2r) pixel mask of a disc of radius r pixels (pixel centres inside)."""
+    c = np.arange(2 * r) + 0.5 - r
+    return ((c[None, :] ** 2 + c[:, None] ** 2) <= r * r).astype(np.uint8)
+
+
+def slab_with_holes(n_scenes=1, seed=0, H=256, W=1024, px=0.5e-3, n_holes=200, n_discs=32,
+                    hole_r=(3, 12), disc_r=(8, 20)):
+    """The large-scene configuration: per scene, an H x W-pixel soft slab (E 1 MPa, nu 0.40,
+    density 1100) lying on the ground with n_holes circular holes of radius U{hole_r} pixels
+    at seeded, non-overlapping centres, and n_discs affine discs of radius U{disc_r} pixels
+    (density U[500, 2000]) placed 5-50 mm above the slab at seeded, non-overlapping x; gravity
+    on, IPC contact between bodies and with the ground. Defaults: 256 x 1024 pixels of 0.5 mm
+    (0.128 m x 0.512 m), 200 holes, 32 discs."""
+    rng = np.random.default_rng(seed)
+    m = Model()
+    m.add_ground(0.0)
+    dhat = px / 8.0
+    for e in range(n_scenes):
+        mask = np.ones((H, W), np.uint8)
+        yy, xx = np.mgrid[0:H, 0:W]
+        placed = []
+        tries = 0
+        while len(placed) < n_holes and tries < 200 * n_holes:
+            tries += 1
+            r = int(rng.integers(hole_r[0], hole_r[1] + 1))
+            cy, cx = rng.uniform(r + 2, H - r - 2), rng.uniform(r + 2, W - r - 2)
+            if any((cy - a) ** 2 + (cx - b) ** 2 < (r + q + 2) ** 2 for a, b, q in placed):
+                continue
+            placed.append((cy, cx, r))
+            mask[(yy + 0.5 - cy) ** 2 + (xx + 0.5 - cx) ** 2 < r * r] = 0
+        m.add_soft_body(mask, physical_size=(W * px, H * px), center=(0.0, 0.5 * H * px + 0.9 * dhat),
+                        E=1.0e6, nu=0.40, density=1100.0, env_id=e)
+        xs = []
+        tries = 0
+        while len(xs) < n_discs and tries < 200 * n_discs:
+            tries += 1
+            r = int(rng.integers(disc_r[0], disc_r[1] + 1))
+            x = rng.uniform(-0.5 * W * px + r * px, 0.5 * W * px - r * px)
+            if any(abs(x - a) < (r + q) * px + 2 * px for a, q in xs):
+                continue
+            xs.append((x, r))
+            y = H * px + rng.uniform(5e-3, 50e-3) + r * px
+            m.add_affine_body(_disc_mask(r), physical_size=(2 * r * px, 2 * r * px), center=(x, y),
+                              density=float(rng.uniform(500.0, 2000.0)), env_id=e)
+    m.finalize()
+    m.gravity = (0.0, -9.81)
+    return m, {}, 1e-3

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define D2F_ABI_VERSION 1
+#define D2F_ABI_VERSION 2
 
 /* status codes */
 #define D2F_OK 0
@@ -67,7 +67,7 @@ typedef struct d2f_scene_desc {
     const d2f_seg *segs;         /* n_scenes */
     /* node state */
     double *x, *v, *xn, *xhat;   /* N x 2 */
-    double *xu;                  /* unused (NULL) */
+    double *xu;                  /* N x 2: the line search's saved positions (NULL without it) */
     const double *xrest;         /* N x 2: rest positions (mixed precision; else NULL) */
     void *grad, *grad_prev, *p, *diagH, *diag_el; /* N x 2 real */
     const double *mass;          /* N */
@@ -128,6 +128,11 @@ typedef struct d2f_scene_desc {
                                     scenes per SM, else 128) */
     int32_t blocks_per_sm;       /* resident scene blocks per SM the register budget targets
                                     (0: the library's default for that width) */
+    /* backtracking energy line search (PNCG2DSolver line_search, solver.py:397-425): FP64
+       solvers without affine bodies; needs xu */
+    double ls_tol;               /* accept while E <= E0 + ls_tol (|E0| + 1) */
+    int32_t line_search;         /* 0 off, 1 on */
+    int32_t n_backtrack;         /* halvings tried per iteration */
 } d2f_scene_desc;
 
 typedef struct d2f_solver d2f_solver;

@@ -15,7 +15,7 @@ from helpers import fixtures, load_fixture, package_ns, rel_err
 
 pytestmark = pytest.mark.gpu
 
-GPU_SCENES = [n for n in fixtures() if n != "line_search"]
+GPU_SCENES = fixtures()
 TOL_FP64 = 1e-9
 TOL_MIXED = 1e-6
 
