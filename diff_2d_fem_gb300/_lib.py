@@ -13,7 +13,7 @@ _I = C.c_int32
 _D = C.c_double
 _P = C.c_void_p
 
-D2F_ABI_VERSION = 2
+D2F_ABI_VERSION = 3
 D2F_FP64, D2F_MIXED = 0, 1
 ERRORS = {0: "ok", -1: "D2F_EINVAL", -2: "D2F_ECUDA", -3: "D2F_ECAP", -4: "D2F_ENAN"}
 
@@ -40,7 +40,7 @@ DESC_FIELDS = (
                          "area_shrink", "ccd_eta", "cg_guard", "gtol", "ipc_mu", "ipc_dhat", "ipc_kappa",
                          "reach", "gap", "bc_floor", "skin")]
     + [(n, _I) for n in ("iter_max", "conv_check", "friction", "per_body", "threads", "blocks_per_sm")]
-    + [("ls_tol", _D), ("line_search", _I), ("n_backtrack", _I)]
+    + [("ls_tol", _D), ("line_search", _I), ("n_backtrack", _I), ("blocks_per_scene", _I)]
 )
 
 
@@ -50,7 +50,7 @@ class SceneDesc(C.Structure):
 
 EXPORTS = ("d2f_abi_version", "d2f_create", "d2f_step", "d2f_set_dt", "d2f_stats", "d2f_destroy",
            "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc", "d2f_mixed_scratch_bytes",
-           "d2f_adjoint_solve", "d2f_adjoint_vjp")
+           "d2f_adjoint_solve", "d2f_adjoint_vjp", "d2f_launch_shape")
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
@@ -83,6 +83,8 @@ def load(build_if_missing: bool = True):
     L.d2f_last_error.restype = C.c_char_p
     L.d2f_kernels_per_step.argtypes = [_P]
     L.d2f_kernels_per_step.restype = _I
+    L.d2f_launch_shape.argtypes = [_P, _P, _P, _P]
+    L.d2f_launch_shape.restype = _I
     L.d2f_step_noalloc.argtypes = [C.POINTER(SceneDesc), _P]
     L.d2f_step_noalloc.restype = _I
     L.d2f_mixed_scratch_bytes.argtypes = [_I, _I, _I, _I, _I]

@@ -4,8 +4,9 @@
 
 struct d2f_solver {
     d2f_scene_desc d;
-    int grid;
+    int grid;  // launched blocks (cs > 1: clusters x cs)
     int smem;
+    int cs;    // blocks per scene (one cluster)
 };
 
 extern thread_local char g_err[512];

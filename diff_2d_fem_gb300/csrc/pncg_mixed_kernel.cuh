@@ -27,6 +27,7 @@
 //   * step caps (inversion, CCD, |p|, clearance) are FP32 minima/maxima.
 // At the end of the step x = x_b + r and v = (x - x_n)/dt in FP64.
 #pragma once
+#include <cooperative_groups.h>
 #include <type_traits>
 
 #include "pncg_kernel.cuh"
@@ -60,6 +61,7 @@ template <int NT, int NS, int NM>
 __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], const int (&mops)[NM],
                                                 double (&out_s)[NS], float (&out_m)[NM], float *fred,
                                                 double *dres, float *mres) {
+    static_assert(NS <= 20 && NM <= 16 && 2 * NS + NM <= 40, "fred / dres / mres of the step kernel");
     constexpr int NW = NT / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -108,6 +110,66 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
     // no barrier here: a later call writes `fred` only after its threads passed this call's
     // second barrier (every read of `fred` is before it), and `dres` / `mres` only after its own
     // first barrier, which every thread reaches after reading this call's results
+}
+
+// Reductions over the thread group working on one scene. CS == 1: the block reduction. A
+// cluster of CS blocks on one scene (large scenes): the block reduction, then the CS block
+// results combined in rank order through distributed shared memory, so every block of the
+// cluster holds the same, deterministic result. `cres` / `cmres`: per-block scratch.
+template <int NT, int CS, int NV>
+__device__ __forceinline__ void scene_reduce(double (&v)[NV], const int (&ops)[NV], double *red, double *cres) {
+    static_assert(NV <= 20, "red / cres of the step kernel");
+    block_reduce<NT, NV>(v, ops, red);
+    if constexpr (CS > 1) {
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+        constexpr int NW = NT / 32;
+        double *mine = red + NW * NV;  // the block result, kept by block_reduce
+        cl.sync();
+        if (threadIdx.x < NV) {
+            const int k = threadIdx.x;
+            double a = cl.map_shared_rank(mine, 0)[k];
+            for (int r = 1; r < CS; ++r) {
+                const double b = cl.map_shared_rank(mine, r)[k];
+                a = ops[k] == 0 ? a + b : (ops[k] == 1 ? dmax(a, b) : dmin(a, b));
+            }
+            cres[k] = a;
+        }
+        cl.sync();  // cres ready, and every remote read of `red` done before it is reused
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = cres[k];
+    }
+}
+
+template <int NT, int CS, int NS, int NM>
+__device__ __forceinline__ void scene_reduce_mx(FF (&s)[NS], float (&m)[NM], const int (&mops)[NM],
+                                                double (&out_s)[NS], float (&out_m)[NM], float *fred,
+                                                double *dres, float *mres, double *cres, float *cmres) {
+    block_reduce_mx<NT, NS, NM>(s, m, mops, out_s, out_m, fred, dres, mres);
+    if constexpr (CS > 1) {
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+        cl.sync();
+        const int k = threadIdx.x;
+        if (k < NS) {
+            double a = 0.0;
+            for (int r = 0; r < CS; ++r) a += cl.map_shared_rank(dres, r)[k];
+            cres[k] = a;
+        } else if (k < NS + NM) {
+            const int j = k - NS;
+            float a = cl.map_shared_rank(mres, 0)[j];
+            for (int r = 1; r < CS; ++r) {
+                const float b = cl.map_shared_rank(mres, r)[j];
+                a = mops[j] == 1 ? fmaxf(a, b) : mops[j] == 2 ? fminf(a, b) : a + b;
+            }
+            cmres[j] = a;
+        }
+        cl.sync();
+#pragma unroll
+        for (int q = 0; q < NS; ++q) out_s[q] = cres[q];
+#pragma unroll
+        for (int q = 0; q < NM; ++q) out_m[q] = cmres[q];
+    }
 }
 
 // Byte layout of the mixed path's per-step scratch (d2f_scene_desc.mscr), 256-aligned parts.
@@ -189,17 +251,27 @@ inline MixedPtrs mixed_ptrs(const d2f_scene_desc &d) {
     return p;
 }
 
-template <int NT, int MINB>
+// CS: blocks per scene. 1: a block per scene (batches). > 1: a cluster of CS blocks works on
+// one scene (large scenes): the scene's loops are spread over the cluster's threads, phases are
+// separated by cluster barriers, reductions combine the blocks' results through distributed
+// shared memory, and the per-scene scalars are kept, identically, by every block.
+template <int NT, int MINB, int CS = 1>
 __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_constant__ d2f_scene_desc d,
                                                               const __grid_constant__ MixedPtrs mp) {
+    namespace cg = cooperative_groups;
     constexpr int NW = NT / 32;
+    constexpr bool CL = CS > 1;
+    constexpr int GS = CS * NT;  // threads working on one scene
     __shared__ SceneSh S;
     __shared__ Col cols[MAX_COL];
     __shared__ double red[NW * 20 + 20];
     __shared__ float fred[NW * 40];
     __shared__ double dres[20];
-    __shared__ float mres[8];
+    __shared__ float mres[16];               // block_reduce_mx: up to 16 FP32 results (rigid pass: 12)
     __shared__ int sc_next;
+    __shared__ int s_cnt;                    // cluster list build: this block's kept pairs
+    __shared__ double cres[24];              // cluster reductions: the combined result
+    __shared__ float cmres[16];
     __shared__ int s_wcnt[NW];
     __shared__ unsigned s_wmask[NW];
     __shared__ double s_H6[6][6], s_L6[6][6];
@@ -209,6 +281,11 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     extern __shared__ float2 pos32[];
 
     const int tid = threadIdx.x;
+    const int crank = CL ? (int)cg::this_cluster().block_rank() : 0;
+    const int gt = crank * NT + tid;  // this thread's index among the scene's threads
+    auto gsync = [&]() {              // a phase barrier of the scene's thread group
+        if constexpr (CL) cg::this_cluster().sync(); else __syncthreads();
+    };
     const double dt = d.dt, h2 = dt * dt, inv_dt = 1.0 / dt;
     const double dhat = d.dhat;
     const float fh2 = (float)h2, fkappa = (float)d.kappa, fdhat = (float)dhat, fepsv = (float)d.epsv,
@@ -258,9 +335,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     }
 
     for (;;) {
-        if (tid == 0) sc_next = atomicAdd(d.work, 1);
-        __syncthreads();
-        const int sc = sc_next;
+        if (tid == 0 && crank == 0) sc_next = atomicAdd(d.work, 1);
+        int sc;
+        if constexpr (CL) {  // rank 0 takes the next scene; the cluster reads it from rank 0
+            cg::cluster_group cl = cg::this_cluster();
+            cl.sync();
+            sc = *cl.map_shared_rank(&sc_next, 0);
+            cl.sync();  // every read of rank 0's sc_next done before any block moves on or exits
+        } else {
+            __syncthreads();
+            sc = sc_next;
+        }
         if (sc >= d.n_scenes) break;
         const d2f_seg sg = d.segs[sc];
         const int n0 = sg.node0, n1 = sg.node0 + sg.nn;
@@ -290,7 +375,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         // converges, so neither the positions' FP32 resolution nor the large, mutually
         // cancelling forces of a loaded body limit how far it converges (iterative refinement).
         auto build_base = [&]() {
-            for (int i = n0 + tid; i < n1; i += NT) {
+            for (int i = n0 + gt; i < n1; i += GS) {
                 const double2 b = XBd[i], xn = Xn[i];
                 const float2 r = XR[i];
                 const double2 xb = make_double2(b.x + (double)r.x, b.y + (double)r.y);
@@ -300,8 +385,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 DB[i] = db;
                 XD[i] = db;
             }
-            __syncthreads();
-            for (int t = t0 + tid; t < t1; t += NT) {
+            gsync();
+            for (int t = t0 + gt; t < t1; t += GS) {
                 const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
                 const double2 a0 = XBd[i0], a1 = XBd[i1], a2 = XBd[i2], r0 = Xr[i0], r1 = Xr[i1], r2 = Xr[i2];
                 const double e1x = (a1.x - a0.x) - (r1.x - r0.x), e1y = (a1.y - a0.y) - (r1.y - r0.y);
@@ -327,8 +412,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 Esc64[3 * t + 1] = make_double2(g1x, g1y);
                 Esc64[3 * t + 2] = make_double2(g2x, g2y);
             }
-            __syncthreads();
-            for (int i = n0 + tid; i < n1; i += NT) {
+            gsync();
+            for (int i = n0 + gt; i < n1; i += GS) {
                 double gx = 0.0, gy = 0.0;
                 for (int k = __ldg(d.inc_ptr + i); k < __ldg(d.inc_ptr + i + 1); ++k) {
                     const double2 c = Esc64[__ldg(d.inc + k)];
@@ -340,9 +425,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 }
                 G0d[i] = make_double2(gx, gy);
             }
-            __syncthreads();
+            gsync();
             if (sg.nten > 0) {  // tendon force at x_b (Tendon.grad_diag, actuation.py:169-228)
-                for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
+                for (int k = sg.ten0 + gt; k < sg.ten0 + sg.nten; k += GS) {
                     double L = 0.0;
                     for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
                         if (d.t_tid[j] != k) continue;
@@ -361,26 +446,26 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     }
                     d.t_state[4 * k + 1] = tau;  // tension at x_b, read by the increments
                 }
-                __syncthreads();
-                for (int j = sg.tent0 + tid; j < sg.tent0 + sg.ntent; j += NT) {
+                gsync();
+                for (int j = sg.tent0 + gt; j < sg.tent0 + sg.ntent; j += GS) {
                     const int n = d.t_node[j];
                     const double tau = d.t_state[4 * d.t_tid[j] + 1];
                     const double2 g = tendon_dlen(xbpos, d.t_node, d.t_prv[j], d.t_nxt[j], n);
                     atomicAdd(&G0d[n].x, h2 * tau * g.x);
                     atomicAdd(&G0d[n].y, h2 * tau * g.y);
                 }
-                __syncthreads();
+                gsync();
             }
-            for (int i = n0 + tid; i < n1; i += NT) {  // to a compensated FP32 pair, in place
+            for (int i = n0 + gt; i < n1; i += GS) {  // to a compensated FP32 pair, in place
                 const double2 g = G0d[i];
                 const float hx = (float)g.x, hy = (float)g.y;
                 G0[i] = make_float4(hx, hy, (float)(g.x - (double)hx), (float)(g.y - (double)hy));
             }
-            __syncthreads();
+            gsync();
         };
 
         // ================================================================ step setup (FP64, once per step)
-        for (int i = n0 + tid; i < n1; i += NT) {
+        for (int i = n0 + gt; i < n1; i += GS) {
             const double2 xi = X[i], vi = Vv[i];
             Xn[i] = xi;
             XD[i] = make_float2(0.f, 0.f);
@@ -407,8 +492,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             S.ncand = 0; S.rebuild = 1; S.gn0 = 0.0; S.beta = 0.0;
             S.motion = 0.0; S.csx = 0.0; S.csy = 0.0;
         }
-        __syncthreads();
-        for (int j = tid; j < nbl; j += NT) {  // half-space distances at x_n
+        gsync();
+        for (int j = gt; j < nbl; j += GS) {  // half-space distances at x_n
             const double2 xb = Xn[d.bnd[sg.bnd0 + j]];
             for (int k = 0; k < n_col; ++k) {
                 const Col c = cols[k];
@@ -416,7 +501,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             }
         }
         if (!scene_ipc) {  // apply_bc_kernel, kernels.py:53-59: x = target
-            for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
+            for (int b = sg.bc0 + gt; b < sg.bc0 + sg.nbc; b += GS) {
                 const int n = d.bc_idx[b];
                 const double2 tg = Tgt[b], xn = Xn[n];
                 XD[n] = make_float2((float)(tg.x - xn.x), (float)(tg.y - xn.y));
@@ -426,7 +511,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         // rigid pieces: step-start centroid c_n (FP64) and the arms x_n - c_n (FP32)
         for (int b = sg.rig0; b < sg.rig0 + sg.nrig; ++b) {
             double c[3] = {0.0, 0.0, 0.0};
-            for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
+            for (int k = sg.rign0 + gt; k < sg.rign0 + sg.nrign; k += GS) {
                 if (d.r_grp[k] != b) continue;
                 const int i = d.r_node[k];
                 const double m = d.mass[i];
@@ -434,17 +519,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 c[0] += m * xi.x; c[1] += m * xi.y; c[2] += m;
             }
             const int ops3[3] = {0, 0, 0};
-            block_reduce<NT, 3>(c, ops3, red);
+            scene_reduce<NT, CS, 3>(c, ops3, red, cres);
             const double cx = c[0] / c[2], cy = c[1] / c[2];
-            for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
+            for (int k = sg.rign0 + gt; k < sg.rign0 + sg.nrign; k += GS) {
                 if (d.r_grp[k] != b) continue;
                 const int i = d.r_node[k];
                 const double2 xi = Xn[i];
                 RARM[i] = make_float2((float)(xi.x - cx), (float)(xi.y - cy));
             }
-            if (tid == 0) { d.r_acc[3 * b] = cx; d.r_acc[3 * b + 1] = cy; d.r_acc[3 * b + 2] = c[2]; }
+            if (tid == 0 && crank == 0) { d.r_acc[3 * b] = cx; d.r_acc[3 * b + 1] = cy; d.r_acc[3 * b + 2] = c[2]; }
         }
-        __syncthreads();
+        gsync();
 
         build_base();
 
@@ -463,43 +548,72 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 ipc_far = S.dmin_c - 2.0 * S.motion >= d.reach;
                 return;
             }
-            __syncthreads();
+            gsync();
             const double2 anchor = xpos(d.bnd[sg.bnd0]);
             for (int j = tid; j < nbl; j += NT) {
                 const int n = d.bnd[sg.bnd0 + j];
                 const double2 xb = xpos(n);
-                DREF[sg.bnd0 + j] = XD[n];
+                if (crank == 0) DREF[sg.bnd0 + j] = XD[n];
                 pos32[j] = make_float2((float)(xb.x - anchor.x), (float)(xb.y - anchor.y));
             }
-            if (tid == 0) S.count = 0;
-            __syncthreads();
             const float rad = (float)(d.reach + d.skin);
             const float slack = 1.0e-5f * rad;
             const long npair = (long)sg.ne * nbl;
             float dmn = 3.0e38f;
-            for (long base = 0; base < npair; base += NT) {
+            // pair q = (edge k, slot j): kept when within reach + skin and not excluded
+            auto pair_keep = [&](long q, int &k, int &j, float &dd) -> bool {
+                k = (int)(q / nbl);
+                j = (int)(q - (long)k * nbl);
+                const int ge = sg.edge0 + k;
+                const int a = d.ea[ge], b = d.eb[ge];
+                const int pn = d.bnd[sg.bnd0 + j];
+                if (pn == a || pn == b) return false;
+                const int la = d.node_bslot[a] - sg.bnd0, lb = d.node_bslot[b] - sg.bnd0;
+                const float2 pa = pos32[la], pb = pos32[lb], pp = pos32[j];
+                const float abx = pb.x - pa.x, aby = pb.y - pa.y;
+                const float wx = pp.x - pa.x, wy = pp.y - pa.y;
+                float t = (wx * abx + wy * aby) / fmaxf(abx * abx + aby * aby, 1e-30f);
+                t = fminf(fmaxf(t, 0.f), 1.f);
+                const float dx = wx - t * abx, dy = wy - t * aby;
+                dd = sqrtf(dx * dx + dy * dy);
+                return dd <= rad + slack && !excluded(d, sg.bnd0 + j, d.ela[ge]) && !excluded(d, sg.bnd0 + j, d.elb[ge]);
+            };
+            // this block's contiguous share of the pair space (all of it for a block per scene):
+            // the list comes out in pair order across the blocks
+            const long chunk = (npair + CS - 1) / CS;
+            const long q0 = CL ? (crank * chunk < npair ? crank * chunk : npair) : 0;
+            const long q1 = CL ? (q0 + chunk < npair ? q0 + chunk : npair) : npair;
+            int base_off = 0, n_all = 0;
+            if constexpr (CL) {  // pass 1: count this block's pairs; offsets from the lower ranks
+                if (tid == 0) s_cnt = 0;
+                __syncthreads();
+                for (long base = q0; base < q1; base += NT) {
+                    const long q = base + tid;
+                    int k, j;
+                    float dd;
+                    const bool keep = q < q1 && pair_keep(q, k, j, dd);
+                    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                    if ((tid & 31) == 0 && bal) atomicAdd(&s_cnt, __popc(bal));
+                }
+                cg::cluster_group cl = cg::this_cluster();
+                cl.sync();
+                for (int r = 0; r < CS; ++r) {
+                    const int c = *cl.map_shared_rank(&s_cnt, r);
+                    if (r < crank) base_off += c;
+                    n_all += c;
+                }
+                cl.sync();
+            }
+            if (tid == 0) S.count = base_off;
+            __syncthreads();
+            for (long base = q0; base < q1; base += NT) {
                 const long q = base + tid;
                 bool keep = false;
                 int k = 0, j = 0;
-                if (q < npair) {
-                    k = (int)(q / nbl);
-                    j = (int)(q - (long)k * nbl);
-                    const int ge = sg.edge0 + k;
-                    const int a = d.ea[ge], b = d.eb[ge];
-                    const int pn = d.bnd[sg.bnd0 + j];
-                    if (pn != a && pn != b) {
-                        const int la = d.node_bslot[a] - sg.bnd0, lb = d.node_bslot[b] - sg.bnd0;
-                        const float2 pa = pos32[la], pb = pos32[lb], pp = pos32[j];
-                        const float abx = pb.x - pa.x, aby = pb.y - pa.y;
-                        const float wx = pp.x - pa.x, wy = pp.y - pa.y;
-                        float t = (wx * abx + wy * aby) / fmaxf(abx * abx + aby * aby, 1e-30f);
-                        t = fminf(fmaxf(t, 0.f), 1.f);
-                        const float dx = wx - t * abx, dy = wy - t * aby;
-                        const float dd = sqrtf(dx * dx + dy * dy);
-                        keep = dd <= rad + slack &&
-                               !excluded(d, sg.bnd0 + j, d.ela[ge]) && !excluded(d, sg.bnd0 + j, d.elb[ge]);
-                        if (keep) dmn = fminf(dmn, dd);
-                    }
+                if (q < q1) {
+                    float dd;
+                    keep = pair_keep(q, k, j, dd);
+                    if (keep) dmn = fminf(dmn, dd);
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, keep);
                 const int lane = tid & 31, warp = tid >> 5;
@@ -517,15 +631,16 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             __syncthreads();
             double vm[1] = {(double)dmn};
             const int opm[1] = {2};
-            block_reduce<NT, 1>(vm, opm, red);
+            scene_reduce<NT, CS, 1>(vm, opm, red, cres);
             if (tid == 0) {
-                if (S.count > sg.ncap) { S.status = D2F_ECAP; S.ncand = sg.ncap; }
-                else S.ncand = S.count;
+                const int cnt = CL ? n_all : S.count;
+                if (cnt > sg.ncap) { S.status = D2F_ECAP; S.ncand = sg.ncap; }
+                else S.ncand = cnt;
                 S.rebuild = 0;
                 S.motion = 0.0;
                 S.dmin_c = vm[0] - 1.0e-4 * (double)rad;  // FP32 rounding of the build distances
             }
-            __syncthreads();
+            gsync();
             ipc_far = S.dmin_c >= d.reach;
         };
 
@@ -544,7 +659,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             const int per_body = d.friction ? d.per_body : 0;
             const double floor_ = d.bc_floor * idhat;
             const int nc = S.ncand;
-            for (int c = tid; c < nc; c += NT) {
+            for (int c = gt; c < nc; c += GS) {
                 const unsigned packed = (unsigned)d.cand[sg.cand0 + c];
                 const int k = (int)(packed >> 16), j = (int)(packed & 0xffffu);
                 const int ge = sg.edge0 + k;
@@ -712,7 +827,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         auto sweep = [&]() {  // kinematic nodes advanced by the step limit, ipc_contact.py:456-463
             ipc_refresh();
             double qi = 0.0;
-            for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
+            for (int b = sg.bc0 + gt; b < sg.bc0 + sg.nbc; b += GS) {
                 const double2 q = kin_dir(d.bc_idx[b]);
                 qi = dmax(qi, sqrt(q.x * q.x + q.y * q.y));
             }
@@ -720,7 +835,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             ipc_pairs(3, dummy, 1.0);
             double v[1] = {qi};
             const int ops[1] = {1};
-            block_reduce<NT, 1>(v, ops, red);
+            scene_reduce<NT, CS, 1>(v, ops, red, cres);
             const double a_tc = tc_scan(1.0);
             if (tid == 0) {
                 double a_s = a_tc;
@@ -729,9 +844,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 S.q_inf = v[0];
                 S.motion += dmin(a_s, 1.0) * v[0];
             }
-            __syncthreads();
+            gsync();
             const double alpha_s = S.alpha_s;
-            for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
+            for (int b = sg.bc0 + gt; b < sg.bc0 + sg.nbc; b += GS) {
                 const int n = d.bc_idx[b];
                 const double2 tg = Tgt[b], x = xpos(n), xn = Xn[n];
                 const double2 nx = alpha_s >= 1.0 ? tg : make_double2(x.x + alpha_s * (tg.x - x.x), x.y + alpha_s * (tg.y - x.y));
@@ -739,13 +854,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 XD[n] = make_float2((float)(nx.x - xn.x), (float)(nx.y - xn.y));
                 XR[n] = make_float2((float)(nx.x - xb.x), (float)(nx.y - xb.y));
             }
-            __syncthreads();
+            gsync();
         };
 
         if (scene_ipc && sg.nbc > 0) {
             sweep();
             if (tid == 0) S.pending = !(S.alpha_s >= 1.0);
-            __syncthreads();
+            gsync();
         }
 
         // ================================================================ PNCG iterations (FP32)
@@ -756,14 +871,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     if (S.q_inf > 0.0) S.active = 1;
                     if (it % 8 == 7) S.pending = !(S.alpha_s >= 1.0);
                 }
-                __syncthreads();
+                gsync();
             }
             if (!S.active && !S.pending) break;
             if (S.status != 0) break;
             if (it > 0 && it % REBASE == 0) build_base();
 
             // ---------------------------------------------- A1: triangles (gradient + diagonal)
-            for (int t = t0 + tid; t < t1; t += NT) {
+            for (int t = t0 + gt; t < t1; t += GS) {
                 const int i0 = __ldg(d.tri + 3 * t), i1 = __ldg(d.tri + 3 * t + 1), i2 = __ldg(d.tri + 3 * t + 2);
                 const float4 B = Bm[t], du = DU0[t];
                 const float A = Ar[t], mu = Mu[t], la = La[t];
@@ -822,10 +937,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 atomicAdd(GD + i1, make_float4(g1x, g1y, d1x_, d1y_));
                 atomicAdd(GD + i2, make_float4(g2x, g2y, d2x_, d2y_));
             }
-            __syncthreads();
+            gsync();
 
             // ---------------------------------------------- A2: nodes (gather, colliders, friction, force)
-            for (int i = n0 + tid; i < n1; i += NT) {
+            for (int i = n0 + gt; i < n1; i += GS) {
                 Gp[i] = G[i];
                 const float2 dx_ = XD[i];
                 const float4 hvm = HVM[i];
@@ -901,17 +1016,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 G[i] = make_float2(g0.x + (g0.z + gx), g0.y + (g0.w + gy));
                 D[i] = make_float2(dxx, dyy);
             }
-            __syncthreads();
+            gsync();
 
             // ---------------------------------------------- A3: contact between bodies, tendons (FP64)
             if (scene_ipc) {
                 ipc_refresh();
                 double z0 = 0.0;
                 ipc_pairs(0, z0, 0.0);
-                __syncthreads();
+                gsync();
             }
             if (sg.nten > 0) {
-                for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
+                for (int k = sg.ten0 + gt; k < sg.ten0 + sg.nten; k += GS) {
                     double L = 0.0;
                     for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
                         if (d.t_tid[j] != k) continue;
@@ -932,8 +1047,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     double *ts = d.t_state + 4 * k;
                     ts[0] = L; ts[2] = tau; ts[3] = keff;
                 }
-                __syncthreads();
-                for (int j = sg.tent0 + tid; j < sg.tent0 + sg.ntent; j += NT) {
+                gsync();
+                for (int j = sg.tent0 + gt; j < sg.tent0 + sg.ntent; j += GS) {
                     const int n = d.t_node[j], k = d.t_tid[j];
                     const double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3];
                     double gLx = 0, gLy = 0, geox = 0, geoy = 0;
@@ -962,7 +1077,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     atomicAdd(dp_, (float)(h2 * (tau * geox + keff * gLx * gLx)));
                     atomicAdd(dp_ + 1, (float)(h2 * (tau * geoy + keff * gLy * gLy)));
                 }
-                __syncthreads();
+                gsync();
             }
 
             // ---------------------------------------------- A4: body-level modes
@@ -970,7 +1085,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 double v[18];
 #pragma unroll
                 for (int q = 0; q < 18; ++q) v[q] = 0.0;
-                for (int k = sg.affn0 + tid; k < sg.affn0 + sg.naffn; k += NT) {
+                for (int k = sg.affn0 + gt; k < sg.affn0 + sg.naffn; k += GS) {
                     if (d.a_grp[k] != b) continue;
                     const int i = d.a_node[k];
                     const double *w = d.a_w + 3 * k;
@@ -983,8 +1098,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     for (int q = 0; q < 6; ++q) { v[6 + q] += dx * o[q]; v[12 + q] += dy * o[q]; }
                 }
                 const int ops[18] = {0};
-                block_reduce<NT, 18>(v, ops, red);
-                if (tid == 0) {
+                scene_reduce<NT, CS, 18>(v, ops, red, cres);
+                if (tid == 0 && crank == 0) {
                     for (int q = 0; q < 6; ++q) {
                         d.a_gq_prev[6 * b + q] = d.a_gq[6 * b + q];
                         d.a_gq[6 * b + q] = v[q];
@@ -993,8 +1108,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 }
             }
             if (sg.naff > 0) {
-                __syncthreads();
-                for (int k = sg.affn0 + tid; k < sg.affn0 + sg.naffn; k += NT) G[d.a_node[k]] = make_float2(0.f, 0.f);
+                gsync();
+                for (int k = sg.affn0 + gt; k < sg.affn0 + sg.naffn; k += GS) G[d.a_node[k]] = make_float2(0.f, 0.f);
             }
             if (tid == 0) { S.gPg = 0.0; S.g_Py = 0.0; S.y_Py = 0.0; }
             // one rigid piece (a free soft body): its gather is folded into the Dai-Kou pass below;
@@ -1004,7 +1119,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int lb = b - sg.rig0;
                 // centroid shift since the step began: sum m dx / M
                 FF cs2[2] = {{0.f, 0.f}, {0.f, 0.f}};
-                for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
+                for (int k = sg.rign0 + gt; k < sg.rign0 + sg.nrign; k += GS) {
                     if (d.r_grp[k] != b) continue;
                     const int i = d.r_node[k];
                     const float m = HVM[i].z;
@@ -1016,13 +1131,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int nmo[1] = {1};
                 double so[2];
                 float mo_[1];
-                block_reduce_mx<NT, 2, 1>(cs2, nm, nmo, so, mo_, fred, dres, mres);
+                scene_reduce_mx<NT, CS, 2, 1>(cs2, nm, nmo, so, mo_, fred, dres, mres, cres, cmres);
                 const double Mtot = d.r_acc[3 * b + 2];
                 const float csx = (float)(so[0] / Mtot), csy = (float)(so[1] / Mtot);
                 FF v[11];
 #pragma unroll
                 for (int q = 0; q < 11; ++q) v[q] = FF{0.f, 0.f};
-                for (int k = sg.rign0 + tid; k < sg.rign0 + sg.nrign; k += NT) {
+                for (int k = sg.rign0 + gt; k < sg.rign0 + sg.nrign; k += GS) {
                     if (d.r_grp[k] != b) continue;
                     const int i = d.r_node[k];
                     const float2 a0 = RARM[i], u = XD[i];
@@ -1036,7 +1151,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     ff_add(v[10], dx * ry * ry + dy * rx * rx);
                 }
                 double vs[11];
-                block_reduce_mx<NT, 11, 1>(v, nm, nmo, vs, mo_, fred, dres, mres);
+                scene_reduce_mx<NT, CS, 11, 1>(v, nm, nmo, vs, mo_, fred, dres, mres, cres, cmres);
                 if (tid == 0) {
                     const double a[9] = {vs[6], 0.0, vs[7], 0.0, vs[8], vs[9], vs[7], vs[9], vs[10]};
                     const double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[6] * a[5]) +
@@ -1066,13 +1181,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     S.g_Py += g[0] * zy[0] + g[1] * zy[1] + g[2] * zy[2];
                     S.y_Py += y[0] * zy[0] + y[1] * zy[1] + y[2] * zy[2];
                 }
-                __syncthreads();
+                gsync();
             }
 
             // ---------------------------------------------- B1: mask + Dai-Kou dot products
             // (+ the single rigid piece's B^T g, B^T g_prev, B^T D' B, affine.py:421-453)
             auto b2 = [&](const double *vs) {
-                if (tid == 0) {  // B2: per-scene scalars, FP64
+                if (tid == 0 && crank == 0) {  // B2: per-scene scalars, FP64
                     double gPg = vs[0] + S.gPg, g_p = vs[1], g_Py = vs[2] + S.g_Py, y_p = vs[3], y_Py = vs[4] + S.y_Py;
                     for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b) {  // affine_reduce_kernel, affine.py:178-205
                         double *q = d.a_q + 6 * b;
@@ -1106,7 +1221,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
                         for (int r = 0; r < 6; ++r) d.a_pq[6 * b + r] = -d.a_zq[6 * b + r] + bta * d.a_pq[6 * b + r];
                 }
-                __syncthreads();
+                gsync();
+                if constexpr (CL) {  // the other blocks take rank 0's scalars
+                    if (tid == 0 && crank != 0) {
+                        const SceneSh *s0 = cg::this_cluster().map_shared_rank(&S, 0);
+                        S.beta = s0->beta; S.gTp = s0->gTp; S.gn2 = s0->gn2;
+                    }
+                    __syncthreads();
+                }
             };
             auto b1 = [&](auto rig_tag) {
                 // the five Dai-Kou dots and |g|^2 as compensated sums; the rigid piece's
@@ -1121,7 +1243,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
 #pragma unroll
                 for (int q = 0; q < NM; ++q) { r[q] = 0.f; rops[q] = q == 0 ? 1 : 0; }
                 const float csx = (float)S.csx, csy = (float)S.csy;
-                for (int i = n0 + tid; i < n1; i += NT) {
+                for (int i = n0 + gt; i < n1; i += GS) {
                     const int inf = NINFO[i].x, fm = inf & 3;
                     float2 g = G[i];
                     const float2 dg = D[i], gp = Gp[i], pp = P[i];
@@ -1153,7 +1275,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 }
                 double vs[NS];
                 float mo_[NM];
-                block_reduce_mx<NT, NS, NM>(v, r, rops, vs, mo_, fred, dres, mres);
+                scene_reduce_mx<NT, CS, NS, NM>(v, r, rops, vs, mo_, fred, dres, mres, cres, cmres);
                 if constexpr (RIG) {
                     if (tid == 0) {  // rigid_reduce_kernel, affine.py:456-473 (FP64)
                         const int b = sg.rig0;
@@ -1195,7 +1317,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             float acc_pinf = 0.f, acc_clr = 1.0e30f, acc_alpha = (float)d.alpha_max;
             {
                 const float bta = (float)S.beta;
-                for (int i = n0 + tid; i < n1; i += NT) {
+                for (int i = n0 + gt; i < n1; i += GS) {
                     const int2 inf = NINFO[i];
                     const int fm = inf.x & 3;
                     const float2 dx_ = XD[i];
@@ -1313,12 +1435,12 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     }
                 }
             }
-            __syncthreads();
+            gsync();
 
             // ---------------------------------------------- B4: triangles (curvature + inversion cap)
             {
                 const float shrink = (float)d.area_shrink;
-                for (int t = t0 + tid; t < t1; t += NT) {
+                for (int t = t0 + gt; t < t1; t += GS) {
                     const int i0 = __ldg(d.tri + 3 * t), i1 = __ldg(d.tri + 3 * t + 1), i2 = __ldg(d.tri + 3 * t + 2);
                     const float2 p0 = P[i0], p1 = P[i1], p2 = P[i2];
                     const float2 u0 = XR[i0], u1 = XR[i1], u2 = XR[i2];
@@ -1368,13 +1490,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     }
                 }
                 if (scene_rare) {
-                    for (int b = sg.aff0 + tid; b < sg.aff0 + sg.naff; b += NT) {  // affine_pHp_kernel
+                    for (int b = sg.aff0 + gt; b < sg.aff0 + sg.naff; b += GS) {  // affine_pHp_kernel
                         const double *q = d.a_q + 6 * b, *pq = d.a_pq + 6 * b;
                         const M2 dA{pq[1], pq[2], pq[4], pq[5]}, A{q[1], q[2], q[4], q[5]};
                         acc_rare += h2 * dmax(ddot2(dA, nh_d2(A, dA, d.a_Mu[b], d.a_La[b])), 0.0);
                     }
                     if (scene_ipc) ipc_pairs(1, acc_rare, d.alpha_max);
-                    for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {  // Tendon.pHp
+                    for (int k = sg.ten0 + gt; k < sg.ten0 + sg.nten; k += GS) {  // Tendon.pHp
                         const double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3];
                         double dL = 0.0;
                         for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
@@ -1405,7 +1527,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int mops[3] = {1, 2, 2};
                 double so[3];
                 float mo[3];
-                block_reduce_mx<NT, 3, 3>(sv, mv, mops, so, mo, fred, dres, mres);
+                scene_reduce_mx<NT, CS, 3, 3>(sv, mv, mops, so, mo, fred, dres, mres, cres, cmres);
                 const double a_ccd = scene_ipc ? tc_scan(d.alpha_max) : 0.0;
                 // ---------------------------------------------- B5: step length and convergence (FP64)
                 if (tid == 0) {
@@ -1441,8 +1563,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         }
                     }
                     if (S.active) {
-                        for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
-                            for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
+                        if (crank == 0)
+                            for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
+                                for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
                         S.motion += S.alpha * pinf;              // bound on any node's move
                         if (rig1) {                              // centroid shift, sum m dx / M
                             const double Mt = d.r_acc[3 * sg.rig0 + 2];
@@ -1451,14 +1574,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         }
                     }
                 }
-                __syncthreads();
+                gsync();
             }
 
             // ---------------------------------------------- D1: r += alpha p, dx = (x_b - x_n) + r (slaved nodes: J q)
             {
                 const bool act = S.active != 0;
                 const float al = (float)S.alpha;
-                for (int i = n0 + tid; i < n1; i += NT) {
+                for (int i = n0 + gt; i < n1; i += GS) {
                     if (NINFO[i].x & NI_AFF) {
                         const int ka = d.node_aff[i];
                         const double *w = d.a_w + 3 * ka, *q = d.a_q + 6 * d.a_grp[ka];
@@ -1474,23 +1597,23 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         XD[i] = make_float2(db.x + rn.x, db.y + rn.y);
                     }
                 }
-                __syncthreads();
+                gsync();
             }
         }
 
         // ================================================================ commit (FP64)
-        for (int i = n0 + tid; i < n1; i += NT) {
+        for (int i = n0 + gt; i < n1; i += GS) {
             const double2 xn = Xn[i];
             const double2 xi = xpos(i);
             X[i] = xi;
             Vv[i] = make_double2((xi.x - xn.x) * inv_dt, (xi.y - xn.y) * inv_dt);
         }
-        if (tid == 0) {
+        if (tid == 0 && crank == 0) {
             d.iters[sc] = S.iters;
             d.active[sc] = S.active;
             d.status[sc] = S.status;
         }
-        __syncthreads();
+        gsync();
     }
 }
 

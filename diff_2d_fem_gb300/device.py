@@ -38,9 +38,11 @@ def _ranges(ids, B):
 
 class DeviceSolver:
     """Binds a problem to device memory and a libd2f handle. `precision`: "fp64" or
-    "mixed". threads / blocks_per_sm: the scene-block launch shape (0 = library default)."""
+    "mixed". threads / blocks_per_sm: the scene-block launch shape (0 = library default).
+    blocks_per_scene (mixed): blocks of one cluster per scene, 1, 8 or 16 (0 = library default)."""
 
-    def __init__(self, prob, precision="fp64", threads=0, blocks_per_sm=0, device="cuda", stream=None):
+    def __init__(self, prob, precision="fp64", threads=0, blocks_per_sm=0, device="cuda", stream=None,
+                 blocks_per_scene=0):
         if torch is None:
             raise RuntimeError("PyTorch is required for device buffers")
         if not torch.cuda.is_available():
@@ -289,6 +291,7 @@ class DeviceSolver:
             d.per_body = int(ipc.get("per_body", 0)) if ipc.get("mu_node") is not None else 0
         d.threads = int(threads or 0)
         d.blocks_per_sm = int(blocks_per_sm or 0)
+        d.blocks_per_scene = int(blocks_per_scene or 0)
         if int(sc.get("line_search", 0)):
             if self.mixed:
                 raise NotImplementedError("the energy line search runs in FP64 only (precision='fp64')")
@@ -371,6 +374,12 @@ class DeviceSolver:
         _lib.check(self.L.d2f_stats(self.h, self._stream_ptr(), it.ctypes.data, ac.ctypes.data, st.ctypes.data),
                    "d2f_stats")
         return it, ac, st
+
+    def launch_shape(self):
+        """(blocks launched, threads per block, blocks per scene) of this solver's step."""
+        b, t, c = C.c_int32(), C.c_int32(), C.c_int32()
+        _lib.check(self.L.d2f_launch_shape(self.h, C.byref(b), C.byref(t), C.byref(c)), "d2f_launch_shape")
+        return b.value, t.value, c.value
 
     def set_nodes(self, nodes, x=None, v=None, xn=False):
         idx = torch.as_tensor(np.asarray(nodes, np.int64), device=self.dev)

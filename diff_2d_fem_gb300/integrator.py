@@ -13,6 +13,8 @@ New keyword-only options, all off by default:
   gtol        stop an environment once its gradient norm falls below gtol x the norm at
               the step's first iteration (in addition to the reference's tests).
   threads, blocks_per_sm   launch shape of the per-scene kernel (0 = tuned default).
+  blocks_per_scene         mixed precision: a cluster of 8 or 16 blocks per scene for large
+                           scenes (0 = library default, 1 = a block per scene).
 """
 from __future__ import annotations
 
@@ -39,7 +41,7 @@ class ImplicitIntegrator:
                  self_radius=None, tol_x=0.0, conv_check=8,
                  line_search=False, n_backtrack=4, ls_tol=1e-7, rigid_modes=True,
                  iters_per_cfl=2.0, max_iter_cap=2000, cg_restart=None, *,
-                 precision=None, gtol=0.0, threads=0, blocks_per_sm=0):
+                 precision=None, gtol=0.0, threads=0, blocks_per_sm=0, blocks_per_scene=0):
         self.precision = _default_precision() if precision is None else str(precision)
         if self.precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
@@ -64,6 +66,7 @@ class ImplicitIntegrator:
         self.gtol = float(gtol)
         self.threads = int(threads)
         self.blocks_per_sm = int(blocks_per_sm)
+        self.blocks_per_scene = int(blocks_per_scene)
 
     # ---- the step (implicit/integrator.py:81-86)
     def simulate(self, model, dt, control=None):
@@ -143,7 +146,8 @@ class ImplicitIntegrator:
                               f"will converge very slowly or not at all. Leave rigid_modes on.",
                               stacklevel=3)
         s = DeviceSolver(prob, precision=self.precision, threads=self.threads,
-                         blocks_per_sm=self.blocks_per_sm, device=model.device)
+                         blocks_per_sm=self.blocks_per_sm, device=model.device,
+                         blocks_per_scene=self.blocks_per_scene)
         s.dt = float(dt)
         s.iter_max = int(prob["iter_max"])
         s._act_version = model._act_version

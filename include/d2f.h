@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define D2F_ABI_VERSION 2
+#define D2F_ABI_VERSION 3
 
 /* status codes */
 #define D2F_OK 0
@@ -133,6 +133,11 @@ typedef struct d2f_scene_desc {
     double ls_tol;               /* accept while E <= E0 + ls_tol (|E0| + 1) */
     int32_t line_search;         /* 0 off, 1 on */
     int32_t n_backtrack;         /* halvings tried per iteration */
+    int32_t blocks_per_scene;    /* mixed precision: thread blocks working on one scene, as one
+                                    cluster of 256-thread blocks: 1, 8 or 16 (0: a cluster of 16
+                                    or 8, whichever finishes the batch first, when the batch has
+                                    fewer scenes than SMs and at least 16384 nodes per scene;
+                                    else 1) */
 } d2f_scene_desc;
 
 typedef struct d2f_solver d2f_solver;
@@ -174,6 +179,10 @@ size_t d2f_mixed_scratch_bytes(int32_t N, int32_t T, int32_t Nb, int32_t n_col, 
 
 /* Number of kernels d2f_step launches per call (for launch accounting). */
 int32_t d2f_kernels_per_step(const d2f_solver *s);
+
+/* The launch shape d2f_step uses: blocks launched, threads per block, blocks per scene (1: a
+ * block per scene; 8 or 16: one cluster per scene). Null outputs are skipped. */
+int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads, int32_t *blocks_per_scene);
 
 /* Size of the library's static device scratch used by d2f_step_noalloc (16 MiB). */
 #define D2F_NOALLOC_SCRATCH_BYTES (16u << 20)
