@@ -13,7 +13,7 @@ _I = C.c_int32
 _D = C.c_double
 _P = C.c_void_p
 
-D2F_ABI_VERSION = 3
+D2F_ABI_VERSION = 4
 D2F_FP64, D2F_MIXED = 0, 1
 ERRORS = {0: "ok", -1: "D2F_EINVAL", -2: "D2F_ECUDA", -3: "D2F_ECAP", -4: "D2F_ENAN"}
 
@@ -40,7 +40,8 @@ DESC_FIELDS = (
                          "area_shrink", "ccd_eta", "cg_guard", "gtol", "ipc_mu", "ipc_dhat", "ipc_kappa",
                          "reach", "gap", "bc_floor", "skin")]
     + [(n, _I) for n in ("iter_max", "conv_check", "friction", "per_body", "threads", "blocks_per_sm")]
-    + [("ls_tol", _D), ("line_search", _I), ("n_backtrack", _I), ("blocks_per_scene", _I)]
+    + [("ls_tol", _D), ("line_search", _I), ("n_backtrack", _I), ("blocks_per_scene", _I),
+       ("a_ptr", _P)]
 )
 
 

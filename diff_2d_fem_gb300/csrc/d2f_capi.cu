@@ -79,7 +79,7 @@ static int validate(const d2f_scene_desc &d, bool scratch) {
         return fail(D2F_EINVAL, "d2f: max_nb must be in 1..24576 with IPC contact");
     if (d.n_rig > 0 && (!d.diag_el || !d.r_node || !d.r_grp || !d.r_acc || !d.r_zq))
         return fail(D2F_EINVAL, "d2f: rigid-mode arrays missing");
-    if (d.n_aff > 0 && (!d.a_node || !d.a_grp || !d.a_w || !d.a_Mu || !d.a_La || !d.a_q || !d.a_pq ||
+    if (d.n_aff > 0 && (!d.a_node || !d.a_grp || !d.a_ptr || !d.a_w || !d.a_Mu || !d.a_La || !d.a_q || !d.a_pq ||
                         !d.a_gq || !d.a_gq_prev || !d.a_zq || !d.a_H))
         return fail(D2F_EINVAL, "d2f: affine arrays missing");
     if (d.n_ten > 0 && (!d.t_node || !d.t_prv || !d.t_nxt || !d.t_tid || !d.t_stiff || !d.t_L0 ||

@@ -174,7 +174,7 @@ __device__ __forceinline__ void scene_reduce_mx(FF (&s)[NS], float (&m)[NM], con
 
 // Byte layout of the mixed path's per-step scratch (d2f_scene_desc.mscr), 256-aligned parts.
 struct MixedLayout {
-    size_t xd, hvm, g0, gd, xbd, xr, db, rarm, ninfo, du0, phi0, rcs, dref, total;
+    size_t xd, hvm, g0, gd, xbd, xr, db, rarm, ninfo, du0, phi0, rcs, pb, total;
 };
 __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, long n_col, long n_rig) {
     auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -192,7 +192,7 @@ __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, lon
     L.du0 = o; o = up(o + (size_t)T * 16);
     L.phi0 = o; o = up(o + (size_t)N * (n_col > 0 ? n_col : 1) * 4);
     L.rcs = o; o = up(o + (size_t)(n_rig > 0 ? n_rig : 1) * 8);
-    L.dref = o; o = up(o + (size_t)(Nb > 0 ? Nb : 1) * 8);
+    L.pb = o; o = up(o + (size_t)(Nb > 0 ? Nb : 1) * 8);
     L.total = o;
     return L;
 }
@@ -220,11 +220,17 @@ __device__ __forceinline__ double2 tendon_dlen(PosF pos, const int32_t *t_node, 
 constexpr int REBASE = 64;
 // packed per-node flags (NINFO.x): bits 0-1 free mask, then these, bits 4-7 the rigid piece
 constexpr int NI_AFF = 4, NI_RIG = 8;
+// contact candidate lists of scenes with at least HASH_MIN_NB boundary nodes are built through
+// a spatial hash of HASH_B buckets (every other scene tests all edge-node pairs)
+constexpr int HASH_MIN_NB = 4096, HASH_B = 4096;
+// the hash (HASH_B bucket ends + the slots, 4 bytes each) reuses the 8 bytes per boundary node
+// of dynamic shared memory the exhaustive build holds its positions in
+static_assert(HASH_MIN_NB >= HASH_B, "hash tables must fit the boundary-position buffer");
 
 // ---------------------------------------------------------------------- the kernel
 // Device pointers of the per-step scratch parts (host-computed from d2f_scene_desc.mscr).
 struct MixedPtrs {
-    float2 *xd, *rarm, *xr, *db, *dref, *rcs;
+    float2 *xd, *rarm, *xr, *db, *pb, *rcs;
     float4 *hvm, *g0, *gd, *du0;
     double2 *g0d, *xbd;
     int2 *ninfo;
@@ -238,7 +244,7 @@ inline MixedPtrs mixed_ptrs(const d2f_scene_desc &d) {
     p.rarm = reinterpret_cast<float2 *>(ms + L.rarm);
     p.xr = reinterpret_cast<float2 *>(ms + L.xr);
     p.db = reinterpret_cast<float2 *>(ms + L.db);
-    p.dref = reinterpret_cast<float2 *>(ms + L.dref);
+    p.pb = reinterpret_cast<float2 *>(ms + L.pb);
     p.rcs = reinterpret_cast<float2 *>(ms + L.rcs);
     p.hvm = reinterpret_cast<float4 *>(ms + L.hvm);
     p.g0 = reinterpret_cast<float4 *>(ms + L.g0);
@@ -274,7 +280,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     __shared__ float cmres[16];
     __shared__ int s_wcnt[NW];
     __shared__ unsigned s_wmask[NW];
-    __shared__ double s_H6[6][6], s_L6[6][6];
     __shared__ double colmu[MAX_COL];
     __shared__ float s_zf[8][3], s_cs[8][2];  // rigid-mode correction of up to 8 pieces, FP32
     __shared__ float colf[MAX_COL][2], colmuf[MAX_COL];  // half-space normals, friction (FP32)
@@ -324,7 +329,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     float2 *__restrict__ XR = mp.xr;       // x - x_b
     float2 *__restrict__ DB = mp.db;       // x_b - x_n
     float *__restrict__ PHI0 = mp.phi0;    // half-space distances at x_n, per node
-    float2 *__restrict__ DREF = mp.dref;   // dx when the candidate list was built
+    float2 *__restrict__ PB = mp.pb;       // boundary positions at the list build (hashed scenes)
     float2 *__restrict__ RCS = mp.rcs;     // rigid pieces: centroid shift
 
     if (tid < n_col && tid < MAX_COL) {
@@ -549,27 +554,27 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 return;
             }
             gsync();
+            // boundary positions in FP32 relative to the first boundary node: in shared memory
+            // (every block its own copy), or for hashed scenes in PB, written once per scene
+            const bool hashed = nbl >= HASH_MIN_NB;
+            float2 *P32 = hashed ? PB + sg.bnd0 : pos32;
             const double2 anchor = xpos(d.bnd[sg.bnd0]);
-            for (int j = tid; j < nbl; j += NT) {
-                const int n = d.bnd[sg.bnd0 + j];
-                const double2 xb = xpos(n);
-                if (crank == 0) DREF[sg.bnd0 + j] = XD[n];
-                pos32[j] = make_float2((float)(xb.x - anchor.x), (float)(xb.y - anchor.y));
+            for (int j = hashed ? gt : tid; j < nbl; j += hashed ? GS : NT) {
+                const double2 xb = xpos(d.bnd[sg.bnd0 + j]);
+                P32[j] = make_float2((float)(xb.x - anchor.x), (float)(xb.y - anchor.y));
             }
+            if (hashed) gsync();
             const float rad = (float)(d.reach + d.skin);
             const float slack = 1.0e-5f * rad;
-            const long npair = (long)sg.ne * nbl;
             float dmn = 3.0e38f;
-            // pair q = (edge k, slot j): kept when within reach + skin and not excluded
-            auto pair_keep = [&](long q, int &k, int &j, float &dd) -> bool {
-                k = (int)(q / nbl);
-                j = (int)(q - (long)k * nbl);
+            // edge k, slot j: a candidate when within reach + skin and not excluded
+            auto pair_keep = [&](int k, int j, float &dd) -> bool {
                 const int ge = sg.edge0 + k;
                 const int a = d.ea[ge], b = d.eb[ge];
                 const int pn = d.bnd[sg.bnd0 + j];
                 if (pn == a || pn == b) return false;
                 const int la = d.node_bslot[a] - sg.bnd0, lb = d.node_bslot[b] - sg.bnd0;
-                const float2 pa = pos32[la], pb = pos32[lb], pp = pos32[j];
+                const float2 pa = P32[la], pb = P32[lb], pp = P32[j];
                 const float abx = pb.x - pa.x, aby = pb.y - pa.y;
                 const float wx = pp.x - pa.x, wy = pp.y - pa.y;
                 float t = (wx * abx + wy * aby) / fmaxf(abx * abx + aby * aby, 1e-30f);
@@ -578,55 +583,182 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 dd = sqrtf(dx * dx + dy * dy);
                 return dd <= rad + slack && !excluded(d, sg.bnd0 + j, d.ela[ge]) && !excluded(d, sg.bnd0 + j, d.elb[ge]);
             };
-            // this block's contiguous share of the pair space (all of it for a block per scene):
-            // the list comes out in pair order across the blocks
-            const long chunk = (npair + CS - 1) / CS;
-            const long q0 = CL ? (crank * chunk < npair ? crank * chunk : npair) : 0;
-            const long q1 = CL ? (q0 + chunk < npair ? q0 + chunk : npair) : npair;
             int base_off = 0, n_all = 0;
-            if constexpr (CL) {  // pass 1: count this block's pairs; offsets from the lower ranks
-                if (tid == 0) s_cnt = 0;
+            // the blocks of a cluster: their kept-pair counts, then each block's offset (the
+            // lower ranks' pairs) and the scene's total; the list comes out in pair order
+            auto cluster_offsets = [&](int mine) {
+                if constexpr (CL) {
+                    if (tid == 0) s_cnt = 0;
+                    __syncthreads();
+                    if ((tid & 31) == 0 && mine) atomicAdd(&s_cnt, mine);
+                    cg::cluster_group cl = cg::this_cluster();
+                    cl.sync();
+                    for (int r = 0; r < CS; ++r) {
+                        const int c = *cl.map_shared_rank(&s_cnt, r);
+                        if (r < crank) base_off += c;
+                        n_all += c;
+                    }
+                    cl.sync();
+                }
+            };
+            if (hashed) {
+                // counting sort of the slots by the hash of their cell (cells of rad + 2 slack),
+                // every block its own table in shared memory: bucket ends, then the slots
+                unsigned *hend = reinterpret_cast<unsigned *>(pos32);
+                int *hslot = reinterpret_cast<int *>(pos32) + HASH_B;
+                const float R = rad + 2.0f * slack, icell = 1.0f / R;
+                auto cell_of = [&](float v) -> int { return (int)floorf(v * icell); };
+                auto bucket = [&](int cx, int cy) -> int {
+                    return (int)(((unsigned)cx * 73856093u ^ (unsigned)cy * 19349663u) & (unsigned)(HASH_B - 1));
+                };
+                for (int h = tid; h < HASH_B; h += NT) hend[h] = 0u;
+                __syncthreads();
+                for (int j = tid; j < nbl; j += NT) {
+                    const float2 p = P32[j];
+                    atomicAdd(&hend[bucket(cell_of(p.x), cell_of(p.y))], 1u);
+                }
+                __syncthreads();
+                {  // exclusive scan of the counts: NT consecutive buckets per pass
+                    unsigned carry = 0;
+                    for (int base = 0; base < HASH_B; base += NT) {
+                        const int h = base + tid;
+                        const unsigned c = h < HASH_B ? hend[h] : 0u;
+                        unsigned incl = c;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+                            if ((tid & 31) >= o) incl += u;
+                        }
+                        if ((tid & 31) == 31) s_wcnt[tid >> 5] = (int)incl;
+                        __syncthreads();
+                        unsigned before = carry, tot = 0;
+                        for (int w = 0; w < NW; ++w) {
+                            if (w < (tid >> 5)) before += (unsigned)s_wcnt[w];
+                            tot += (unsigned)s_wcnt[w];
+                        }
+                        if (h < HASH_B) hend[h] = before + incl - c;  // the bucket's start
+                        carry += tot;
+                        __syncthreads();
+                    }
+                }
+                for (int j = tid; j < nbl; j += NT) {  // the starts advance to the ends
+                    const float2 p = P32[j];
+                    hslot[atomicAdd(&hend[bucket(cell_of(p.x), cell_of(p.y))], 1u)] = j;
+                }
+                __syncthreads();
+                // edge k's candidates: the slots in the buckets of the cells its box (grown by
+                // R) covers, each bucket once; all slots for an edge longer than that allows
+                auto walk = [&](int k, bool wr, int off) -> int {
+                    const int ge = sg.edge0 + k;
+                    const float2 pa = P32[d.node_bslot[d.ea[ge]] - sg.bnd0], pb = P32[d.node_bslot[d.eb[ge]] - sg.bnd0];
+                    const int cx0 = cell_of(fminf(pa.x, pb.x) - R), cx1 = cell_of(fmaxf(pa.x, pb.x) + R);
+                    const int cy0 = cell_of(fminf(pa.y, pb.y) - R), cy1 = cell_of(fmaxf(pa.y, pb.y) + R);
+                    int n = 0;
+                    auto take = [&](int j) {
+                        float dd;
+                        if (!pair_keep(k, j, dd)) return;
+                        dmn = fminf(dmn, dd);
+                        if (wr && off + n < sg.ncap) d.cand[sg.cand0 + off + n] = (int)(((unsigned)k << 16) | (unsigned)j);
+                        ++n;
+                    };
+                    // (non-finite positions give saturated cells: a huge box, so every slot)
+                    const long ncell = ((long)cx1 - (long)cx0 + 1) * ((long)cy1 - (long)cy0 + 1);
+                    if (cx1 < cx0 || cy1 < cy0 || ncell > 16) {
+                        for (int j = 0; j < nbl; ++j) take(j);
+                        return n;
+                    }
+                    for (int cy = cy0; cy <= cy1; ++cy) {
+                        for (int cx = cx0; cx <= cx1; ++cx) {
+                            const int h = bucket(cx, cy);
+                            bool seen = false;  // the same bucket from an earlier cell of this box
+                            for (int cy2 = cy0; cy2 <= cy && !seen; ++cy2)
+                                for (int cx2 = cx0; cx2 <= cx1; ++cx2) {
+                                    if (cy2 == cy && cx2 >= cx) break;
+                                    if (bucket(cx2, cy2) == h) { seen = true; break; }
+                                }
+                            if (seen) continue;
+                            const int s1 = (int)hend[h], s0 = h > 0 ? (int)hend[h - 1] : 0;
+                            for (int q = s0; q < s1; ++q) take(hslot[q]);
+                        }
+                    }
+                    return n;
+                };
+                // this block's contiguous share of the edges (all of them for a block per scene)
+                const int echunk = (sg.ne + CS - 1) / CS;
+                const int e0 = CL ? min(crank * echunk, sg.ne) : 0;
+                const int e1 = CL ? min(e0 + echunk, sg.ne) : sg.ne;
+                if constexpr (CL) {  // pass 1: count
+                    int mine = 0;
+                    for (int k = e0 + tid; k < e1; k += NT) mine += walk(k, false, 0);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, o);
+                    cluster_offsets(mine);
+                }
+                if (tid == 0) S.count = base_off;
+                __syncthreads();
+                for (int base = e0; base < e1; base += NT) {  // pass 2: count, place, write
+                    const int k = base + tid;
+                    const int c = k < e1 ? walk(k, false, 0) : 0;
+                    int incl = c;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                        if ((tid & 31) >= o) incl += u;
+                    }
+                    if ((tid & 31) == 31) s_wcnt[tid >> 5] = incl;
+                    __syncthreads();
+                    int off = S.count + incl - c, tot = 0;
+                    for (int w = 0; w < NW; ++w) {
+                        if (w < (tid >> 5)) off += s_wcnt[w];
+                        tot += s_wcnt[w];
+                    }
+                    if (c > 0) walk(k, true, off);
+                    __syncthreads();
+                    if (tid == 0) S.count += tot;
+                }
+            } else {
+                const long npair = (long)sg.ne * nbl;
+                // this block's contiguous share of the pair space (all of it for a block per scene)
+                const long chunk = (npair + CS - 1) / CS;
+                const long q0 = CL ? (crank * chunk < npair ? crank * chunk : npair) : 0;
+                const long q1 = CL ? (q0 + chunk < npair ? q0 + chunk : npair) : npair;
+                __syncthreads();  // pos32 complete
+                if constexpr (CL) {  // pass 1: count
+                    int mine = 0;
+                    for (long base = q0; base < q1; base += NT) {
+                        const long q = base + tid;
+                        float dd;
+                        const bool keep = q < q1 && pair_keep((int)(q / nbl), (int)(q % nbl), dd);
+                        mine += __popc(__ballot_sync(0xffffffffu, keep));
+                    }
+                    cluster_offsets((tid & 31) == 0 ? mine : 0);
+                }
+                if (tid == 0) S.count = base_off;
                 __syncthreads();
                 for (long base = q0; base < q1; base += NT) {
                     const long q = base + tid;
-                    int k, j;
-                    float dd;
-                    const bool keep = q < q1 && pair_keep(q, k, j, dd);
+                    bool keep = false;
+                    int k = 0, j = 0;
+                    if (q < q1) {
+                        k = (int)(q / nbl);
+                        j = (int)(q - (long)k * nbl);
+                        float dd;
+                        keep = pair_keep(k, j, dd);
+                        if (keep) dmn = fminf(dmn, dd);
+                    }
                     const unsigned bal = __ballot_sync(0xffffffffu, keep);
-                    if ((tid & 31) == 0 && bal) atomicAdd(&s_cnt, __popc(bal));
+                    const int lane = tid & 31, warp = tid >> 5;
+                    if (lane == 0) s_wcnt[warp] = __popc(bal);
+                    __syncthreads();
+                    int off = S.count + __popc(bal & ((1u << lane) - 1u)), tot = 0;
+                    for (int w = 0; w < NW; ++w) {
+                        if (w < warp) off += s_wcnt[w];
+                        tot += s_wcnt[w];
+                    }
+                    if (keep && off < sg.ncap) d.cand[sg.cand0 + off] = (int)(((unsigned)k << 16) | (unsigned)j);
+                    __syncthreads();
+                    if (tid == 0) S.count += tot;
                 }
-                cg::cluster_group cl = cg::this_cluster();
-                cl.sync();
-                for (int r = 0; r < CS; ++r) {
-                    const int c = *cl.map_shared_rank(&s_cnt, r);
-                    if (r < crank) base_off += c;
-                    n_all += c;
-                }
-                cl.sync();
-            }
-            if (tid == 0) S.count = base_off;
-            __syncthreads();
-            for (long base = q0; base < q1; base += NT) {
-                const long q = base + tid;
-                bool keep = false;
-                int k = 0, j = 0;
-                if (q < q1) {
-                    float dd;
-                    keep = pair_keep(q, k, j, dd);
-                    if (keep) dmn = fminf(dmn, dd);
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, keep);
-                const int lane = tid & 31, warp = tid >> 5;
-                if (lane == 0) s_wcnt[warp] = __popc(bal);
-                __syncthreads();
-                int off = S.count + __popc(bal & ((1u << lane) - 1u)), tot = 0;
-                for (int w = 0; w < NW; ++w) {
-                    if (w < warp) off += s_wcnt[w];
-                    tot += s_wcnt[w];
-                }
-                if (keep && off < sg.ncap) d.cand[sg.cand0 + off] = (int)(((unsigned)k << 16) | (unsigned)j);
-                __syncthreads();
-                if (tid == 0) S.count += tot;
             }
             __syncthreads();
             double vm[1] = {(double)dmn};
@@ -1081,12 +1213,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             }
 
             // ---------------------------------------------- A4: body-level modes
-            for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b) {  // AffineBodies.gather, affine.py:156-175
+            // AffineBodies.gather, affine.py:156-175: a warp per body over the body's own nodes,
+            // summed in a fixed shuffle tree (FP64)
+            for (int b = sg.aff0 + (gt >> 5); b < sg.aff0 + sg.naff; b += GS / 32) {
                 double v[18];
 #pragma unroll
                 for (int q = 0; q < 18; ++q) v[q] = 0.0;
-                for (int k = sg.affn0 + gt; k < sg.affn0 + sg.naffn; k += GS) {
-                    if (d.a_grp[k] != b) continue;
+                const int k1 = d.a_ptr[b + 1];
+                for (int k = d.a_ptr[b] + (tid & 31); k < k1; k += 32) {
                     const int i = d.a_node[k];
                     const double *w = d.a_w + 3 * k;
                     const float2 g = G[i], dg = D[i];
@@ -1097,9 +1231,12 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
 #pragma unroll
                     for (int q = 0; q < 6; ++q) { v[6 + q] += dx * o[q]; v[12 + q] += dy * o[q]; }
                 }
-                const int ops[18] = {0};
-                scene_reduce<NT, CS, 18>(v, ops, red, cres);
-                if (tid == 0 && crank == 0) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+                    for (int q = 0; q < 18; ++q) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+                }
+                if ((tid & 31) == 0) {
                     for (int q = 0; q < 6; ++q) {
                         d.a_gq_prev[6 * b + q] = d.a_gq[6 * b + q];
                         d.a_gq[6 * b + q] = v[q];
@@ -1187,16 +1324,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             // ---------------------------------------------- B1: mask + Dai-Kou dot products
             // (+ the single rigid piece's B^T g, B^T g_prev, B^T D' B, affine.py:421-453)
             auto b2 = [&](const double *vs) {
-                if (tid == 0 && crank == 0) {  // B2: per-scene scalars, FP64
-                    double gPg = vs[0] + S.gPg, g_p = vs[1], g_Py = vs[2] + S.g_Py, y_p = vs[3], y_Py = vs[4] + S.y_Py;
-                    for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b) {  // affine_reduce_kernel, affine.py:178-205
-                        double *q = d.a_q + 6 * b;
+                // affine_reduce_kernel, affine.py:178-205: each body's 6x6 solve by one thread
+                // (FP64), its five Dai-Kou terms summed over the bodies in a fixed tree
+                double ab[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // gPg, g.p, g.Py, y.p, y.Py of the bodies
+                if (sg.naff > 0) {
+                    for (int b = sg.aff0 + gt; b < sg.aff0 + sg.naff; b += GS) {
+                        const double *q = d.a_q + 6 * b;
                         const M2 A{q[1], q[2], q[4], q[5]};
                         const M2 Pm = nh_P(A, d.a_Mu[b], d.a_La[b]);
-                        double g[6], y[6], z[6], zy[6];
+                        double g[6], y[6], z[6], zy[6], H[6][6], L[6][6];
                         const double hp[6] = {0.0, h2 * Pm.a, h2 * Pm.b, 0.0, h2 * Pm.c, h2 * Pm.d};
                         for (int r = 0; r < 6; ++r) g[r] = d.a_gq[6 * b + r] + hp[r];
-                        double (*H)[6] = s_H6, (*L)[6] = s_L6;
                         reduced_hessian(A, d.a_Mu[b], d.a_La[b], h2, d.a_H + 18 * b, H);
                         chol6(H, L);
                         for (int r = 0; r < 6; ++r) y[r] = g[r] - d.a_gq_prev[6 * b + r];
@@ -1204,11 +1342,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         chol6_solve(L, y, zy);
                         const double *pq = d.a_pq + 6 * b;
                         for (int r = 0; r < 6; ++r) {
-                            gPg += g[r] * z[r]; g_p += g[r] * pq[r]; g_Py += g[r] * zy[r];
-                            y_p += y[r] * pq[r]; y_Py += y[r] * zy[r];
+                            ab[0] += g[r] * z[r]; ab[1] += g[r] * pq[r]; ab[2] += g[r] * zy[r];
+                            ab[3] += y[r] * pq[r]; ab[4] += y[r] * zy[r];
                         }
                         for (int r = 0; r < 6; ++r) { d.a_gq[6 * b + r] = g[r]; d.a_zq[6 * b + r] = z[r]; }
                     }
+                    const int ops5[5] = {0, 0, 0, 0, 0};
+                    scene_reduce<NT, CS, 5>(ab, ops5, red, cres);
+                }
+                if (tid == 0) {  // B2: per-scene scalars, FP64 (every block of a cluster alike)
+                    const double gPg = vs[0] + S.gPg + ab[0], g_p = vs[1] + ab[1], g_Py = vs[2] + S.g_Py + ab[2];
+                    const double y_p = vs[3] + ab[3], y_Py = vs[4] + S.y_Py + ab[4];
                     double bta = 0.0;  // finalize_beta_kernel, kernels.py:195-217
                     if (it > 0 && dabs(y_p) > 1.0e-30) bta = g_Py / y_p - y_Py * g_p / (y_p * y_p);
                     double gtp = -gPg + bta * g_p;
@@ -1218,16 +1362,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         if (hold <= 0.0 && y_p < d.cg_guard * S.alpha * S.pHp) { bta = 0.0; gtp = -gPg; }
                     }
                     S.beta = bta; S.gTp = gtp; S.gn2 = vs[5];
-                    for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
-                        for (int r = 0; r < 6; ++r) d.a_pq[6 * b + r] = -d.a_zq[6 * b + r] + bta * d.a_pq[6 * b + r];
                 }
                 gsync();
-                if constexpr (CL) {  // the other blocks take rank 0's scalars
-                    if (tid == 0 && crank != 0) {
-                        const SceneSh *s0 = cg::this_cluster().map_shared_rank(&S, 0);
-                        S.beta = s0->beta; S.gTp = s0->gTp; S.gn2 = s0->gn2;
-                    }
-                    __syncthreads();
+                if (sg.naff > 0) {  // the bodies' directions, read by B3
+                    const double bta = S.beta;
+                    for (int b = sg.aff0 + gt; b < sg.aff0 + sg.naff; b += GS)
+                        for (int r = 0; r < 6; ++r) d.a_pq[6 * b + r] = -d.a_zq[6 * b + r] + bta * d.a_pq[6 * b + r];
+                    gsync();
                 }
             };
             auto b1 = [&](auto rig_tag) {
@@ -1563,9 +1704,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         }
                     }
                     if (S.active) {
-                        if (crank == 0)
-                            for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
-                                for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
                         S.motion += S.alpha * pinf;              // bound on any node's move
                         if (rig1) {                              // centroid shift, sum m dx / M
                             const double Mt = d.r_acc[3 * sg.rig0 + 2];
@@ -1575,6 +1713,11 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     }
                 }
                 gsync();
+                if (sg.naff > 0 && S.active) {  // AffineBodies.advance, affine.py:249-257: q += alpha p_q
+                    for (int b = sg.aff0 + gt; b < sg.aff0 + sg.naff; b += GS)
+                        for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
+                    gsync();
+                }
             }
 
             // ---------------------------------------------- D1: r += alpha p, dx = (x_b - x_n) + r (slaved nodes: J q)

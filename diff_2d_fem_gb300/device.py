@@ -248,6 +248,7 @@ class DeviceSolver:
         if af is not None:
             T_("a_node", af["node"], i32)
             T_("a_grp", af["grp"], i32)
+            T_("a_ptr", np.searchsorted(af["grp"], np.arange(n_aff + 1)), i32)
             T_("a_w", af["w"], f64)
             T_("a_Mu", af["Mu"], f64)
             T_("a_La", af["La"], f64)

@@ -169,13 +169,13 @@ def _disc_mask(r):
 
 
 def slab_with_holes(n_scenes=1, seed=0, H=256, W=1024, px=0.5e-3, n_holes=200, n_discs=32,
-                    hole_r=(3, 12), disc_r=(8, 20)):
+                    hole_r=(3, 12), disc_r=(8, 20), drop=(5e-3, 50e-3)):
     """The large-scene configuration: per scene, an H x W-pixel soft slab (E 1 MPa, nu 0.40,
     density 1100) lying on the ground with n_holes circular holes of radius U{hole_r} pixels
     at seeded, non-overlapping centres, and n_discs affine discs of radius U{disc_r} pixels
-    (density U[500, 2000]) placed 5-50 mm above the slab at seeded, non-overlapping x; gravity
-    on, IPC contact between bodies and with the ground. Defaults: 256 x 1024 pixels of 0.5 mm
-    (0.128 m x 0.512 m), 200 holes, 32 discs."""
+    (density U[500, 2000]) placed U[drop] above the slab (default 5-50 mm) at seeded,
+    non-overlapping x; gravity on, IPC contact between bodies and with the ground. Defaults:
+    256 x 1024 pixels of 0.5 mm (0.128 m x 0.512 m), 200 holes, 32 discs."""
     rng = np.random.default_rng(seed)
     m = Model()
     m.add_ground(0.0)
@@ -204,7 +204,7 @@ def slab_with_holes(n_scenes=1, seed=0, H=256, W=1024, px=0.5e-3, n_holes=200, n
             if any(abs(x - a) < (r + q) * px + 2 * px for a, q in xs):
                 continue
             xs.append((x, r))
-            y = H * px + rng.uniform(5e-3, 50e-3) + r * px
+            y = H * px + rng.uniform(drop[0], drop[1]) + r * px
             m.add_affine_body(_disc_mask(r), physical_size=(2 * r * px, 2 * r * px), center=(x, y),
                               density=float(rng.uniform(500.0, 2000.0)), env_id=e)
     m.finalize()

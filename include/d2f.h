@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define D2F_ABI_VERSION 3
+#define D2F_ABI_VERSION 4
 
 /* status codes */
 #define D2F_OK 0
@@ -138,6 +138,8 @@ typedef struct d2f_scene_desc {
                                     or 8, whichever finishes the batch first, when the batch has
                                     fewer scenes than SMs and at least 16384 nodes per scene;
                                     else 1) */
+    const int32_t *a_ptr;        /* n_aff + 1: affine body b owns entries a_ptr[b] .. a_ptr[b+1]-1 of
+                                    a_node / a_grp / a_w (required with affine bodies) */
 } d2f_scene_desc;
 
 typedef struct d2f_solver d2f_solver;

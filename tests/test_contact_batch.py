@@ -96,14 +96,16 @@ def test_step_in_contact_matches_oracle():
 
 
 def test_converged_step_in_contact_mixed_matches_fp64():
-    """From the in-contact state, one step run (nearly) to convergence: 20000 iterations (the
+    """From the in-contact state, one step run (nearly) to convergence: 40000 iterations (the
     1 GPa block squeezed between 0.3 MPa pads is so ill-conditioned that 4000 iterations still
     leave 3e-5 and 20000 leave 2e-9 of the 60000-iteration answer, against which mixed and FP64
-    agree to 2.5e-11). The mixed path within 1e-8 of the FP64 path, relative to the
-    coordinates, and the IPC contact energies (oracle-evaluated) within 1e-6 relative: the
-    barrier energy varies like (position change) / (gap ~ 1e-5 m), far faster than positions."""
+    agree to 2.5e-11; the mixed path's FP32 atomic sums vary its approach from run to run, up
+    to 5e-7 from FP64 after 20000 iterations, 3e-10 after 40000). The mixed path within 1e-8
+    of the FP64 path, relative to the coordinates, and the IPC contact energies
+    (oracle-evaluated) within 1e-6 relative: the barrier energy varies like
+    (position change) / (gap ~ 1e-5 m), far faster than positions."""
     p2, tg, x0 = _contact_state()
-    p2["iter_max"], p2["eps"] = 20000, 0.0
+    p2["iter_max"], p2["eps"] = 40000, 0.0
     x64 = _one_step(p2, tg, "fp64")
     xmx = _one_step(p2, tg, "mixed")
     assert rel_err(xmx, x64) < 1e-8
