@@ -215,7 +215,7 @@ int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads,
     if (!s) return fail(D2F_EINVAL, "d2f_launch_shape: null handle");
     if (blocks) *blocks = s->grid;
     if (threads) {
-        int vnt = 256, vminb = 1;
+        int vnt = d2f::kClusterThreads, vminb = 1;
         if (s->cs == 1) pick_variant(d2f_default_threads(s->d), s->d.blocks_per_sm, &vnt, &vminb);
         *threads = vnt;
     }

@@ -7,7 +7,6 @@
 namespace d2f {
 
 namespace {
-constexpr int kClusterThreads = 256;
 
 template <int CS>
 void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute &at, int grid, int smem, cudaStream_t st) {

@@ -223,6 +223,8 @@ constexpr int NI_AFF = 4, NI_RIG = 8;
 // contact candidate lists of scenes with at least HASH_MIN_NB boundary nodes are built through
 // a spatial hash of HASH_B buckets (every other scene tests all edge-node pairs)
 constexpr int HASH_MIN_NB = 4096, HASH_B = 4096;
+// the cluster path's ACCD replay: candidates below the running cap, per block
+constexpr int REL_CAP = 512;
 // the hash (HASH_B bucket ends + the slots, 4 bytes each) reuses the 8 bytes per boundary node
 // of dynamic shared memory the exhaustive build holds its positions in
 static_assert(HASH_MIN_NB >= HASH_B, "hash tables must fit the boundary-position buffer");
@@ -276,6 +278,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     __shared__ float mres[16];               // block_reduce_mx: up to 16 FP32 results (rigid pass: 12)
     __shared__ int sc_next;
     __shared__ int s_cnt;                    // cluster list build: this block's kept pairs
+    __shared__ int s_nrel;                   // cluster ACCD replay: this block's pairs below the cap
+    __shared__ int s_rel[REL_CAP];           // ... their candidate indices, in order
     __shared__ double cres[24];              // cluster reductions: the combined result
     __shared__ float cmres[16];
     __shared__ int s_wcnt[NW];
@@ -930,9 +934,56 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             // T < m0 are replayed — found by warp ballots in candidate order, walked in that
             // order by thread 0 with the same per-edge reset: the result equals the full serial
             // replay.
+            const int nc = S.ncand;
+            if constexpr (CL) {
+                // each block filters its contiguous share of the candidates into an ordered list
+                // in shared memory; thread 0 of every block walks the lists in rank order
+                // (distributed shared memory): the same pairs in the same order as the full walk
+                const int cchunk = (nc + CS - 1) / CS;
+                const int c0 = min(crank * cchunk, nc), c1 = min(c0 + cchunk, nc);
+                if (tid == 0) s_nrel = 0;
+                __syncthreads();
+                for (int base = c0; base < c1; base += NT) {
+                    const int c = base + tid;
+                    const bool rel = c < c1 && Ctr[sg.cand0 + c].x < m0;
+                    const unsigned bal = __ballot_sync(0xffffffffu, rel);
+                    if ((tid & 31) == 0) s_wmask[tid >> 5] = bal;
+                    __syncthreads();
+                    int off = s_nrel + __popc(bal & ((1u << (tid & 31)) - 1u)), tot = 0;
+                    for (int w = 0; w < NW; ++w) {
+                        const int pc = __popc(s_wmask[w]);
+                        if (w < (tid >> 5)) off += pc;
+                        tot += pc;
+                    }
+                    if (rel && off < REL_CAP) s_rel[off] = c;
+                    __syncthreads();
+                    if (tid == 0) s_nrel += tot;
+                }
+                cg::cluster_group cl = cg::this_cluster();
+                cl.sync();
+                bool over = false;  // a list that did not fit: the full walk below, every block
+                for (int r = 0; r < CS; ++r) over |= *cl.map_shared_rank(&s_nrel, r) > REL_CAP;
+                double m = m0;
+                if (!over && tid == 0) {
+                    double t_c = m0;
+                    int prevk = -1;
+                    for (int r = 0; r < CS; ++r) {
+                        const int n = *cl.map_shared_rank(&s_nrel, r);
+                        const int *lst = cl.map_shared_rank(s_rel, r);
+                        for (int i = 0; i < n; ++i) {
+                            const int cc = lst[i];
+                            const int k = (int)((unsigned)d.cand[sg.cand0 + cc] >> 16);
+                            const double2 pr = Ctr[sg.cand0 + cc];
+                            if (k != prevk) { t_c = m; prevk = k; }
+                            m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+                        }
+                    }
+                }
+                cl.sync();  // every remote read done before the lists are rebuilt
+                if (!over) return m;
+            }
             double m = m0, t_c = m0;
             int prevk = -1;
-            const int nc = S.ncand;
             for (int base = 0; base < nc; base += NT) {
                 const int c = base + tid;
                 const bool rel = c < nc && Ctr[sg.cand0 + c].x < m0;
@@ -1017,8 +1068,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const float2 u0 = XR[i0], u1 = XR[i1], u2 = XR[i2];
                 const float q1x = u1.x - u0.x, q1y = u1.y - u0.y;  // edges of x - x_b
                 const float q2x = u2.x - u0.x, q2y = u2.y - u0.y;
-                const float d1x = du.x + q1x, d1y = du.y + q1y;
-                const float d2x = du.z + q2x, d2y = du.w + q2y;
                 // displacement gradient Hn at the base x_b and its increment K (F = I + Hn + K)
                 const float n00 = du.x * B.x + du.z * B.z, n01 = du.x * B.y + du.z * B.w;
                 const float n10 = du.y * B.x + du.w * B.z, n11 = du.y * B.y + du.w * B.w;

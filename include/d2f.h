@@ -134,7 +134,7 @@ typedef struct d2f_scene_desc {
     int32_t line_search;         /* 0 off, 1 on */
     int32_t n_backtrack;         /* halvings tried per iteration */
     int32_t blocks_per_scene;    /* mixed precision: thread blocks working on one scene, as one
-                                    cluster of 256-thread blocks: 1, 8 or 16 (0: a cluster of 16
+                                    cluster of 512-thread blocks: 1, 8 or 16 (0: a cluster of 16
                                     or 8, whichever finishes the batch first, when the batch has
                                     fewer scenes than SMs and at least 16384 nodes per scene;
                                     else 1) */
