@@ -13,7 +13,7 @@ _I = C.c_int32
 _D = C.c_double
 _P = C.c_void_p
 
-D2F_ABI_VERSION = 4
+D2F_ABI_VERSION = 5
 D2F_FP64, D2F_MIXED = 0, 1
 ERRORS = {0: "ok", -1: "D2F_EINVAL", -2: "D2F_ECUDA", -3: "D2F_ECAP", -4: "D2F_ENAN"}
 
@@ -21,7 +21,8 @@ ERRORS = {0: "ok", -1: "D2F_EINVAL", -2: "D2F_ECUDA", -3: "D2F_ECAP", -4: "D2F_E
 class Seg(C.Structure):
     _fields_ = [(n, _I) for n in (
         "node0", "nn", "tri0", "nt", "bnd0", "nb", "edge0", "ne", "cand0", "ncap", "bc0", "nbc",
-        "aff0", "naff", "affn0", "naffn", "rig0", "nrig", "rign0", "nrign", "ten0", "nten", "tent0", "ntent")]
+        "aff0", "naff", "affn0", "naffn", "rig0", "nrig", "rign0", "nrign", "ten0", "nten", "tent0", "ntent",
+        "sp0", "nsp", "pe0", "npe")]
 
 
 DESC_FIELDS = (
@@ -41,7 +42,8 @@ DESC_FIELDS = (
                          "reach", "gap", "bc_floor", "skin")]
     + [(n, _I) for n in ("iter_max", "conv_check", "friction", "per_body", "threads", "blocks_per_sm")]
     + [("ls_tol", _D), ("line_search", _I), ("n_backtrack", _I), ("blocks_per_scene", _I),
-       ("a_ptr", _P)]
+       ("a_ptr", _P), ("n_sp", _I)] + [(n, _P) for n in ("sp_a", "sp_b", "sp_k", "sp_L0", "sp_anchor")]
+    + [("n_pe", _I), ("n_ch", _I)] + [(n, _P) for n in ("pe_a", "pe_b", "pe_ch", "ch_p", "ch_ref")]
 )
 
 

@@ -55,7 +55,18 @@ def _solver_of(obj):
             "ImplicitIntegrator(self_collision=False)")
     if s.desc.n_aff > 0:
         raise NotImplementedError("the adjoint operator has no tangent for affine bodies")
+    _refuse_actuators(s.desc.n_pe > 0, s.desc.n_sp > 0, bool(s.prob.get("active_regions", 0)))
     return s
+
+
+def _refuse_actuators(pressure, springs, active):
+    """The reference's refusal (implicit/adjoint.py:376-385): no gradient of a different
+    system for terms the adjoint operator has no tangent for."""
+    missing = [nm for nm, on in (("ActiveStrain", active), ("Pressure", pressure), ("Springs", springs)) if on]
+    if missing:
+        raise NotImplementedError(
+            f"the adjoint operator has no tangent for {', '.join(missing)}: the gradient would be "
+            f"of a different system. Differentiate without these actuators.")
 
 
 class AdjointPNCG2D:
@@ -65,9 +76,10 @@ class AdjointPNCG2D:
     mu_e = E(rho_e) mu0_e, lam_e = E(rho_e) lam0_e with E(rho) = Emin + rho (1 - Emin), mu0 and
     lam0 the moduli the solver was built with."""
 
-    def __init__(self, solver, Emin=1e-3):
+    def __init__(self, solver, Emin=1e-3, model=None):
         s = _solver_of(solver)
-        self.s = s
+        self._s = s
+        self.model = model          # its current solver is followed: one rebuilt for a new term
         self.Emin = float(Emin)
         self.dev = s.dev
         self.N, self.n_tri, self.B = s.N, int(s.desc.T), s.B
@@ -84,6 +96,17 @@ class AdjointPNCG2D:
         self.max_iters = torch.zeros(self.B, dtype=torch.int32, device=self.dev)
         self.total_iters = torch.zeros(self.B, dtype=torch.int64, device=self.dev)
         self.solves = 0
+
+    @property
+    def s(self):
+        """The solver: the model's current one when built from a model (the integrator
+        rebuilds it when a term is added), with this adjoint's modulus multipliers applied."""
+        m = self.model
+        if m is not None and m._solver is not None and m._solver is not self._s:
+            self._s = _solver_of(m._solver)
+            self._s.tensor("mu").copy_(self.mu0 * self.E)
+            self._s.tensor("lam").copy_(self.lam0 * self.E)
+        return self._s
 
     @property
     def h2(self):
@@ -158,6 +181,10 @@ class AdjointPNCG2D:
         """implicit/adjoint.py:371-399. xs = [x_0 .. x_T] (the forward states, arrays or
         tensors (N, 2)), seed = {k: dJ/dx_k (N, 2)}. Returns dJ/drho (n_tri,) as a device
         tensor, accumulated over the trajectory."""
+        m = self.model
+        if m is not None:
+            _refuse_actuators(bool(m._chambers), bool(m._springs), bool(m._regions))
+            self.s                  # the model's current solver
         T = len(xs) - 1
         dr = self.drag if drag is None else float(drag)
         m2 = self.mass[:, None]

@@ -389,6 +389,8 @@ int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs,
     if (s->d.precision != D2F_FP64) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: needs an FP64 solver");
     if (s->d.Ne > 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: IPC contact between bodies has no adjoint tangent");
     if (s->d.n_aff > 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: affine bodies have no adjoint tangent");
+    if (s->d.n_sp > 0 || s->d.n_pe > 0)
+        return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: springs and pressure chambers have no adjoint tangent");
     if (!(rtol > 0.0) || max_iter <= 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: rtol > 0 and max_iter > 0");
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(s->d.work, 0, 4 * sizeof(int32_t), st) != cudaSuccess)

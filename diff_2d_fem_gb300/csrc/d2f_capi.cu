@@ -95,6 +95,10 @@ static int validate(const d2f_scene_desc &d, bool scratch) {
         if (!d.xu) return fail(D2F_EINVAL, "d2f: the line search needs xu (N x 2 doubles)");
         if (d.n_backtrack < 0 || !(d.ls_tol >= 0.0)) return fail(D2F_EINVAL, "d2f: n_backtrack >= 0, ls_tol >= 0");
     }
+    if (d.n_sp < 0 || (d.n_sp > 0 && (!d.sp_a || !d.sp_b || !d.sp_k || !d.sp_L0 || !d.sp_anchor)))
+        return fail(D2F_EINVAL, "d2f: spring arrays missing");
+    if (d.n_pe < 0 || d.n_ch < 0 || (d.n_pe > 0 && (d.n_ch <= 0 || !d.pe_a || !d.pe_b || !d.pe_ch || !d.ch_p || !d.ch_ref)))
+        return fail(D2F_EINVAL, "d2f: pressure arrays missing");
     if (d.blocks_per_scene != 0 && d.blocks_per_scene != 1 && d.blocks_per_scene != 8 && d.blocks_per_scene != 16)
         return fail(D2F_EINVAL, "d2f: blocks_per_scene must be 0, 1, 8 or 16");
     if (d.blocks_per_scene > 1 && d.precision != D2F_MIXED)

@@ -109,6 +109,22 @@ struct Col {
 };
 
 // ---------------------------------------------------------------------- small helpers
+// Springs._spring (implicit/actuation.py:396-402): d = x_a - x_b, length |d| = sqrt(d.d + 1e-30),
+// tension k (|d| - L0), tangential stiffness max(k (1 - L0 / |d|), 0), direction d / |d|.
+struct SpringAt {
+    double ten, kt, len, nx, ny;
+};
+__device__ __forceinline__ SpringAt spring_at(double2 xa, double2 xb, double k, double L0) {
+    const double dx = xa.x - xb.x, dy = xa.y - xb.y;
+    const double ln = sqrt(dx * dx + dy * dy + 1.0e-30);
+    const double kt = k * (1.0 - L0 / ln);
+    return SpringAt{k * (ln - L0), kt > 0.0 ? kt : 0.0, ln, dx / ln, dy / ln};
+}
+// the other end of spring k: node sp_b, or the world anchor
+__device__ __forceinline__ double2 spring_anchor(const d2f_scene_desc &d, int k) {
+    return make_double2(d.sp_anchor[2 * k], d.sp_anchor[2 * k + 1]);
+}
+
 __device__ __forceinline__ bool excluded(const d2f_scene_desc &d, int slot, int local) {
     int lo = __ldg(d.excl_ptr + slot), hi = __ldg(d.excl_ptr + slot + 1);
     while (lo < hi) {
@@ -558,6 +574,19 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 e += h2 * (0.5 * d.a_Mu[b] * (ddot2(A, A) - 2.0) - d.a_Mu[b] * logJ + 0.5 * d.a_La[b] * logJ * logJ);
             }
             if (scene_ipc) ipc_pairs(2, e, 0.0);
+            for (int k = sg.sp0 + tid; k < sg.sp0 + sg.nsp; k += NT) {  // Springs.energy, actuation.py:447-456
+                const int b = d.sp_b[k];
+                const SpringAt sa = spring_at(X[d.sp_a[k]], b >= 0 ? X[b] : spring_anchor(d, k), d.sp_k[k], d.sp_L0[k]);
+                const double ext = sa.len - d.sp_L0[k];
+                e += 0.5 * h2 * d.sp_k[k] * ext * ext;
+            }
+            for (int q = sg.pe0 + tid; q < sg.pe0 + sg.npe; q += NT) {  // Pressure.energy, actuation.py:121-130
+                const int c = d.pe_ch[q];
+                const double2 xa = X[d.pe_a[q]], xb = X[d.pe_b[q]];
+                const double rax = xa.x - d.ch_ref[2 * c], ray = xa.y - d.ch_ref[2 * c + 1];
+                const double rbx = xb.x - d.ch_ref[2 * c], rby = xb.y - d.ch_ref[2 * c + 1];
+                e += -h2 * d.ch_p[c] * 0.5 * (rax * rby - ray * rbx);
+            }
             for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
                 double L = 0.0;
                 for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
@@ -821,6 +850,33 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 ipc_refresh(false);
                 double z0 = 0.0;
                 ipc_pairs(0, z0, 0.0);
+                __syncthreads();
+            }
+            if (sg.nsp > 0 || sg.npe > 0) {
+                for (int k = sg.sp0 + tid; k < sg.sp0 + sg.nsp; k += NT) {  // Springs.grad_diag, actuation.py:405-424
+                    const int a = d.sp_a[k], b = d.sp_b[k];
+                    const SpringAt sa = spring_at(X[a], b >= 0 ? X[b] : spring_anchor(d, k), d.sp_k[k], d.sp_L0[k]);
+                    const double gx = h2 * sa.ten * sa.nx, gy = h2 * sa.ten * sa.ny, kk = d.sp_k[k];
+                    const double hx = h2 * (kk * sa.nx * sa.nx + sa.kt * (1.0 - sa.nx * sa.nx));
+                    const double hy = h2 * (kk * sa.ny * sa.ny + sa.kt * (1.0 - sa.ny * sa.ny));
+                    R *ga = reinterpret_cast<R *>(G + a), *da = reinterpret_cast<R *>(D + a);
+                    atomicAdd(ga, R(gx)); atomicAdd(ga + 1, R(gy));
+                    atomicAdd(da, R(hx)); atomicAdd(da + 1, R(hy));
+                    if (b >= 0) {
+                        R *gb = reinterpret_cast<R *>(G + b), *db = reinterpret_cast<R *>(D + b);
+                        atomicAdd(gb, R(-gx)); atomicAdd(gb + 1, R(-gy));
+                        atomicAdd(db, R(hx)); atomicAdd(db + 1, R(hy));
+                    }
+                }
+                for (int e = sg.pe0 + tid; e < sg.pe0 + sg.npe; e += NT) {  // Pressure.grad_diag, actuation.py:98-108
+                    const int a = d.pe_a[e], b = d.pe_b[e];
+                    const double2 xa = X[a], xb = X[b];
+                    const double sp = -0.5 * h2 * d.ch_p[d.pe_ch[e]];
+                    const double gx = sp * (xb.y - xa.y), gy = -sp * (xb.x - xa.x);
+                    R *ga = reinterpret_cast<R *>(G + a), *gb = reinterpret_cast<R *>(G + b);
+                    atomicAdd(ga, R(gx)); atomicAdd(ga + 1, R(gy));
+                    atomicAdd(gb, R(gx)); atomicAdd(gb + 1, R(gy));
+                }
                 __syncthreads();
             }
             if (sg.nten > 0) {  // Tendon.grad_diag, actuation.py:169-212, 298-303
@@ -1181,6 +1237,18 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 // IPC mode 1: curvature along p and the ACCD step limit (t_c = the step cap at
                 // the start of the contact pass, alpha_max)
                 if (scene_ipc) ipc_pairs(1, acc_pHp, d.alpha_max);
+                for (int k = sg.sp0 + tid; k < sg.sp0 + sg.nsp; k += NT) {  // Springs.pHp, actuation.py:427-444
+                    const int a = d.sp_a[k], b = d.sp_b[k];
+                    const SpringAt sa = spring_at(X[a], b >= 0 ? X[b] : spring_anchor(d, k), d.sp_k[k], d.sp_L0[k]);
+                    double dpx = double(P[a].x), dpy = double(P[a].y);
+                    if (b >= 0) { dpx -= double(P[b].x); dpy -= double(P[b].y); }
+                    const double along = dpx * sa.nx + dpy * sa.ny;
+                    acc_pHp += h2 * (d.sp_k[k] * along * along + sa.kt * ((dpx * dpx + dpy * dpy) - along * along));
+                }
+                for (int e = sg.pe0 + tid; e < sg.pe0 + sg.npe; e += NT) {  // Pressure.pHp, actuation.py:111-118
+                    const R2 pa = P[d.pe_a[e]], pb = P[d.pe_b[e]];
+                    acc_pHp += -h2 * d.ch_p[d.pe_ch[e]] * (double(pa.x) * double(pb.y) - double(pa.y) * double(pb.x));
+                }
                 // Tendon.pHp (actuation.py:244-268, 305-310)
                 for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
                     double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3], dL = 0.0;

@@ -317,7 +317,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     const double2 *__restrict__ Fx = reinterpret_cast<const double2 *>(d.fext);
     const double2 *__restrict__ Tgt = reinterpret_cast<const double2 *>(d.bc_target);
     double2 *__restrict__ Ctr = reinterpret_cast<double2 *>(d.cand_tr);
-    const double2 *__restrict__ Xr = reinterpret_cast<const double2 *>(d.xrest);
+    // rest edge vectors of each triangle (X1 - X0, X2 - X0 after any active-strain change)
+    const double2 *__restrict__ Dm2 = reinterpret_cast<const double2 *>(d.Dm);
     // the per-step scratch arrays: pointers from the parameter space (constant bank), not
     // registers
     float2 *__restrict__ XD = mp.xd;       // x - x_n
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         const int t0 = sg.tri0, t1 = sg.tri0 + sg.nt;
         const bool scene_ipc = has_ipc && sg.ne > 0;
         const bool scene_rig = sg.nrig > 0;
-        const bool scene_rare = scene_ipc || sg.naff > 0 || sg.nten > 0;  // terms with FP64 contributions
+        const bool scene_rare = scene_ipc || sg.naff > 0 || sg.nten > 0 || sg.nsp > 0 || sg.npe > 0;  // terms with FP64 contributions
         const int nbl = sg.nb;
         const double near = d.near_factor * dhat;
         if (tid < n_col && tid < MAX_COL) {
@@ -397,9 +398,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             gsync();
             for (int t = t0 + gt; t < t1; t += GS) {
                 const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
-                const double2 a0 = XBd[i0], a1 = XBd[i1], a2 = XBd[i2], r0 = Xr[i0], r1 = Xr[i1], r2 = Xr[i2];
-                const double e1x = (a1.x - a0.x) - (r1.x - r0.x), e1y = (a1.y - a0.y) - (r1.y - r0.y);
-                const double e2x = (a2.x - a0.x) - (r2.x - r0.x), e2y = (a2.y - a0.y) - (r2.y - r0.y);
+                const double2 a0 = XBd[i0], a1 = XBd[i1], a2 = XBd[i2], r1 = Dm2[2 * t], r2 = Dm2[2 * t + 1];
+                const double e1x = (a1.x - a0.x) - r1.x, e1y = (a1.y - a0.y) - r1.y;
+                const double e2x = (a2.x - a0.x) - r2.x, e2y = (a2.y - a0.y) - r2.y;
                 DU0[t] = make_float4((float)e1x, (float)e1y, (float)e2x, (float)e2y);
                 const float4 Bf = Bm[t];
                 const double bx = Bf.x, by = Bf.y, bz = Bf.z, bw = Bf.w;
@@ -462,6 +463,24 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     const double2 g = tendon_dlen(xbpos, d.t_node, d.t_prv[j], d.t_nxt[j], n);
                     atomicAdd(&G0d[n].x, h2 * tau * g.x);
                     atomicAdd(&G0d[n].y, h2 * tau * g.y);
+                }
+                gsync();
+            }
+            if (sg.nsp > 0 || sg.npe > 0) {  // spring and pressure forces at x_b (FP64)
+                for (int k = sg.sp0 + gt; k < sg.sp0 + sg.nsp; k += GS) {
+                    const int a = d.sp_a[k], b = d.sp_b[k];
+                    const SpringAt sa = spring_at(XBd[a], b >= 0 ? XBd[b] : spring_anchor(d, k), d.sp_k[k], d.sp_L0[k]);
+                    const double gx = h2 * sa.ten * sa.nx, gy = h2 * sa.ten * sa.ny;
+                    atomicAdd(&G0d[a].x, gx); atomicAdd(&G0d[a].y, gy);
+                    if (b >= 0) { atomicAdd(&G0d[b].x, -gx); atomicAdd(&G0d[b].y, -gy); }
+                }
+                for (int e = sg.pe0 + gt; e < sg.pe0 + sg.npe; e += GS) {
+                    const int a = d.pe_a[e], b = d.pe_b[e];
+                    const double2 xa = XBd[a], xb = XBd[b];
+                    const double sp = -0.5 * h2 * d.ch_p[d.pe_ch[e]];
+                    const double gx = sp * (xb.y - xa.y), gy = -sp * (xb.x - xa.x);
+                    atomicAdd(&G0d[a].x, gx); atomicAdd(&G0d[a].y, gy);
+                    atomicAdd(&G0d[b].x, gx); atomicAdd(&G0d[b].y, gy);
                 }
                 gsync();
             }
@@ -1261,6 +1280,39 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 gsync();
             }
 
+            if (sg.nsp > 0 || sg.npe > 0) {
+                // Springs.grad_diag (actuation.py:405-424): the force at x minus the one at x_b in
+                // the base gradient (FP64), the diagonal at x
+                for (int k = sg.sp0 + gt; k < sg.sp0 + sg.nsp; k += GS) {
+                    const int a = d.sp_a[k], b = d.sp_b[k];
+                    const double kk = d.sp_k[k], L0 = d.sp_L0[k];
+                    const SpringAt sa = spring_at(xpos(a), b >= 0 ? xpos(b) : spring_anchor(d, k), kk, L0);
+                    const SpringAt s0 = spring_at(XBd[a], b >= 0 ? XBd[b] : spring_anchor(d, k), kk, L0);
+                    const float gx = (float)(h2 * (sa.ten * sa.nx - s0.ten * s0.nx));
+                    const float gy = (float)(h2 * (sa.ten * sa.ny - s0.ten * s0.ny));
+                    const float hx = (float)(h2 * (kk * sa.nx * sa.nx + sa.kt * (1.0 - sa.nx * sa.nx)));
+                    const float hy = (float)(h2 * (kk * sa.ny * sa.ny + sa.kt * (1.0 - sa.ny * sa.ny)));
+                    float *ga = reinterpret_cast<float *>(G + a), *da = reinterpret_cast<float *>(D + a);
+                    atomicAdd(ga, gx); atomicAdd(ga + 1, gy); atomicAdd(da, hx); atomicAdd(da + 1, hy);
+                    if (b >= 0) {
+                        float *gb = reinterpret_cast<float *>(G + b), *db = reinterpret_cast<float *>(D + b);
+                        atomicAdd(gb, -gx); atomicAdd(gb + 1, -gy); atomicAdd(db, hx); atomicAdd(db + 1, hy);
+                    }
+                }
+                // Pressure.grad_diag (actuation.py:98-108): linear in x, so the increment since x_b
+                // is the same term of the offsets r
+                for (int e = sg.pe0 + gt; e < sg.pe0 + sg.npe; e += GS) {
+                    const int a = d.pe_a[e], b = d.pe_b[e];
+                    const float2 ra = XR[a], rb = XR[b];
+                    const double sp = -0.5 * h2 * d.ch_p[d.pe_ch[e]];
+                    const float gx = (float)(sp * ((double)rb.y - (double)ra.y));
+                    const float gy = (float)(-sp * ((double)rb.x - (double)ra.x));
+                    float *ga = reinterpret_cast<float *>(G + a), *gb = reinterpret_cast<float *>(G + b);
+                    atomicAdd(ga, gx); atomicAdd(ga + 1, gy); atomicAdd(gb, gx); atomicAdd(gb + 1, gy);
+                }
+                gsync();
+            }
+
             // ---------------------------------------------- A4: body-level modes
             // AffineBodies.gather, affine.py:156-175: a warp per body over the body's own nodes,
             // summed in a fixed shuffle tree (FP64)
@@ -1686,6 +1738,18 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         acc_rare += h2 * dmax(ddot2(dA, nh_d2(A, dA, d.a_Mu[b], d.a_La[b])), 0.0);
                     }
                     if (scene_ipc) ipc_pairs(1, acc_rare, d.alpha_max);
+                    for (int k = sg.sp0 + gt; k < sg.sp0 + sg.nsp; k += GS) {  // Springs.pHp, actuation.py:427-444
+                        const int a = d.sp_a[k], b = d.sp_b[k];
+                        const SpringAt sa = spring_at(xpos(a), b >= 0 ? xpos(b) : spring_anchor(d, k), d.sp_k[k], d.sp_L0[k]);
+                        double dpx = (double)P[a].x, dpy = (double)P[a].y;
+                        if (b >= 0) { dpx -= (double)P[b].x; dpy -= (double)P[b].y; }
+                        const double along = dpx * sa.nx + dpy * sa.ny;
+                        acc_rare += h2 * (d.sp_k[k] * along * along + sa.kt * ((dpx * dpx + dpy * dpy) - along * along));
+                    }
+                    for (int e = sg.pe0 + gt; e < sg.pe0 + sg.npe; e += GS) {  // Pressure.pHp, actuation.py:111-118
+                        const float2 pa = P[d.pe_a[e]], pb = P[d.pe_b[e]];
+                        acc_rare += -h2 * d.ch_p[d.pe_ch[e]] * ((double)pa.x * (double)pb.y - (double)pa.y * (double)pb.x);
+                    }
                     for (int k = sg.ten0 + gt; k < sg.ten0 + sg.nten; k += GS) {  // Tendon.pHp
                         const double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3];
                         double dL = 0.0;

@@ -69,7 +69,7 @@ class DeviceSolver:
         b_s, b_c = _ranges(prob["b2e"], B)
         Nb = len(bnd)
 
-        segs = np.zeros((B, 24), np.int32)
+        segs = np.zeros((B, 28), np.int32)
         segs[:, 0], segs[:, 1] = n_s, n_c
         segs[:, 2], segs[:, 3] = t_s, t_c
         segs[:, 4], segs[:, 5] = b_s, b_c
@@ -170,6 +170,27 @@ class DeviceSolver:
             segs[:, 22], segs[:, 23] = tn_s, tn_c
         self.td = td
 
+        # springs and pins, grouped by environment
+        sp = prob.get("springs")
+        n_sp = 0
+        self.sp_order = None
+        if sp is not None and len(sp["env"]):
+            self.sp_order = np.argsort(np.asarray(sp["env"], np.int64), kind="stable")
+            sp = {k: np.asarray(v)[self.sp_order] for k, v in sp.items()}
+            n_sp = len(sp["env"])
+            segs[:, 24], segs[:, 25] = _ranges(sp["env"], B)
+        # pressure boundary edges, grouped by their chamber's environment
+        pr = prob.get("pressure")
+        n_pe = n_ch = 0
+        if pr is not None and len(pr["ea"]):
+            ch2env = np.asarray(pr["ch2env"], np.int64)
+            ch = np.asarray(pr["ch"], np.int64)
+            eo = np.argsort(ch2env[ch], kind="stable")
+            pr = dict(pr, ea=np.asarray(pr["ea"])[eo], eb=np.asarray(pr["eb"])[eo], ch=ch[eo])
+            n_pe, n_ch = len(pr["ea"]), len(ch2env)
+            segs[:, 26], segs[:, 27] = _ranges(ch2env[pr["ch"]], B)
+        self.sp, self.pr = sp, pr
+
         # node -> corner CSR, ascending triangle per node
         corner_node = tri.reshape(-1)
         order = np.argsort(corner_node, kind="stable")
@@ -190,7 +211,10 @@ class DeviceSolver:
             # from the rest shape (rest edge vectors per triangle)
             rest = np.asarray(prob.get("rest", x), np.float64)
             T_("xrest", rest, f64)
-            T_("Dm", np.concatenate([rest[tri[:, 1]] - rest[tri[:, 0]], rest[tri[:, 2]] - rest[tri[:, 0]]], 1), rdt)
+            Dm = prob.get("Dm")
+            if Dm is None:
+                Dm = np.concatenate([rest[tri[:, 1]] - rest[tri[:, 0]], rest[tri[:, 2]] - rest[tri[:, 0]]], 1)
+            T_("Dm", np.asarray(Dm, np.float64).reshape(T, 4), f64)
         self.xhat = T_("xhat", np.zeros_like(x), f64)
         for nm in ("grad", "grad_prev", "p", "diagH", "diag_el"):
             T_(nm, np.zeros((N, 2)), rdt)
@@ -245,6 +269,18 @@ class DeviceSolver:
             T_("t_L0", td["L0"], f64)
             T_("t_Tcmd", td["Tcmd"], f64)
             T_("t_state", np.zeros((n_ten, 4)), f64)
+        if sp is not None and n_sp:
+            T_("sp_a", sp["a"], i32)
+            T_("sp_b", sp["b"], i32)
+            T_("sp_k", sp["k"], f64)
+            T_("sp_L0", sp["L0"], f64)
+            T_("sp_anchor", np.asarray(sp["anchor"], np.float64).reshape(-1, 2), f64)
+        if pr is not None and n_pe:
+            T_("pe_a", pr["ea"], i32)
+            T_("pe_b", pr["eb"], i32)
+            T_("pe_ch", pr["ch"], i32)
+            T_("ch_p", pr["p"], f64)
+            T_("ch_ref", np.asarray(pr["ref"], np.float64).reshape(-1, 2), f64)
         if af is not None:
             T_("a_node", af["node"], i32)
             T_("a_grp", af["grp"], i32)
@@ -277,6 +313,7 @@ class DeviceSolver:
         d.n_scenes, d.N, d.T, d.Nb, d.Ne, d.n_bc, d.n_col = B, N, T, Nb, Ne, len(bc_sorted), len(cols)
         d.n_aff, d.n_affn, d.n_rig, d.n_rign, d.n_ten, d.n_tent = n_aff, n_affn, n_rig, n_rign, n_ten, n_tent
         d.cand_total, d.max_nb = cand_total, max_nb
+        d.n_sp, d.n_pe, d.n_ch = n_sp, n_pe, n_ch
         for name, _ in _lib.DESC_FIELDS:
             if _ is C.c_void_p and name in self._t:
                 setattr(d, name, self._t[name].data_ptr())
@@ -350,6 +387,31 @@ class DeviceSolver:
             self._t["t_Tcmd"].copy_(torch.as_tensor(np.asarray(Tcmd, np.float64)[self.ten_order]))
         if L0 is not None:
             self._t["t_L0"].copy_(torch.as_tensor(np.asarray(L0, np.float64)[self.ten_order]))
+
+    def set_pressures(self, p):
+        """Gauge pressure of every chamber [Pa], in the model's chamber order."""
+        if self.pr is None:
+            return
+        self._t["ch_p"].copy_(torch.as_tensor(np.asarray(p, np.float64)))
+
+    def set_springs(self, anchor=None, L0=None):
+        """World anchors ((n, 2)) and rest lengths of the springs, in the model's order."""
+        if self.sp_order is None:
+            return
+        if anchor is not None:
+            a = np.asarray(anchor, np.float64).reshape(-1, 2)[self.sp_order]
+            self._t["sp_anchor"].copy_(torch.as_tensor(a))
+        if L0 is not None:
+            self._t["sp_L0"].copy_(torch.as_tensor(np.asarray(L0, np.float64)[self.sp_order]))
+
+    def set_rest_shape(self, Bm, area, Dm):
+        """Every triangle's rest-shape inverse, rest area and rest edge vectors (the active
+        regions' rest-shape change; ActiveStrain.set, implicit/actuation.py:335-341)."""
+        T = self.desc.T
+        self._t["Bm"].copy_(torch.as_tensor(np.asarray(Bm, np.float64).reshape(T, 4)))
+        self._t["area"].copy_(torch.as_tensor(np.asarray(area, np.float64)))
+        if "Dm" in self._t:
+            self._t["Dm"].copy_(torch.as_tensor(np.asarray(Dm, np.float64).reshape(T, 4)))
 
     # ---- state
     def get_x(self):

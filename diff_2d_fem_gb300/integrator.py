@@ -112,18 +112,41 @@ class ImplicitIntegrator:
         return s
 
     def _sync_actuation(self, model):
-        """Push the commands that changed since the last step: force field (gravity folded
-        in), tendon tensions and lengths (implicit/integrator.py:151-229)."""
+        """Rebuild the solver when an actuator was added (from the current state), and push
+        the commands that changed since the last step: force field (gravity folded in),
+        chamber pressures, tendon tensions and lengths, active-region rest shapes, spring
+        anchors and lengths (implicit/integrator.py:151-229)."""
         s = model._solver
-        if s._act_version != model._act_version:
-            raise RuntimeError("actuators were added after the first simulate(); add them before")
+        f = _scene.external_force(model) if s._ctrl_version != model._ctrl_version else None
+        # a term the solver was built without (an actuator, or a first force field): rebuild
+        if s._act_version != model._act_version or (f is not None and "fext" not in s._t):
+            model._x_host, model._v0 = s.get_x(), s.get_v()
+            dt = s.dt
+            s.close()
+            model._solver = None
+            self._build(model, dt)
+            s = model._solver
         if s._ctrl_version != model._ctrl_version:
-            f = _scene.external_force(model)
             if f is not None:
                 s.set_fext(f)
+            if model._chambers:
+                s.set_pressures([c["pressure"] for c in model._chambers])
             if model._tendons:
                 s.set_tendons([t["tension"] for t in model._tendons], [t["length"] for t in model._tendons])
+            if model._regions:
+                s.set_rest_shape(*_scene.rest_shape(model))
+            if model._springs:
+                s.set_springs([k["anchor"] for k in model._springs], [k["length"] for k in model._springs])
             s._ctrl_version = model._ctrl_version
+
+    def adjoint(self, model, dt, Emin=1e-3):
+        """Adjoint of the implicit solve on this model (implicit/integrator.py:231-250): an
+        AdjointPNCG2D over its FP64 solver. Density scales each element's stiffness,
+        E(rho) = Emin + rho (1 - Emin); transient_adjoint refuses to run while the model has
+        actuators the adjoint operator has no tangent for (pressure, springs, active
+        material) or IPC contact between bodies."""
+        from .adjoint import AdjointPNCG2D
+        return AdjointPNCG2D(self.attach(model, dt), Emin=Emin, model=model)
 
     def _build(self, model, dt):
         from .device import DeviceSolver

@@ -25,6 +25,7 @@ from typing import Optional
 
 import numpy as np
 
+from . import actuators as _act
 from . import mesh as _mesh
 
 DISC, ELLIPSE, BOX, TRIANGLE, HALFSPACE = 0, 1, 2, 3, 4
@@ -64,6 +65,10 @@ class Model:
         self._gravity = (0.0, 0.0)
         self._fext = None
         self._tendons = []
+        self._chambers = []
+        self._springs = []
+        self._regions = []
+        self._regions_of = {}
         self._affine = []
         self._affine_of = {}
         self._extra_excl = []
@@ -489,6 +494,193 @@ class Model:
         if t["stiffness"] <= 0:
             raise ValueError("this tendon is tension-controlled; use set_tendon_tension")
         t["length"] = float(length)
+        self._ctrl_version += 1
+
+    def tendon_length(self, tendon):
+        """Current path length of a cable through its eyelets [m]."""
+        x = self.get_x()[self._tendons[tendon]["nodes"]]
+        return float(np.linalg.norm(np.diff(x, axis=0), axis=1).sum())
+
+    def tendon_tension(self, tendon):
+        """Current tension of a cable [N/m] (zero when a length-controlled cable is slack)."""
+        t = self._tendons[tendon]
+        if t["stiffness"] > 0:
+            return t["stiffness"] * max(self.tendon_length(tendon) - t["length"], 0.0)
+        return max(t["tension"], 0.0)
+
+    # ---- pneumatic / hydraulic: pressure in sealed cavities (sim_model.py:825-929)
+    def _node_of(self, handle):
+        """Vectorised (ix, iy) grid corner -> global node id (or -1) of a pixel body."""
+        me = self.me
+        base, ny = int(me.body_node_range[handle][0]), int(me.body_grid[handle][1])
+        live = np.asarray(me.grid_to_live_node_per_body[handle])
+
+        def node_of(ix, iy):
+            loc = live[(ny + 1) * np.asarray(ix, np.int64) + np.asarray(iy, np.int64)]
+            return np.where(loc < 0, -1, base + loc)
+        return node_of
+
+    def add_pressure_chambers(self, handle, min_pixels=1):
+        """Make every sealed cavity of a body (a void region enclosed by solid, not reaching the
+        edge of the pixel grid) a pressure chamber. Returns their handles, ordered by the
+        cavity's first pixel, bottom row first then left to right."""
+        self._need_mesh()
+        mask = self._bodies[handle]["mask"]
+        lab, ids = _act.enclosed_voids(mask)
+        ids = [k for k in ids if (lab == k).sum() >= min_pixels]
+        ids.sort(key=lambda k: tuple(np.argwhere(lab == k)[0]))
+        return [self._add_chamber(handle, lab, k) for k in ids]
+
+    def add_pressure_chamber(self, handle, at):
+        """Make the sealed cavity holding the world point `at` a pressure chamber."""
+        self._need_mesh()
+        b = self._bodies[handle]
+        mask = b["mask"]
+        px = _act.pixel_of(at, b["size"], b["center"], mask.shape)
+        if px is None or mask[px] > 0:
+            raise ValueError(f"point {tuple(at)} is not inside a void of this body")
+        lab, ids = _act.enclosed_voids(mask)
+        if lab[px] not in ids:
+            raise ValueError(f"the void at {tuple(at)} is open to the outside, not a sealed cavity")
+        return self._add_chamber(handle, lab, int(lab[px]))
+
+    def add_ambient_pressure(self, handle):
+        """A pressure on a body's outer surface (its outline, including channels open to the
+        outside); positive squeezes the body. Returns a handle used with set_pressure."""
+        self._need_mesh()
+        mask = self._bodies[handle]["mask"]
+        lab, ids = _act.enclosed_voids(mask)
+        ea, eb = _act.exterior_edges(mask, lab, ids, self._node_of(handle))
+        n_px = int((mask > 0).sum() + sum((lab == k).sum() for k in ids))
+        pw, ph = self.pixel_size(handle)
+        return self._register_chamber(handle, ea, eb, n_px * pw * ph, sign=-1.0)
+
+    def _add_chamber(self, handle, lab, label):
+        ea, eb = _act.chamber_edges(self._bodies[handle]["mask"], lab, label, self._node_of(handle))
+        pw, ph = self.pixel_size(handle)
+        return self._register_chamber(handle, ea, eb, int((lab == label).sum()) * pw * ph, sign=1.0)
+
+    def _register_chamber(self, handle, ea, eb, expect, sign):
+        """sign +1: edges counter-clockwise round a cavity; -1: clockwise round the body. The
+        edges must enclose `expect` m^2 (the closure and orientation check)."""
+        rest = self.me.rest_pos
+        ref = rest[np.concatenate([ea, eb])].mean(0)
+        got = sign * _act.loop_area(rest, ea, eb, ref)
+        if not expect > 0 or abs(got - expect) > 1e-6 * expect:
+            raise RuntimeError(f"pressure boundary encloses {got:.6e} m^2, expected {expect:.6e}")
+        self._chambers.append(dict(body=handle, ea=np.asarray(ea, np.int64), eb=np.asarray(eb, np.int64),
+                                   ref=np.asarray(ref, np.float64), area0=float(expect), sign=sign,
+                                   pressure=0.0))
+        self._act_version += 1
+        return len(self._chambers) - 1
+
+    def set_pressure(self, chamber, pressure):
+        """Gauge pressure of the fluid in a chamber [Pa]. Positive inflates a cavity (and
+        squeezes a body through an ambient-pressure handle)."""
+        self._chambers[chamber]["pressure"] = float(pressure)
+        self._ctrl_version += 1
+
+    def chamber_area(self, chamber):
+        """Current area inside a pressure boundary [m^2]: a cavity's volume per unit depth; for
+        an ambient-pressure handle, the area inside the body's outline."""
+        c = self._chambers[chamber]
+        return c["sign"] * _act.loop_area(self.get_x(), c["ea"], c["eb"], c["ref"])
+
+    # ---- springs, pins and joints (sim_model.py:988-1066)
+    def _nearest(self, handle, point):
+        ids = self._node_range[handle]
+        d = np.linalg.norm(self.me.rest_pos[ids] - np.asarray(point, np.float64)[None, :], axis=1)
+        return int(ids[d.argmin()])
+
+    def add_spring(self, handle_a, point_a, handle_b=None, point_b=None, stiffness=None, rest_length=None):
+        """A linear spring from a point of one body to a point of another, or with
+        handle_b=None to a point fixed in the world (point_b, default where point_a snapped
+        to). Ends snap to the nearest node of their body. stiffness k [Pa] (default
+        model.rigid_young); rest_length None keeps the built length. Returns a handle."""
+        self._need_mesh()
+        ia = self._nearest(handle_a, point_a)
+        if handle_b is None:
+            ib = -1
+            anchor = np.asarray(self.me.rest_pos[ia] if point_b is None else point_b, np.float64)
+        else:
+            ib = self._nearest(handle_b, point_a if point_b is None else point_b)
+            if self.body_env(handle_a) != self.body_env(handle_b):
+                raise ValueError("a spring cannot join bodies of different environments")
+            if ib == ia:
+                raise ValueError("both ends of the spring snapped to the same node")
+            anchor = np.asarray(self.me.rest_pos[ib], np.float64)
+        L = float(np.linalg.norm(self.me.rest_pos[ia] - anchor)) if rest_length is None else float(rest_length)
+        if handle_b is not None and L <= 0.0:
+            raise ValueError("a spring between two bodies needs a rest length: at zero it would "
+                             "pull two nodes to one place while contact holds the bodies apart")
+        k = float(self.rigid_young if stiffness is None else stiffness)
+        if k <= 0 or L < 0:
+            raise ValueError("spring stiffness must be positive and its rest length non-negative")
+        self._springs.append(dict(a=int(ia), b=int(ib), stiffness=k, length=L, anchor=anchor,
+                                  env=self.body_env(handle_a)))
+        self._act_version += 1
+        return len(self._springs) - 1
+
+    def add_pin(self, handle, point, handle_b=None, stiffness=None):
+        """Pin a point of a body to the world where it is (a zero-length stiff spring): the
+        body can still turn about it."""
+        if handle_b is not None:
+            raise NotImplementedError(
+                "a pin between two bodies is not supported: it would hold two nodes at one "
+                "place while contact holds the bodies apart. Pin to the world (leave handle_b "
+                "out), or use add_spring with a rest length.")
+        return self.add_spring(handle, point, None, point, stiffness, rest_length=0.0)
+
+    def set_spring_length(self, spring, length):
+        """Rest length of a spring [m] (drive it for a linear actuator)."""
+        self._springs[spring]["length"] = float(length)
+        self._ctrl_version += 1
+
+    def set_spring_anchor(self, spring, point):
+        """Move the world end of a world spring or pin."""
+        if self._springs[spring]["b"] >= 0:
+            raise ValueError("this spring joins two bodies and has no world anchor")
+        self._springs[spring]["anchor"] = np.asarray(point, np.float64)
+        self._ctrl_version += 1
+
+    def spring_force(self, spring):
+        """(tension [N/m], negative in compression; current length [m]) of a spring."""
+        sp = self._springs[spring]
+        x = self.get_x()
+        ln = float(np.linalg.norm(x[sp["a"]] - (x[sp["b"]] if sp["b"] >= 0 else sp["anchor"])))
+        return sp["stiffness"] * (ln - sp["length"]), ln
+
+    # ---- active material (sim_model.py:1068-1096)
+    def add_active_region(self, handle, region, fiber=None):
+        """Mark part of a body ((H, W) boolean map laid out like its mask) as actively
+        deforming material; fiber None for isotropic change, else an angle [rad] or a
+        2-vector along which `stretch` acts. Returns a handle."""
+        self._need_mesh()
+        b = self._bodies[handle]
+        region = np.asarray(region) > 0
+        if region.shape != b["mask"].shape:
+            raise ValueError(f"region is {region.shape}, the mask is {b['mask'].shape}")
+        H = b["mask"].shape[0]
+        tris = self._tri_range[handle]
+        q = np.asarray(self.me.tri_quad)[tris]
+        elems = tris[region[q % H, q // H]]
+        if len(elems) == 0:
+            raise ValueError("the region contains no solid pixel of this body")
+        mine = self._regions_of.setdefault(handle, [])
+        if mine and np.intersect1d(elems, np.concatenate(mine)).size:
+            raise ValueError("active regions must not overlap")
+        mine.append(np.asarray(elems, np.int64))
+        self._regions.append(dict(body=handle, elems=np.asarray(elems, np.int64), fiber=fiber, A=np.eye(2)))
+        self._act_version += 1
+        return len(self._regions) - 1
+
+    def set_activation(self, region, stretch, transverse=1.0):
+        """Rest-length ratio of an active region: 1 passive, 0.9 a 10 % contraction; along
+        the fiber with `transverse` across it, or isotropic without a fiber."""
+        if stretch <= 0 or transverse <= 0:
+            raise ValueError("stretch ratios must be positive")
+        r = self._regions[region]
+        r["A"] = _act.activation_matrix(stretch, transverse, r["fiber"])
         self._ctrl_version += 1
 
     def affine_state(self, index):

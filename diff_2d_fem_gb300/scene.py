@@ -156,6 +156,51 @@ def _tendon_arrays(model):
                 Tcmd=np.asarray([t["tension"] for t in T], np.float64))
 
 
+def _spring_arrays(model):
+    """Springs and pins (implicit/actuation.py:381-476): node b = -1 ties node a to `anchor`."""
+    S = model._springs
+    return dict(a=np.asarray([k["a"] for k in S], np.int64), b=np.asarray([k["b"] for k in S], np.int64),
+                k=np.asarray([k["stiffness"] for k in S], np.float64),
+                L0=np.asarray([k["length"] for k in S], np.float64),
+                anchor=np.asarray([k["anchor"] for k in S], np.float64).reshape(-1, 2),
+                env=np.asarray([k["env"] for k in S], np.int64))
+
+
+def _pressure_arrays(model):
+    """Pressure boundaries (implicit/actuation.py:80-152): every chamber's directed edges
+    (fluid on the left), its environment, gauge pressure and shoelace reference point."""
+    Cs = model._chambers
+    return dict(ea=np.concatenate([c["ea"] for c in Cs]).astype(np.int64),
+                eb=np.concatenate([c["eb"] for c in Cs]).astype(np.int64),
+                ch=np.concatenate([np.full(len(c["ea"]), i) for i, c in enumerate(Cs)]).astype(np.int64),
+                ch2env=np.asarray([model.body_env(c["body"]) for c in Cs], np.int64),
+                p=np.asarray([c["pressure"] for c in Cs], np.float64),
+                ref=np.asarray([c["ref"] for c in Cs], np.float64).reshape(-1, 2))
+
+
+def rest_shape(model):
+    """(Bm, area, Dm) of every triangle with the active regions' rest-shape change A applied
+    (ActiveStrain, implicit/actuation.py:318-345): the rest edge vectors become A Dm0, so
+    Bm = Bm0 A^-1 and area = area0 det A. Dm: (T, 4) rest edge vectors (e1x, e1y, e2x, e2y)."""
+    me = model.me
+    Bm0 = np.asarray(me.D_m_inv, np.float64)
+    shape = Bm0.shape
+    Bm = Bm0.reshape(-1, 2, 2).copy()
+    area = np.asarray(me.rest_area, np.float64).copy()
+    rest = np.asarray(me.rest_pos, np.float64)
+    tri = np.asarray(me.tri, np.int64)
+    e1, e2 = rest[tri[:, 1]] - rest[tri[:, 0]], rest[tri[:, 2]] - rest[tri[:, 0]]
+    for r in model._regions:
+        A = np.asarray(r["A"], np.float64)
+        if np.array_equal(A, np.eye(2)):
+            continue
+        el = r["elems"]
+        Bm[el] = Bm[el] @ np.linalg.inv(A)
+        area[el] = area[el] * np.linalg.det(A)
+        e1[el], e2[el] = e1[el] @ A.T, e2[el] @ A.T
+    return Bm.reshape(shape), area, np.concatenate([e1, e2], 1)
+
+
 def external_force(model):
     """The ExternalForce field f = fext + m g (implicit/integrator.py:205-211), or None."""
     g = model._gravity
@@ -188,7 +233,7 @@ def solver_problem(model, integ, dt):
         B=int(me.n_envs), x=x, v=v, rest=np.asarray(me.rest_pos, np.float64),
         mass=np.asarray(me.mass, np.float64), free=free,
         node2env=np.asarray(me.node2env, np.int64), tri=np.asarray(me.tri, np.int64),
-        Bm=np.asarray(me.D_m_inv, np.float64), area=np.asarray(me.rest_area, np.float64),
+        Bm=None, area=None,
         mu=mu_s, lam=lam_s, tri2env=np.asarray(me.tri2env, np.int64),
         bnd=np.asarray(me.boundary_nodes, np.int64), b2e=np.asarray(me.boundary2env, np.int64),
         bc_idx=np.asarray(bc, np.int64),
@@ -200,6 +245,7 @@ def solver_problem(model, integ, dt):
         area_shrink=integ.area_shrink, ccd_eta=integ.ccd_eta, ls_tol=integ.ls_tol, gtol=integ.gtol,
         iter_max=iters_for(model, integ, dt), conv_check=integ.conv_check, friction=int(integ.friction),
         line_search=int(integ.line_search), n_bt=integ.n_backtrack)
+    prob["Bm"], prob["area"], prob["Dm"] = rest_shape(model)
     if model._col_mu_env:
         cm = np.repeat(prob["colliders"][None, :, 7], prob["B"], axis=0)
         for k, arr in model._col_mu_env.items():
@@ -216,6 +262,11 @@ def solver_problem(model, integ, dt):
         prob["fext"] = f
     if model._tendons:
         prob["tendon"] = _tendon_arrays(model)
+    if model._springs:
+        prob["springs"] = _spring_arrays(model)
+    if model._chambers:
+        prob["pressure"] = _pressure_arrays(model)
+    prob["active_regions"] = len(model._regions)
     prob["cg_guard"] = float((0.5 if ipc is not None else 0.0) if integ.cg_restart is None else integ.cg_restart)
     if integ.rigid_modes:
         rg = _rigid_arrays(model, free, slaved)
@@ -297,8 +348,9 @@ def subset_problem(prob, envs):
             out[k] = np.asarray(prob[k])[keep_n]
     out["node2env"] = newenv[node2env[keep_n]]
     out["tri"] = nmap[np.asarray(prob["tri"], np.int64)[keep_t]]
-    for k in ("Bm", "area", "mu", "lam"):
-        out[k] = np.asarray(prob[k])[keep_t]
+    for k in ("Bm", "area", "mu", "lam", "Dm"):
+        if prob.get(k) is not None:
+            out[k] = np.asarray(prob[k])[keep_t]
     out["tri2env"] = newenv[tri2env[keep_t]]
     out["bnd"] = nmap[np.asarray(prob["bnd"], np.int64)[keep_b]]
     out["b2e"] = newenv[b2e[keep_b]]
@@ -336,7 +388,7 @@ def subset_problem(prob, envs):
         kn = np.nonzero(pmap[grp] >= 0)[0]
         kn = kn[np.argsort(pmap[grp[kn]], kind="stable")]
         out["rigid"] = dict(node=nmap[np.asarray(rg["node"], np.int64)[kn]], grp=pmap[grp[kn]], env=newenv[renv[kp]])
-    for key in ("affine", "tendon"):
+    for key in ("affine", "tendon", "springs", "pressure"):
         if prob.get(key) is not None:
             raise NotImplementedError(f"subset_problem: {key} terms are not sliced")
     return out

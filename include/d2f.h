@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define D2F_ABI_VERSION 4
+#define D2F_ABI_VERSION 5
 
 /* status codes */
 #define D2F_OK 0
@@ -53,6 +53,8 @@ typedef struct d2f_seg {
     int32_t rign0, nrign;   /* rigid-mode piece node entries */
     int32_t ten0, nten;     /* tendons */
     int32_t tent0, ntent;   /* tendon eyelet entries */
+    int32_t sp0, nsp;       /* springs and pins */
+    int32_t pe0, npe;       /* pressure boundary edges */
 } d2f_seg;
 
 /* Everything one solver needs. Pointers are device pointers unless noted; arrays of
@@ -84,7 +86,8 @@ typedef struct d2f_scene_desc {
     const int32_t *tri;          /* T x 3 */
     const void *Bm;              /* T x 4 real: rest-shape inverse, row-major */
     const void *area, *mu, *lam; /* T real */
-    const void *Dm;              /* T x 4 real: rest edge vectors X1-X0, X2-X0 (mixed; else NULL) */
+    const double *Dm;            /* T x 4: rest edge vectors X1-X0, X2-X0 (after any active-strain
+                                    rest-shape change; mixed; else NULL) */
     void *escr;                  /* T x 12 real: per-corner gradient and diagonal */
     void *ecache;                /* T x 9 real: F^-T, la log J - mu, edge vectors */
     void *mscr;                  /* mixed precision: per-step scratch of d2f_mixed_scratch_bytes() bytes; else NULL */
@@ -140,6 +143,18 @@ typedef struct d2f_scene_desc {
                                     else 1) */
     const int32_t *a_ptr;        /* n_aff + 1: affine body b owns entries a_ptr[b] .. a_ptr[b+1]-1 of
                                     a_node / a_grp / a_w (required with affine bodies) */
+    /* springs and pins (Springs, implicit/actuation.py:381-476): E = k/2 (|x_a - x_b| - L0)^2,
+       x_b the node sp_b, or the world point sp_anchor where sp_b = -1 */
+    int32_t n_sp;
+    const int32_t *sp_a, *sp_b;  /* n_sp (global node ids) */
+    const double *sp_k, *sp_L0;  /* n_sp: stiffness [Pa], rest length [m] */
+    const double *sp_anchor;     /* n_sp x 2 */
+    /* pressure boundaries (Pressure, implicit/actuation.py:80-152): E = -p A, A the shoelace
+       area inside a chamber's directed edges (fluid on the left) */
+    int32_t n_pe, n_ch;
+    const int32_t *pe_a, *pe_b, *pe_ch; /* n_pe: edge start / end node, chamber (global ids) */
+    const double *ch_p;          /* n_ch: gauge pressure [Pa] */
+    const double *ch_ref;        /* n_ch x 2: the shoelace sum's reference point (energy) */
 } d2f_scene_desc;
 
 typedef struct d2f_solver d2f_solver;

@@ -64,6 +64,10 @@ _FIELDS = [
     ("r_node", _PI), ("r_grp", _PI), ("r_env", _PI),
     ("r_acc", _PD), ("r_gq", _PD), ("r_gq_prev", _PD), ("r_zq", _PD), ("r_Hc", _PD),
     ("diag_el", _PD),
+    ("n_spring", _I), ("sp_a", _PI), ("sp_b", _PI), ("sp2env", _PI),
+    ("sp_k", _PD), ("sp_L0", _PD), ("sp_anchor", _PD),
+    ("n_pedge", _I), ("n_chamber", _I), ("pe_a", _PI), ("pe_b", _PI), ("pe_ch", _PI), ("ch2env", _PI),
+    ("ch_p", _PD), ("ch_ref", _PD),
 ]
 
 
@@ -82,6 +86,8 @@ def lib():
         _LIB.d2o_energy.restype = None
         _LIB.d2o_ipc_energy.argtypes = [C.POINTER(_Solver), _PD]
         _LIB.d2o_ipc_energy.restype = None
+        _LIB.d2o_term.argtypes = [C.POINTER(_Solver), C.c_int, _PD]
+        _LIB.d2o_term.restype = None
     return _LIB
 
 
@@ -222,6 +228,26 @@ class OracleSolver:
             s.a_Hx = state("a_Hx", (na, 9))
             s.a_Hy = state("a_Hy", (na, 9))
 
+        sp = prob.get("springs")
+        if sp is not None and len(sp["env"]):
+            s.n_spring = len(sp["env"])
+            s.sp_a, _ = P(sp["a"], "i")
+            s.sp_b, _ = P(sp["b"], "i")
+            s.sp2env, _ = P(sp["env"], "i")
+            s.sp_k, _ = P(sp["k"])
+            s.sp_L0 = state("sp_L0", (s.n_spring,), sp["L0"])
+            s.sp_anchor = state("sp_anchor", (s.n_spring, 2), sp["anchor"])
+
+        pr = prob.get("pressure")
+        if pr is not None and len(pr["ea"]):
+            s.n_pedge, s.n_chamber = len(pr["ea"]), len(pr["ch2env"])
+            s.pe_a, _ = P(pr["ea"], "i")
+            s.pe_b, _ = P(pr["eb"], "i")
+            s.pe_ch, _ = P(pr["ch"], "i")
+            s.ch2env, _ = P(pr["ch2env"], "i")
+            s.ch_p = state("ch_p", (s.n_chamber,), pr["p"])
+            s.ch_ref = state("ch_ref", (s.n_chamber, 2), pr["ref"])
+
         rg = prob.get("rigid")
         if rg is not None and len(rg["env"]):
             nr, nn = len(rg["env"]), len(rg["node"])
@@ -245,6 +271,30 @@ class OracleSolver:
             self.state["t_Tcmd"][:] = np.asarray(Tcmd, np.float64)
         if L0 is not None:
             self.state["t_L0"][:] = np.asarray(L0, np.float64)
+
+    def term(self, which, x, p=None, xn=None):
+        """One actuation term alone (which: "springs" or "pressure") at positions x:
+        (gradient (N, 2), diagonal (N, 2), curvature along p per environment, energy per
+        environment) — for derivative checks."""
+        st = self.state
+        st["x"][:] = np.asarray(x, np.float64)
+        if xn is not None:
+            st["xn"][:] = np.asarray(xn, np.float64)
+        st["p"][:] = 0.0 if p is None else np.asarray(p, np.float64)
+        E = np.zeros(int(self.s.B))
+        lib().d2o_term(C.byref(self.s), {"springs": 0, "pressure": 1}[which], E.ctypes.data_as(_PD))
+        return st["grad"].copy(), st["diagH"].copy(), st["pHp"].copy(), E
+
+    def set_pressure(self, p):
+        """Gauge pressure of every chamber [Pa]."""
+        self.state["ch_p"][:] = np.asarray(p, np.float64)
+
+    def set_springs(self, anchor=None, L0=None):
+        """World anchors (n, 2) and rest lengths of the springs."""
+        if anchor is not None:
+            self.state["sp_anchor"][:] = np.asarray(anchor, np.float64).reshape(-1, 2)
+        if L0 is not None:
+            self.state["sp_L0"][:] = np.asarray(L0, np.float64)
 
     def set_fext(self, f):
         self.state["fext"][:] = np.asarray(f, np.float64).reshape(-1, 2)
@@ -301,7 +351,8 @@ def run(prob: dict, steps: int, commands=None):
 
 def problem_keys():
     return ["B", "x", "v", "mass", "free", "node2env", "tri", "Bm", "area", "mu", "lam", "tri2env",
-            "bnd", "b2e", "bc_idx", "colliders", "fext", "ipc", "tendon", "affine", "rigid"] + list(SCALARS)
+            "bnd", "b2e", "bc_idx", "colliders", "fext", "ipc", "tendon", "affine", "rigid", "springs",
+            "pressure"] + list(SCALARS)
 
 
 os.environ.setdefault("OMP_NUM_THREADS", "1")

@@ -1158,6 +1158,80 @@ static void set_x_from_x0(d2o_solver *s) {
 }
 
 /* ------------------------------------------------------------------ energy, solver.py:453-498 */
+/* ------------------------------------------------------------------ Springs, implicit/actuation.py:381-476 */
+typedef struct { double ten, kt, len; v2 n; } spring_at_t;
+/* _spring (:396-402): tension k (|d| - L0), tangential stiffness max(k (1 - L0/|d|), 0) */
+static spring_at_t spring_at(const d2o_solver *s, int k) {
+    int a = s->sp_a[k], b = s->sp_b[k];
+    v2 xb = b >= 0 ? ld(s->x, b) : ld(s->sp_anchor, k);
+    v2 d = sub(ld(s->x, a), xb);
+    double ln = sqrt(dot(d, d) + 1.0e-30);
+    spring_at_t r;
+    r.ten = s->sp_k[k] * (ln - s->sp_L0[k]);
+    r.kt = fmax_(s->sp_k[k] * (1.0 - s->sp_L0[k] / ln), 0.0);
+    r.len = ln;
+    r.n = vdiv(d, ln);
+    return r;
+}
+static void spring_grad(d2o_solver *s) {  /* grad_diag_spring_kernel, :405-424 */
+    for (int k = 0; k < s->n_spring; ++k) {
+        spring_at_t r = spring_at(s, k);
+        int a = s->sp_a[k], b = s->sp_b[k];
+        double kk = s->sp_k[k];
+        v2 g = scl(s->h2 * r.ten, r.n);
+        v2 hd = V(s->h2 * (kk * r.n.x * r.n.x + r.kt * (1.0 - r.n.x * r.n.x)),
+                  s->h2 * (kk * r.n.y * r.n.y + r.kt * (1.0 - r.n.y * r.n.y)));
+        atomic_add2(s->grad, a, g);
+        atomic_add2(s->diagH, a, hd);
+        if (b >= 0) {
+            atomic_add2(s->grad, b, scl(-1.0, g));
+            atomic_add2(s->diagH, b, hd);
+        }
+    }
+}
+static void spring_pHp(d2o_solver *s) {  /* pHp_spring_kernel, :427-444 */
+    for (int k = 0; k < s->n_spring; ++k) {
+        spring_at_t r = spring_at(s, k);
+        int a = s->sp_a[k], b = s->sp_b[k];
+        v2 dp = ld(s->p, a);
+        if (b >= 0) dp = sub(dp, ld(s->p, b));
+        double along = dot(dp, r.n);
+        s->pHp[s->sp2env[k]] += s->h2 * (s->sp_k[k] * along * along + r.kt * (dot(dp, dp) - along * along));
+    }
+}
+static void spring_energy(d2o_solver *s, double *E) {  /* energy_spring_kernel, :447-456 */
+    for (int k = 0; k < s->n_spring; ++k) {
+        spring_at_t r = spring_at(s, k);
+        double ext = r.len - s->sp_L0[k];
+        E[s->sp2env[k]] += 0.5 * s->h2 * s->sp_k[k] * ext * ext;
+    }
+}
+/* ------------------------------------------------------------------ Pressure, implicit/actuation.py:80-152 */
+static void pressure_grad(d2o_solver *s) {  /* grad_pressure_kernel, :98-108 */
+    for (int e = 0; e < s->n_pedge; ++e) {
+        int a = s->pe_a[e], b = s->pe_b[e];
+        v2 t = sub(ld(s->x, b), ld(s->x, a));
+        v2 g = scl(-0.5 * s->h2 * s->ch_p[s->pe_ch[e]], V(t.y, -t.x));
+        atomic_add2(s->grad, a, g);
+        atomic_add2(s->grad, b, g);
+    }
+}
+static void pressure_pHp(d2o_solver *s) {  /* pHp_pressure_kernel, :111-118 */
+    for (int e = 0; e < s->n_pedge; ++e) {
+        int c = s->pe_ch[e];
+        v2 pa = ld(s->p, s->pe_a[e]), pb = ld(s->p, s->pe_b[e]);
+        s->pHp[s->ch2env[c]] += -s->h2 * s->ch_p[c] * (pa.x * pb.y - pa.y * pb.x);
+    }
+}
+static void pressure_energy(d2o_solver *s, double *E) {  /* energy_pressure_kernel, :121-130 */
+    for (int e = 0; e < s->n_pedge; ++e) {
+        int c = s->pe_ch[e];
+        v2 ref = ld(s->ch_ref, c);
+        v2 ra = sub(ld(s->x, s->pe_a[e]), ref), rb = sub(ld(s->x, s->pe_b[e]), ref);
+        E[s->ch2env[c]] += -s->h2 * s->ch_p[c] * 0.5 * (ra.x * rb.y - ra.y * rb.x);
+    }
+}
+
 static void energy_into(d2o_solver *s, double *E) {
     for (int e = 0; e < s->B; ++e) E[e] = 0.0;
     for (int i = 0; i < s->N; ++i) {  /* energy_kernel, kernels.py:445-452 */
@@ -1217,10 +1291,13 @@ static void energy_into(d2o_solver *s, double *E) {
             }
         }
     }
-    /* terms in the reference's order: ExternalForce, AffineBodies, IPCContact, Tendon */
+    /* terms in the reference's order (implicit/integrator.py:151-229): ExternalForce,
+       AffineBodies, IPCContact, Springs, Pressure, Tendon */
     if (s->has_ext) ext_energy(s, E);
     if (s->n_aff) affine_energy(s, E);
     if (s->has_ipc) { ipc_launch L = ipc_base(s, 2, s->p, E, s->clr_min, s->alpha); ipc_pair(&L); }
+    if (s->n_spring) spring_energy(s, E);
+    if (s->n_pedge) pressure_energy(s, E);
     if (s->n_tendon) tendon_energy(s, E);
 }
 void d2o_energy(d2o_solver *s, double *buf) { energy_into(s, buf); }
@@ -1231,6 +1308,17 @@ void d2o_ipc_energy(d2o_solver *s, double *buf) {
     if (!s->has_ipc) return;
     ipc_launch L = ipc_base(s, 2, s->p, buf, s->clr_min, s->alpha);
     ipc_pair(&L);
+}
+
+/* One actuation term alone at s->x (which: 0 Springs, 1 Pressure): its gradient and diagonal
+   into s->grad / s->diagH and its curvature along s->p into s->pHp (all zeroed first), its
+   energy per environment into E — the derivative checks of tests/test_actuation.py. */
+void d2o_term(d2o_solver *s, int which, double *E) {
+    memset(s->grad, 0, sizeof(double) * 2 * s->N);
+    memset(s->diagH, 0, sizeof(double) * 2 * s->N);
+    for (int e = 0; e < s->B; ++e) { s->pHp[e] = 0.0; E[e] = 0.0; }
+    if (which == 0) { spring_grad(s); spring_pHp(s); spring_energy(s, E); }
+    else { pressure_grad(s); pressure_pHp(s); pressure_energy(s, E); }
 }
 
 /* ------------------------------------------------------------------ the loop, solver.py:252-425 */
@@ -1262,6 +1350,8 @@ static void iterate(d2o_solver *s) {
             }
         if (s->has_ext) ext_grad(s);
         if (s->has_ipc) { ipc_launch L = ipc_base(s, 0, s->p, s->Ener, s->clr_min, s->alpha); ipc_pair(&L); }
+        if (s->n_spring) spring_grad(s);
+        if (s->n_pedge) pressure_grad(s);
         if (s->n_tendon) tendon_grad(s);
         if (s->n_aff) affine_gather(s);
         if (s->n_rig) rigid_gather(s);
@@ -1297,6 +1387,8 @@ static void iterate(d2o_solver *s) {
             ipc_pair(&L);
             ipc_far_cap(s, s->p_inf, s->alpha);
         }
+        if (s->n_spring) spring_pHp(s);
+        if (s->n_pedge) pressure_pHp(s);
         if (s->n_tendon) tendon_pHp(s);
         inversion_alpha(s);
         for (int k = 0; k < s->n_col; ++k) {

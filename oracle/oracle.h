@@ -80,6 +80,17 @@ typedef struct {
     const int32_t *r_node, *r_grp, *r_env;
     double *r_acc, *r_gq, *r_gq_prev, *r_zq, *r_Hc; /* n_rig x 3 / x 9 */
     double *diag_el;                                /* N x 2 */
+
+    /* ---- Springs term (n_spring > 0): node b = -1 ties node a to the world point anchor */
+    int32_t n_spring;
+    const int32_t *sp_a, *sp_b, *sp2env;            /* n_spring */
+    double *sp_k, *sp_L0, *sp_anchor;               /* n_spring, n_spring, n_spring x 2 */
+
+    /* ---- Pressure term (n_pedge > 0): directed chamber edges, fluid on the left */
+    int32_t n_pedge, n_chamber;
+    const int32_t *pe_a, *pe_b, *pe_ch;             /* n_pedge */
+    const int32_t *ch2env;                          /* n_chamber */
+    double *ch_p, *ch_ref;                          /* n_chamber, n_chamber x 2 */
 } d2o_solver;
 
 /* One implicit step (PNCG2DSolver.step_targets), bc_target already set. */
@@ -89,6 +100,9 @@ int d2o_step(d2o_solver *s);
 /* Per-env total energy (PNCG2DSolver._energy_into) into s->Ener. */
 void d2o_energy(d2o_solver *s, double *buf);
 void d2o_ipc_energy(d2o_solver *s, double *buf);
+/* One actuation term (0 Springs, 1 Pressure) alone at s->x: gradient, diagonal, curvature
+   along s->p, energy per environment (test access). */
+void d2o_term(d2o_solver *s, int which, double *E);
 
 /* Number of floating-point operations the element pass of one iteration would perform
  * is not counted here; see the Python side. */

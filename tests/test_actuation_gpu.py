@@ -1,0 +1,215 @@
+"""Actuators on the GPU: pressure chambers, springs and pins, active material, through the
+public API (Model / ImplicitIntegrator.simulate) against the oracle, mixed against FP64, and
+the closed-form states of the reference's tests/test_actuation.py on the device."""
+import warnings
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import rel_err
+from test_actuation_oracle import E, NU, RHO, _cavity_block, _hydrostatic_stretch, _integ, _model, _prob
+
+pytestmark = pytest.mark.gpu
+
+DT = 1e-3
+
+
+def _actuated(with_strain=True):
+    """The cavity block and a small second body: cavity pressure, ambient pressure, a spring
+    between the bodies, a world spring and a pin, a fiber-active lower half, gravity."""
+    m, h, h2 = _cavity_block(second=(0.03, 0.065))
+    m.set_pressure(m.add_pressure_chambers(h)[0], 2.0e4)
+    m.set_pressure(m.add_ambient_pressure(h), 4.0e3)
+    s1 = m.add_spring(h, (0.024, 0.059), h2, (0.029, 0.064), stiffness=2.0e4)
+    m.set_spring_length(s1, 0.8 * m._springs[s1]["length"])
+    m.add_spring(h, (0.036, 0.041), None, (0.040, 0.035), stiffness=3.0e4, rest_length=0.004)
+    m.add_pin(h, (0.024, 0.041), stiffness=5.0e4)
+    if with_strain:
+        reg = np.zeros((20, 14), np.uint8)
+        reg[:8] = 1
+        m.set_activation(m.add_active_region(h, reg, fiber=0.4), 0.96, transverse=1.02)
+    m.gravity = (0.0, -9.81)
+    return m, h, h2
+
+
+def _simulate(m, integ, n, dt=DT):
+    xs = []
+    for _ in range(n):
+        integ.simulate(m, dt)
+        st = integ.stats(m)["status"]
+        assert (st == 0).all(), st
+        xs.append(m.get_x())
+    return xs
+
+
+def test_fp64_matches_oracle_with_actuators():
+    """Six steps at the configuration's own iteration budget: within 1e-9 of the oracle."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    m, _, _ = _actuated()
+    integ = ImplicitIntegrator(precision="fp64")
+    prob = _prob(m, integ, DT)
+    _, xo, _ = oracle.run(prob, 6)
+    xg = _simulate(m, integ, 6)
+    for k in range(6):
+        assert rel_err(xg[k], xo[k]) < 1e-9, k
+
+
+def test_line_search_with_actuators_matches_oracle():
+    """The FP64 energy line search with the spring and pressure energies: within 1e-9."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    m, _, _ = _actuated(with_strain=False)
+    integ = ImplicitIntegrator(precision="fp64", line_search=True)
+    prob = _prob(m, integ, DT)
+    _, xo, _ = oracle.run(prob, 3)
+    xg = _simulate(m, integ, 3)
+    for k in range(3):
+        assert rel_err(xg[k], xo[k]) < 1e-9, k
+
+
+@pytest.mark.parametrize("cs", [1, 16])
+def test_mixed_matches_fp64_with_actuators(cs):
+    """Converged steps (3000 iterations, eps 1e-13): mixed on a block or on a 16-block
+    cluster within 1e-6 of FP64."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    xs = {}
+    for prec in ("fp64", "mixed"):
+        m, _, _ = _actuated()
+        integ = ImplicitIntegrator(precision=prec, max_iter=3000, eps=1e-13,
+                                   blocks_per_scene=(cs if prec == "mixed" else 0))
+        xs[prec] = _simulate(m, integ, 4)
+    for k in range(4):
+        assert rel_err(xs["mixed"][k], xs["fp64"][k]) < 1e-6, k
+
+
+def test_commands_reach_the_device():
+    """Pressure, spring length and anchor changed between steps, then an activation change:
+    the device follows the oracle given the same commands."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator, scene
+    m, h, h2 = _actuated(with_strain=False)
+    reg = np.zeros((20, 14), np.uint8)
+    reg[12:] = 1
+    r = m.add_active_region(h, reg)
+    integ = ImplicitIntegrator(precision="fp64")
+    prob = _prob(m, integ, DT)
+    o = oracle.OracleSolver(prob)
+    xg = _simulate(m, integ, 2)
+    for _ in range(2):
+        o.step()
+    assert rel_err(xg[-1], o.x) < 1e-9
+    m.set_pressure(0, 3.5e4)
+    m.set_spring_length(0, 0.7 * m._springs[0]["length"])
+    m.set_spring_anchor(1, (0.041, 0.034))
+    o.set_pressure([3.5e4, 4.0e3])
+    o.set_springs(anchor=[s["anchor"] for s in m._springs], L0=[s["length"] for s in m._springs])
+    xg = _simulate(m, integ, 2)
+    for _ in range(2):
+        o.step()
+    assert rel_err(xg[-1], o.x) < 1e-9
+    m.set_activation(r, 1.05)
+    Bm, area, _ = scene.rest_shape(m)
+    p2 = dict(prob, x=m.get_x(), v=m._solver.get_v(), Bm=Bm, area=area)
+    p2["pressure"] = dict(prob["pressure"], p=np.array([3.5e4, 4.0e3]))
+    p2["springs"] = dict(prob["springs"], L0=np.array([s["length"] for s in m._springs]),
+                         anchor=np.array([s["anchor"] for s in m._springs]))
+    _, xo, _ = oracle.run(p2, 2)
+    xg = _simulate(m, integ, 2)
+    assert rel_err(xg[-1], xo[-1]) < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_hydrostatic_state_is_exact(precision):
+    """Equal pressure in two cavities and outside: a uniform stretch (any geometry)."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    p = 6.0e4
+    s_exact = _hydrostatic_stretch(p)
+    mk = np.ones((20, 14), np.uint8)
+    mk[5:15, 4:10] = 0
+    mk[2:4, 8:12] = 0
+    m, h, _ = _model(mk, (0.014, 0.020), center=(0.03, 0.05))
+    for c in m.add_pressure_chambers(h) + [m.add_ambient_pressure(h)]:
+        m.set_pressure(c, p)
+    integ = ImplicitIntegrator(max_iter=2000, eps=1e-14, tol_x=2e-9, conv_check=8, self_collision=False,
+                               friction=False, precision=precision)
+    x = _simulate(m, integ, 30, 5e-3)[-1]
+    X = np.asarray(m.me.rest_pos, np.float64)
+    Xc = X - X.mean(0)
+    s_fem = float(((x - x.mean(0)) * Xc).sum() / (Xc ** 2).sum())
+    assert abs(s_fem - s_exact) < 5e-3 * (1 - s_exact)
+    assert np.abs((x - x.mean(0)) - s_exact * Xc).max() < 1e-4 * np.ptp(X[:, 1])
+
+
+def test_thick_walled_ring():
+    """Lame: internal pressure in a pixel ring, plane strain, small strain
+    (reference tests/test_actuation.py:183-200): cavity area change within 3 %."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    n, size, p = 48, 0.048, 1.0e-3 * E
+    yy, xx = np.mgrid[0:n, 0:n] + 0.5 - n / 2
+    r = np.hypot(xx, yy)
+    mk = ((r >= n // 4) & (r <= n // 2 - 1)).astype(np.uint8)
+    m, h, _ = _model(mk, (size, size))
+    ch = m.add_pressure_chamber(h, at=(0.0, 0.0))
+    A0 = m.chamber_area(ch)
+    m.set_pressure(ch, p)
+    integ = ImplicitIntegrator(max_iter=4000, eps=1e-14, tol_x=2e-9, conv_check=8, self_collision=False,
+                               friction=False, precision="fp64")
+    _simulate(m, integ, 25, 5e-3)
+    a = np.sqrt(A0 / np.pi)
+    b = np.sqrt((mk.sum() * (size / n) ** 2 + A0) / np.pi)
+    ua = (1 + NU) / E * p * a * a / (b * b - a * a) * ((1 - 2 * NU) * a + b * b / a)
+    dA, exact = m.chamber_area(ch) - A0, 2 * np.pi * a * ua
+    assert abs(dA - exact) < 0.03 * exact, (dA, exact)
+
+
+def test_active_material_free_growth():
+    """A fully active free body takes the prescribed shape A (mixed precision)."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    mk = np.ones((16, 10), np.uint8)
+    mk[5:9, 3:7] = 0
+    m, h, _ = _model(mk, (0.010, 0.016))
+    th = np.deg2rad(30.0)
+    m.set_activation(m.add_active_region(h, np.ones_like(mk), fiber=th), 0.85, transverse=1.10)
+    integ = ImplicitIntegrator(max_iter=3000, eps=1e-14, tol_x=2e-9, conv_check=8, self_collision=False,
+                               friction=False, alpha_max=1e9, precision="mixed")
+    x = _simulate(m, integ, 10, 2e-2)[-1]
+    X = np.asarray(m.me.rest_pos, np.float64)
+    F = np.linalg.lstsq(X - X.mean(0), x - x.mean(0), rcond=None)[0].T
+    assert np.allclose(np.linalg.svd(F)[1], [1.10, 0.85], atol=2e-4)
+
+
+def test_pin_holds_a_hanging_body():
+    """A body pinned at one point under gravity hangs from it: the pinned node stays within
+    the spring's static stretch of the anchor, and the centroid settles below it."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    m, h, _ = _model(np.ones((6, 6), np.uint8), (0.006, 0.006), center=(0.0, 0.0), damping=50.0)
+    pin = m.add_pin(h, (-0.003, 0.003), stiffness=1.0e7)
+    m.gravity = (0.0, -9.81)
+    integ = ImplicitIntegrator(precision="fp64", max_iter=3000, eps=1e-13, self_collision=False)
+    for _ in range(200):
+        integ.simulate(m, 1e-2)
+    x = m.get_x()
+    a = m._springs[pin]["a"]
+    W = float(np.asarray(m.me.mass).sum()) * 9.81
+    assert np.linalg.norm(x[a] - np.array([-0.003, 0.003])) < 5 * W / 1.0e7
+    c = x.mean(0)
+    assert c[1] < 0.003 - 0.002 and abs(c[0] - (-0.003)) < 1e-3
+
+
+def test_adjoint_refuses_actuators_it_cannot_differentiate():
+    """Gravity is fine; after a pressure chamber is added (the solver rebuilt from the
+    current state) transient_adjoint refuses (reference tests/test_actuation.py:329-345)."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    m, h, _ = _cavity_block()
+    integ = ImplicitIntegrator(max_iter=50, self_collision=False, friction=False, precision="fp64")
+    adj = integ.adjoint(m, 1e-3)
+    m.gravity = (0.0, -9.81)
+    integ.simulate(m, 1e-3)
+    xs = [np.asarray(m.me.rest_pos, np.float64), m.get_x()]
+    seed = {1: np.ones_like(xs[0])}
+    adj.transient_adjoint(xs, seed=seed)
+    m.set_pressure(m.add_pressure_chambers(h)[0], 1.0e3)
+    integ.simulate(m, 1e-3)
+    with pytest.raises(NotImplementedError):
+        adj.transient_adjoint(xs, seed=seed)
+    with pytest.raises(NotImplementedError):
+        integ.adjoint(m, 1e-3)
