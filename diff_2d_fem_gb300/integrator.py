@@ -109,7 +109,7 @@ class ImplicitIntegrator:
             s.iter_max = _scene.iters_for(model, self, dt)
             s.set_dt(dt, s.iter_max)
         self._sync_actuation(model)
-        return s
+        return model._solver        # rebuilt by the sync when a term was added
 
     def _sync_actuation(self, model):
         """Rebuild the solver when an actuator was added (from the current state), and push
