@@ -55,7 +55,7 @@ def _solver_of(obj):
             "ImplicitIntegrator(self_collision=False)")
     if s.desc.n_aff > 0:
         raise NotImplementedError("the adjoint operator has no tangent for affine bodies")
-    _refuse_actuators(s.desc.n_pe > 0, s.desc.n_sp > 0, bool(s.prob.get("active_regions", 0)))
+    _refuse_actuators(False, False, bool(s.prob.get("active_regions", 0)))
     return s
 
 
@@ -171,6 +171,20 @@ class AdjointPNCG2D:
                                             C.c_void_p(dscale.data_ptr()), dt_, self.s._stream_ptr()),
                    "d2f_adjoint_vjp")
 
+    def dpressure(self, xk, lam, out=None):
+        """dL/dp of every chamber (model order) for one step: the product of lam (from
+        adjoint_solve at x_k) with the step residual's derivative in each chamber's pressure.
+        Added into `out` (n_ch, device) if given; returned."""
+        n_ch = int(self.s.desc.n_ch)
+        if out is None:
+            out = torch.zeros(n_ch, dtype=torch.float64, device=self.dev)
+        if n_ch:
+            xk, lam = self._x(xk), self._x(lam)
+            _lib.check(self.s.L.d2f_adjoint_vjp_pressure(self.s.h, C.c_void_p(xk.data_ptr()), C.c_void_p(lam.data_ptr()),
+                                                         C.c_void_p(out.data_ptr()), self.s._stream_ptr()),
+                       "d2f_adjoint_vjp_pressure")
+        return out
+
     def drho(self, xk, lam):
         """implicit/adjoint.py:277-283: -(1 - Emin) lam . [h^2 f_e(x_k)] at full density."""
         d = torch.zeros(self.n_tri, dtype=torch.float64, device=self.dev)
@@ -181,10 +195,13 @@ class AdjointPNCG2D:
         """implicit/adjoint.py:371-399. xs = [x_0 .. x_T] (the forward states, arrays or
         tensors (N, 2)), seed = {k: dJ/dx_k (N, 2)}. Returns dJ/drho (n_tri,) as a device
         tensor, accumulated over the trajectory."""
+        # the operator has the springs' and chambers' tangents at their current commands, but a
+        # trajectory may have changed those commands step by step: refused as the reference does
         m = self.model
         if m is not None:
             _refuse_actuators(bool(m._chambers), bool(m._springs), bool(m._regions))
             self.s                  # the model's current solver
+        _refuse_actuators(self.s.desc.n_pe > 0, self.s.desc.n_sp > 0, False)
         T = len(xs) - 1
         dr = self.drag if drag is None else float(drag)
         m2 = self.mass[:, None]

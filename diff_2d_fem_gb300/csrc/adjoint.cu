@@ -191,6 +191,33 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                 }
                 __syncthreads();
             }
+            if (sg.nsp > 0 || sg.npe > 0) {
+                // springs: h^2 (k n n^T + k (1 - L0/|d|) (I - n n^T)) on the ends' difference
+                // (Springs, implicit/actuation.py:381-393), the tangential term unclamped (the
+                // exact tangent)
+                for (int k = sg.sp0 + tid; k < sg.sp0 + sg.nsp; k += NT) {
+                    const int a = d.sp_a[k], b = d.sp_b[k];
+                    const double2 xa = XL[a], xb = b >= 0 ? XL[b] : make_double2(d.sp_anchor[2 * k], d.sp_anchor[2 * k + 1]);
+                    const double dx = xa.x - xb.x, dy = xa.y - xb.y, ln = sqrt(dx * dx + dy * dy + 1.0e-30);
+                    const double nx = dx / ln, ny = dy / ln, kk = d.sp_k[k], kt = kk * (1.0 - d.sp_L0[k] / ln);
+                    double vx = V[a].x, vy = V[a].y;
+                    if (b >= 0) { vx -= V[b].x; vy -= V[b].y; }
+                    const double al = vx * nx + vy * ny;
+                    const double fx = h2 * (kk * al * nx + kt * (vx - al * nx)), fy = h2 * (kk * al * ny + kt * (vy - al * ny));
+                    atomicAdd(&AP[a].x, fx); atomicAdd(&AP[a].y, fy);
+                    if (b >= 0) { atomicAdd(&AP[b].x, -fx); atomicAdd(&AP[b].y, -fy); }
+                }
+                // pressure: the gradient -h^2 p/2 (t.y, -t.x) on both ends of an edge is linear in
+                // x, so its product with V is the same with t -> V_b - V_a (Pressure, :98-118)
+                for (int e = sg.pe0 + tid; e < sg.pe0 + sg.npe; e += NT) {
+                    const int a = d.pe_a[e], b = d.pe_b[e];
+                    const double sp = -0.5 * h2 * d.ch_p[d.pe_ch[e]];
+                    const double tx = V[b].x - V[a].x, ty = V[b].y - V[a].y;
+                    atomicAdd(&AP[a].x, sp * ty); atomicAdd(&AP[a].y, -sp * tx);
+                    atomicAdd(&AP[b].x, sp * ty); atomicAdd(&AP[b].y, -sp * tx);
+                }
+                __syncthreads();
+            }
         };
 
         // ---- tangent at x_lin: F^-T and (la log J - mu) per triangle, the Jacobi diagonal per corner
@@ -219,7 +246,6 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
         __syncthreads();
         // ---- the Jacobi preconditioner; the initial guess (0, or lam as given with warm)
         for (int i = n0 + tid; i < n1; i += NT) {
-            const uint8_t fm = d.free_mask[i];
             const double m = d.mass[i];
             double dx = m, dy = m;
             for (int k = d.inc_ptr[i]; k < d.inc_ptr[i + 1]; ++k) {
@@ -234,7 +260,23 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                     dx += h2 * dmax(h00, 0.0); dy += h2 * dmax(h11, 0.0);
                 }
             }
-            DI[i] = make_double2((fm & 1) ? 1.0 / dx : 0.0, (fm & 2) ? 1.0 / dy : 0.0);
+            DI[i] = make_double2(dx, dy);
+        }
+        __syncthreads();
+        for (int k = sg.sp0 + tid; k < sg.sp0 + sg.nsp; k += NT) {  // springs' diagonal (clamped, as the step's)
+            const int a = d.sp_a[k], b = d.sp_b[k];
+            const double2 xa = XL[a], xb = b >= 0 ? XL[b] : make_double2(d.sp_anchor[2 * k], d.sp_anchor[2 * k + 1]);
+            const double dx = xa.x - xb.x, dy = xa.y - xb.y, ln = sqrt(dx * dx + dy * dy + 1.0e-30);
+            const double nx = dx / ln, ny = dy / ln, kk = d.sp_k[k], kt = dmax(kk * (1.0 - d.sp_L0[k] / ln), 0.0);
+            const double hx = h2 * (kk * nx * nx + kt * (1.0 - nx * nx)), hy = h2 * (kk * ny * ny + kt * (1.0 - ny * ny));
+            atomicAdd(&DI[a].x, hx); atomicAdd(&DI[a].y, hy);
+            if (b >= 0) { atomicAdd(&DI[b].x, hx); atomicAdd(&DI[b].y, hy); }
+        }
+        __syncthreads();
+        for (int i = n0 + tid; i < n1; i += NT) {
+            const uint8_t fm = d.free_mask[i];
+            const double2 dd = DI[i];
+            DI[i] = make_double2((fm & 1) ? 1.0 / dd.x : 0.0, (fm & 2) ? 1.0 / dd.y : 0.0);
             double2 l0 = make_double2(0.0, 0.0);
             if (warm) {
                 const double2 l = LAM[i];
@@ -342,6 +384,22 @@ __global__ void vjp_scale_kernel(const __grid_constant__ d2f_scene_desc d, const
     }
 }
 
+// dL/dp (gauge pressure of each chamber at this step) = -lam . dg/dp with the pressure
+// gradient g_a = g_b = -h^2 p / 2 (t.y, -t.x), t = x_b - x_a, per edge (grad_pressure_kernel,
+// implicit/actuation.py:98-108): + h^2 / 2 (lam_a + lam_b) . (t.y, -t.x), one thread per edge
+__global__ void vjp_pressure_kernel(const __grid_constant__ d2f_scene_desc d, const double *__restrict__ xl,
+                                    const double *__restrict__ lam, double *__restrict__ dp) {
+    const double2 *X = reinterpret_cast<const double2 *>(xl);
+    const double2 *L = reinterpret_cast<const double2 *>(lam);
+    const double h2 = d.dt * d.dt;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.n_pe; e += gridDim.x * blockDim.x) {
+        const int a = d.pe_a[e], b = d.pe_b[e];
+        const double tx = X[b].x - X[a].x, ty = X[b].y - X[a].y;
+        const double lx = L[a].x + L[b].x, ly = L[a].y + L[b].y;
+        atomicAdd(dp + d.pe_ch[e], 0.5 * h2 * (lx * ty - ly * tx));
+    }
+}
+
 // dL/dT (tension of each tendon at this step) = -h^2 lam . dlen/dx: one block per scene, one
 // thread per tendon of the scene, summed over its eyelets in eyelet order (deterministic)
 __global__ void vjp_tension_kernel(const __grid_constant__ d2f_scene_desc d, const double *__restrict__ xl,
@@ -389,8 +447,6 @@ int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs,
     if (s->d.precision != D2F_FP64) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: needs an FP64 solver");
     if (s->d.Ne > 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: IPC contact between bodies has no adjoint tangent");
     if (s->d.n_aff > 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: affine bodies have no adjoint tangent");
-    if (s->d.n_sp > 0 || s->d.n_pe > 0)
-        return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: springs and pressure chambers have no adjoint tangent");
     if (!(rtol > 0.0) || max_iter <= 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: rtol > 0 and max_iter > 0");
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(s->d.work, 0, 4 * sizeof(int32_t), st) != cudaSuccess)
@@ -429,6 +485,22 @@ int32_t d2f_adjoint_vjp(d2f_solver *s, const double *x_lin, const double *lam, d
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         snprintf(g_err, sizeof g_err, "d2f_adjoint_vjp: launch failed: %s", cudaGetErrorString(e));
+        return D2F_ECUDA;
+    }
+    return D2F_OK;
+}
+
+int32_t d2f_adjoint_vjp_pressure(d2f_solver *s, const double *x_lin, const double *lam, double *dpressure,
+                                 void *stream) {
+    g_err[0] = 0;
+    if (!s || !x_lin || !lam || !dpressure) return d2f_fail(D2F_EINVAL, "d2f_adjoint_vjp_pressure: null argument");
+    if (s->d.precision != D2F_FP64) return d2f_fail(D2F_EINVAL, "d2f_adjoint_vjp_pressure: needs an FP64 solver");
+    if (s->d.n_pe <= 0) return D2F_OK;
+    const int blocks = (s->d.n_pe + 255) / 256 < 1024 ? (s->d.n_pe + 255) / 256 : 1024;
+    d2f::adj::vjp_pressure_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(s->d, x_lin, lam, dpressure);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        snprintf(g_err, sizeof g_err, "d2f_adjoint_vjp_pressure: launch failed: %s", cudaGetErrorString(e));
         return D2F_ECUDA;
     }
     return D2F_OK;

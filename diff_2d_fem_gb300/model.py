@@ -350,6 +350,47 @@ class Model:
         np.add.at(out, (q % H, q // H), np.asarray(values, np.float64))
         return out
 
+    # ---- read-outs (sim_model.py:625-642, core/fields.py), computed on the GPU
+    def element_strain(self, x=None, handle=None, signed=False):
+        """Strain of every element at positions x (default: now), or of one body's elements
+        in body_elements order: the von Mises equivalent of the Green-Lagrange strain (>= 0);
+        signed=True: the in-plane principal strain of larger magnitude (+ tension)."""
+        return self._field("strain", x, handle, signed)
+
+    def element_stress(self, x=None, handle=None, signed=False):
+        """Cauchy stress [Pa] of every element at positions x (default: now) with the bodies'
+        own moduli, or of one body's elements: von Mises (>= 0), or with signed=True the
+        in-plane principal stress of larger magnitude (+ tension)."""
+        return self._field("stress", x, handle, signed)
+
+    def _field(self, field, x, handle, signed=False):
+        import torch
+        from . import _lib
+        if not torch.cuda.is_available():
+            raise RuntimeError("element read-outs run on the GPU: no CUDA device")
+        L = _lib.load()
+        dev = torch.device(self.device if str(self.device).startswith("cuda") else "cuda")
+        me = self.me
+        c = getattr(self, "_field_bufs", None)
+        if c is None:
+            f64 = torch.float64
+            c = self._field_bufs = dict(
+                tri=torch.as_tensor(np.asarray(me.tri), dtype=torch.int32, device=dev).contiguous(),
+                Bm=torch.as_tensor(np.asarray(me.D_m_inv, np.float64).reshape(-1, 4), dtype=f64, device=dev).contiguous(),
+                mu=torch.as_tensor(np.asarray(me.mu, np.float64), dtype=f64, device=dev),
+                lam=torch.as_tensor(np.asarray(me.lam, np.float64), dtype=f64, device=dev))
+        T = int(c["tri"].shape[0])
+        xx = torch.as_tensor(np.asarray(self.get_x() if x is None else x, np.float64), device=dev).contiguous()
+        out = torch.empty(T, dtype=torch.float64, device=dev)
+        slot = {("strain", False): 6, ("strain", True): 7, ("stress", False): 8, ("stress", True): 9}[(field, bool(signed))]
+        args = [None] * 4
+        args[slot - 6] = out.data_ptr()
+        rc = L.d2f_element_fields(T, c["tri"].data_ptr(), c["Bm"].data_ptr(), c["mu"].data_ptr(), c["lam"].data_ptr(),
+                                  xx.data_ptr(), *args, torch.cuda.current_stream(dev).cuda_stream)
+        _lib.check(rc, "d2f_element_fields")
+        v = out.cpu().numpy()
+        return v if handle is None else v[self._tri_range[handle]]
+
     def rigid_motion(self, handle, translation=(0.0, 0.0), angle=0.0, about=None):
         x = self.rest_x(handle)
         c = np.asarray(self._bodies[handle]["center"] if about is None else about, np.float64)

@@ -197,6 +197,15 @@ size_t d2f_mixed_scratch_bytes(int32_t N, int32_t T, int32_t Nb, int32_t n_col, 
 /* Number of kernels d2f_step launches per call (for launch accounting). */
 int32_t d2f_kernels_per_step(const d2f_solver *s);
 
+/* Strain and stress of every triangle at positions x (core/fields.py: element_field; the
+ * read-outs Model.element_strain / element_stress, sim_model.py:625-642), FP64 device arrays:
+ * tri (T x 3), Bm (T x 4 row-major rest-shape inverse), mu, lam (T), x (N x 2). Outputs (T,
+ * NULL to skip): the von Mises Green-Lagrange strain, its signed in-plane principal value,
+ * the von Mises Neo-Hookean Cauchy stress, its signed principal value. One launch on stream. */
+int32_t d2f_element_fields(int32_t T, const int32_t *tri, const double *Bm, const double *mu, const double *lam,
+                           const double *x, double *strain_vm, double *strain_signed, double *stress_vm,
+                           double *stress_signed, void *stream);
+
 /* The launch shape d2f_step uses: blocks launched, threads per block, blocks per scene (1: a
  * block per scene; 8 or 16: one cluster per scene). Null outputs are skipped. */
 int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads, int32_t *blocks_per_scene);
@@ -247,6 +256,12 @@ int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs,
  *   dtension[k]  = -h^2 lam . dL_k/dx       (L_k: length of tendon k; NULL to skip)
  * Replaces AdjointPNCG2D.drho (implicit/adjoint.py:277-283, drho_kernel :164-178), which
  * returns the same product pre-multiplied by the density map's (1 - Emin). */
+/* dL/dp += the product of lam (from d2f_adjoint_solve at x_lin) with the derivative of the
+ * step's residual with respect to each chamber's pressure (n_ch doubles, atomics). The
+ * pressure and spring terms are in d2f_adjoint_solve's operator. */
+int32_t d2f_adjoint_vjp_pressure(d2f_solver *s, const double *x_lin, const double *lam, double *dpressure,
+                                 void *stream);
+
 int32_t d2f_adjoint_vjp(d2f_solver *s, const double *x_lin, const double *lam, double *dscale, double *dtension,
                         void *stream);
 
