@@ -54,7 +54,7 @@ class SceneDesc(C.Structure):
 EXPORTS = ("d2f_abi_version", "d2f_create", "d2f_step", "d2f_set_dt", "d2f_stats", "d2f_destroy",
            "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc", "d2f_mixed_scratch_bytes",
            "d2f_adjoint_solve", "d2f_adjoint_vjp", "d2f_launch_shape",
-           "d2f_element_fields", "d2f_adjoint_vjp_pressure")
+           "d2f_element_fields", "d2f_adjoint_vjp_pressure", "d2f_contact_force")
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
@@ -93,6 +93,8 @@ def load(build_if_missing: bool = True):
     L.d2f_element_fields.restype = _I
     L.d2f_adjoint_vjp_pressure.argtypes = [_P] * 5
     L.d2f_adjoint_vjp_pressure.restype = _I
+    L.d2f_contact_force.argtypes = [_P, _I, _I, _I, _P, _P]
+    L.d2f_contact_force.restype = _I
     L.d2f_step_noalloc.argtypes = [C.POINTER(SceneDesc), _P]
     L.d2f_step_noalloc.restype = _I
     L.d2f_mixed_scratch_bytes.argtypes = [_I, _I, _I, _I, _I]

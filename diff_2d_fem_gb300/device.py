@@ -388,6 +388,26 @@ class DeviceSolver:
         if L0 is not None:
             self._t["t_L0"].copy_(torch.as_tensor(np.asarray(L0, np.float64)[self.ten_order]))
 
+    # ---- contact read-outs (implicit/solver.py:553-612), on the device
+    def contact_force(self, friction=True, colliders=True, bodies=True):
+        """Force that contact exerts ON each node [N/m], (N, 2): the colliders' barrier and
+        the contact between bodies, with friction unless friction=False; kinematic nodes
+        included. Evaluated where the bodies are now, with the slip of the last step."""
+        out = torch.empty((self.N, 2), dtype=torch.float64, device=self.dev)
+        flags = (1 if colliders else 0) | (2 if bodies else 0) | (4 if friction else 0)
+        _lib.check(self.L.d2f_contact_force(self.h, 0, -1, flags, out.data_ptr(), self._stream_ptr()),
+                   "d2f_contact_force")
+        return out.cpu().numpy()
+
+    def collider_force(self, index=None, include_friction=False):
+        """Reaction on the colliders per environment (B, 2): on collider `index`, or on all of
+        them together when index is None."""
+        out = torch.empty((self.B, 2), dtype=torch.float64, device=self.dev)
+        _lib.check(self.L.d2f_contact_force(self.h, 1, -1 if index is None else int(index),
+                                            4 if include_friction else 0, out.data_ptr(), self._stream_ptr()),
+                   "d2f_contact_force")
+        return out.cpu().numpy()
+
     def set_pressures(self, p):
         """Gauge pressure of every chamber [Pa], in the model's chamber order."""
         if self.pr is None:

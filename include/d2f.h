@@ -206,6 +206,13 @@ int32_t d2f_element_fields(int32_t T, const int32_t *tri, const double *Bm, cons
                            const double *x, double *strain_vm, double *strain_signed, double *stress_vm,
                            double *stress_signed, void *stream);
 
+/* Contact read-outs at the solver's current x, with the last step's slip from x_n
+ * (PNCG2DSolver.contact_force / collider_force, implicit/solver.py:553-612). what 0: the force
+ * contact exerts on every node into out (N x 2 doubles; zeroed first): flags 1 colliders'
+ * barrier, 2 contact between bodies, 4 friction; every DOF. what 1: the reaction on collider
+ * `collider` (all of them when < 0) per scene into out (n_scenes x 2), flag 4 adds friction. */
+int32_t d2f_contact_force(d2f_solver *s, int32_t what, int32_t collider, int32_t flags, double *out, void *stream);
+
 /* The launch shape d2f_step uses: blocks launched, threads per block, blocks per scene (1: a
  * block per scene; 8 or 16: one cluster per scene). Null outputs are skipped. */
 int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads, int32_t *blocks_per_scene);

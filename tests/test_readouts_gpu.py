@@ -42,3 +42,58 @@ def test_uniform_stretch_closed_form():
     x = s * X
     assert np.allclose(m.element_strain(x), 2.0 * e / 3.0, rtol=1e-12)
     assert np.allclose(m.element_strain(x, signed=True), e, rtol=1e-12)
+
+
+def _settle(m, steps=300, dt=5e-3):
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    integ = ImplicitIntegrator(precision="fp64", max_iter=2000, eps=1e-14)
+    for _ in range(steps):
+        integ.simulate(m, dt)
+    return m._solver
+
+
+def test_resting_block_contact_force_balances_weight():
+    """A block settled on the ground: the ground's contact force on its nodes carries its
+    weight, the ground's reaction is its weight downward, and with the block at rest the
+    friction in the reaction vanishes (PNCG2DSolver.contact_force / collider_force)."""
+    from diff_2d_fem_gb300 import Model
+    m = Model()
+    m.add_ground(0.0, mu=0.5)
+    m.damping = 20.0
+    h = m.add_soft_body(np.ones((8, 8), np.uint8), physical_size=(0.008, 0.008), center=(0.0, 0.0041),
+                        E=2.0e5, nu=0.4, density=1000.0)
+    m.finalize()
+    m.gravity = (0.0, -9.81)
+    s = _settle(m)
+    W = float(np.asarray(m.me.mass).sum()) * 9.81
+    F = s.contact_force(bodies=False)
+    assert abs(F[:, 1].sum() - W) < 1e-3 * W
+    assert abs(F[:, 0].sum()) < 1e-3 * W
+    R = s.collider_force(0)
+    assert np.allclose(R[0], [0.0, -W], atol=1e-3 * W)
+    Rf = s.collider_force(0, include_friction=True)
+    assert np.allclose(Rf, R, atol=1e-3 * W)
+    assert np.abs(s.contact_force(colliders=False)).max() < 1e-9 * W
+
+
+def test_stacked_blocks_contact_between_bodies():
+    """A block settled on another: the contact between bodies pushes the upper block up by
+    its weight, and its forces sum to zero over both (action and reaction)."""
+    from diff_2d_fem_gb300 import Model
+    m = Model()
+    m.add_ground(0.0, mu=0.5)
+    m.damping = 20.0
+    lo = m.add_soft_body(np.ones((6, 10), np.uint8), physical_size=(0.010, 0.006), center=(0.0, 0.0031),
+                         E=3.0e5, nu=0.4, density=1000.0)
+    up = m.add_soft_body(np.ones((6, 6), np.uint8), physical_size=(0.006, 0.006), center=(0.0, 0.0095),
+                         E=3.0e5, nu=0.4, density=1000.0)
+    m.finalize()
+    m.gravity = (0.0, -9.81)
+    s = _settle(m)
+    Wup = float(np.asarray(m.me.mass)[m.body_nodes(up)].sum()) * 9.81
+    Fb = s.contact_force(colliders=False)
+    assert np.abs(Fb.sum(0)).max() < 1e-9 * Wup
+    assert abs(Fb[m.body_nodes(up), 1].sum() - Wup) < 1e-2 * Wup
+    F = s.contact_force()
+    Wall = float(np.asarray(m.me.mass).sum()) * 9.81
+    assert abs(F[:, 1].sum() - Wall) < 1e-2 * Wall
