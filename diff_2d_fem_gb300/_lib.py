@@ -13,7 +13,7 @@ _I = C.c_int32
 _D = C.c_double
 _P = C.c_void_p
 
-D2F_ABI_VERSION = 5
+D2F_ABI_VERSION = 6
 D2F_FP64, D2F_MIXED = 0, 1
 ERRORS = {0: "ok", -1: "D2F_EINVAL", -2: "D2F_ECUDA", -3: "D2F_ECAP", -4: "D2F_ENAN"}
 
@@ -44,6 +44,7 @@ DESC_FIELDS = (
     + [("ls_tol", _D), ("line_search", _I), ("n_backtrack", _I), ("blocks_per_scene", _I),
        ("a_ptr", _P), ("n_sp", _I)] + [(n, _P) for n in ("sp_a", "sp_b", "sp_k", "sp_L0", "sp_anchor")]
     + [("n_pe", _I), ("n_ch", _I)] + [(n, _P) for n in ("pe_a", "pe_b", "pe_ch", "ch_p", "ch_ref")]
+    + [("energy_out", _P)]
 )
 
 
@@ -54,7 +55,7 @@ class SceneDesc(C.Structure):
 EXPORTS = ("d2f_abi_version", "d2f_create", "d2f_step", "d2f_set_dt", "d2f_stats", "d2f_destroy",
            "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc", "d2f_mixed_scratch_bytes",
            "d2f_adjoint_solve", "d2f_adjoint_vjp", "d2f_launch_shape",
-           "d2f_element_fields", "d2f_adjoint_vjp_pressure", "d2f_contact_force")
+           "d2f_element_fields", "d2f_adjoint_vjp_pressure", "d2f_contact_force", "d2f_energy")
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
@@ -95,6 +96,8 @@ def load(build_if_missing: bool = True):
     L.d2f_adjoint_vjp_pressure.restype = _I
     L.d2f_contact_force.argtypes = [_P, _I, _I, _I, _P, _P]
     L.d2f_contact_force.restype = _I
+    L.d2f_energy.argtypes = [_P, _P, _P]
+    L.d2f_energy.restype = _I
     L.d2f_step_noalloc.argtypes = [C.POINTER(SceneDesc), _P]
     L.d2f_step_noalloc.restype = _I
     L.d2f_mixed_scratch_bytes.argtypes = [_I, _I, _I, _I, _I]

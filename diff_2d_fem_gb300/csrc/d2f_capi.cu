@@ -215,6 +215,23 @@ int32_t d2f_destroy(d2f_solver *s) {
 
 int32_t d2f_kernels_per_step(const d2f_solver *s) { return s ? 1 : 0; }
 
+int32_t d2f_energy(d2f_solver *s, double *out, void *stream) {
+    g_err[0] = 0;
+    if (!s || !out) return fail(D2F_EINVAL, "d2f_energy: null argument");
+    if (s->d.precision != D2F_FP64) return fail(D2F_EINVAL, "d2f_energy: the energy read-out runs in FP64 solvers");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(s->d.work, 0, 4 * sizeof(int32_t), st) != cudaSuccess)
+        return fail(D2F_ECUDA, "d2f_energy: cudaMemsetAsync failed");
+    d2f_scene_desc d = s->d;
+    d.energy_out = out;
+    cudaError_t e = launch(d, s->grid, s->smem, 1, st);
+    if (e != cudaSuccess) {
+        snprintf(g_err, sizeof g_err, "d2f_energy: launch failed: %s", cudaGetErrorString(e));
+        return D2F_ECUDA;
+    }
+    return D2F_OK;
+}
+
 int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads, int32_t *blocks_per_scene) {
     if (!s) return fail(D2F_EINVAL, "d2f_launch_shape: null handle");
     if (blocks) *blocks = s->grid;

@@ -205,8 +205,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
         if (tid < n_col && tid < MAX_COL) colmu[tid] = d.col_mu_env ? d.col_mu_env[sc * n_col + tid] : cols[tid].mu;
 
         // ================================================================ step setup
-        // init_step_kernel (kernels.py:41-50); p = grad = 0 (solver.py:447)
-        for (int i = n0 + tid; i < n1; i += NT) {
+        // init_step_kernel (kernels.py:41-50); p = grad = 0 (solver.py:447); none of it for
+        // an energy read-out, which takes the state as the last step left it
+        const bool eread = d.energy_out != nullptr;
+        for (int i = n0 + tid; !eread && i < n1; i += NT) {
             double2 xi = X[i], vi = Vv[i];
             Xn[i] = xi;
             Xh[i] = make_double2(xi.x + dt * d.drag * vi.x, xi.y + dt * d.drag * vi.y);
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             S.ncand = 0; S.rebuild = 1; S.gn0 = 0.0; S.beta = 0.0;
         }
         __syncthreads();
-        if (!scene_ipc) {  // apply_bc_kernel, kernels.py:53-59
+        if (!scene_ipc && !eread) {  // apply_bc_kernel, kernels.py:53-59
             for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
                 int n = d.bc_idx[b];
                 X[n] = Tgt[b];
@@ -642,6 +644,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             if (tid == 0) S.q_inf = v[0];
             __syncthreads();
         };
+
+        if (eread) {  // PNCG2DSolver.energy (solver.py:453-502): every term at x, nothing moved
+            if (scene_ipc) ipc_refresh(true);
+            const double e = scene_energy();
+            if (tid == 0) d.energy_out[sc] = e;
+            __syncthreads();
+            continue;
+        }
 
         if (scene_ipc && sg.nbc > 0) {  // IPCContact.advance_bc, ipc_contact.py:465-473
             sweep();

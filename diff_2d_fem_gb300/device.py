@@ -388,6 +388,13 @@ class DeviceSolver:
         if L0 is not None:
             self._t["t_L0"].copy_(torch.as_tensor(np.asarray(L0, np.float64)[self.ten_order]))
 
+    def energy(self):
+        """Total energy of every scene at the current state (PNCG2DSolver.energy,
+        implicit/solver.py:500-502), (B,); FP64 solvers."""
+        out = torch.empty(self.B, dtype=torch.float64, device=self.dev)
+        _lib.check(self.L.d2f_energy(self.h, out.data_ptr(), self._stream_ptr()), "d2f_energy")
+        return out.cpu().numpy()
+
     # ---- contact read-outs (implicit/solver.py:553-612), on the device
     def contact_force(self, friction=True, colliders=True, bodies=True):
         """Force that contact exerts ON each node [N/m], (N, 2): the colliders' barrier and

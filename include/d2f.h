@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define D2F_ABI_VERSION 5
+#define D2F_ABI_VERSION 6
 
 /* status codes */
 #define D2F_OK 0
@@ -155,6 +155,7 @@ typedef struct d2f_scene_desc {
     const int32_t *pe_a, *pe_b, *pe_ch; /* n_pe: edge start / end node, chamber (global ids) */
     const double *ch_p;          /* n_ch: gauge pressure [Pa] */
     const double *ch_ref;        /* n_ch x 2: the shoelace sum's reference point (energy) */
+    double *energy_out;          /* NULL for a step; set by d2f_energy only */
 } d2f_scene_desc;
 
 typedef struct d2f_solver d2f_solver;
@@ -212,6 +213,12 @@ int32_t d2f_element_fields(int32_t T, const int32_t *tri, const double *Bm, cons
  * barrier, 2 contact between bodies, 4 friction; every DOF. what 1: the reaction on collider
  * `collider` (all of them when < 0) per scene into out (n_scenes x 2), flag 4 adds friction. */
 int32_t d2f_contact_force(d2f_solver *s, int32_t what, int32_t collider, int32_t flags, double *out, void *stream);
+
+/* Total energy of every scene at the solver's current state (PNCG2DSolver.energy,
+ * implicit/solver.py:453-502): inertia against the last step's prediction, elastic,
+ * collider barriers and lagged friction, external force, affine bodies, IPC, springs,
+ * pressure, tendons; into out (n_scenes doubles, device). Moves nothing. FP64 solvers. */
+int32_t d2f_energy(d2f_solver *s, double *out, void *stream);
 
 /* The launch shape d2f_step uses: blocks launched, threads per block, blocks per scene (1: a
  * block per scene; 8 or 16: one cluster per scene). Null outputs are skipped. */

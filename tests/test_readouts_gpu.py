@@ -97,3 +97,27 @@ def test_stacked_blocks_contact_between_bodies():
     F = s.contact_force()
     Wall = float(np.asarray(m.me.mass).sum()) * 9.81
     assert abs(F[:, 1].sum() - Wall) < 1e-2 * Wall
+
+
+def test_energy_readout_matches_oracle():
+    """PNCG2DSolver.energy: every term of every scene at the state three steps left, against
+    the oracle's energy at its own (1e-9-equal) state; reading it moves nothing."""
+    import oracle
+    from diff_2d_fem_gb300 import ImplicitIntegrator
+    from test_actuation_gpu import _actuated, _simulate
+    from test_actuation_oracle import _prob
+    m, _, _ = _actuated()
+    integ = ImplicitIntegrator(precision="fp64")
+    prob = _prob(m, integ, 1e-3)
+    o, _, _ = oracle.run(prob, 3)
+    _simulate(m, integ, 3)
+    s = m._solver
+    x0 = s.get_x()
+    e = s.energy()
+    eo = o.energy()
+    assert np.abs(e - eo).max() <= 1e-7 * np.abs(eo).max()
+    assert np.array_equal(s.get_x(), x0)
+    _simulate(m, integ, 1)
+    o.step()
+    from helpers import rel_err
+    assert rel_err(s.get_x(), o.x) < 1e-9
