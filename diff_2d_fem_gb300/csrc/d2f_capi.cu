@@ -99,30 +99,36 @@ static int validate(const d2f_scene_desc &d, bool scratch) {
         return fail(D2F_EINVAL, "d2f: spring arrays missing");
     if (d.n_pe < 0 || d.n_ch < 0 || (d.n_pe > 0 && (d.n_ch <= 0 || !d.pe_a || !d.pe_b || !d.pe_ch || !d.ch_p || !d.ch_ref)))
         return fail(D2F_EINVAL, "d2f: pressure arrays missing");
-    if (d.blocks_per_scene != 0 && d.blocks_per_scene != 1 && d.blocks_per_scene != 8 && d.blocks_per_scene != 16)
-        return fail(D2F_EINVAL, "d2f: blocks_per_scene must be 0, 1, 8 or 16");
+    if (d.blocks_per_scene != 0 && d.blocks_per_scene != 1 && d.blocks_per_scene != 8 && d.blocks_per_scene != 12 &&
+        d.blocks_per_scene != 16)
+        return fail(D2F_EINVAL, "d2f: blocks_per_scene must be 0, 1, 8, 12 or 16");
     if (d.blocks_per_scene > 1 && d.precision != D2F_MIXED)
         return fail(D2F_EINVAL, "d2f: several blocks per scene run in mixed precision only");
     return D2F_OK;
 }
 
-// Blocks per scene: the caller's choice (8 when 16-block clusters cannot be placed, 1 when
-// neither can), else clusters for batches of fewer scenes than SMs whose scenes average at
-// least 16384 nodes (a block per scene would leave most SMs idle and each scene
-// latency-bound): 16 or 8 blocks, whichever finishes the batch first, taking a scene on a
-// 16-block cluster as 1.3x faster than on an 8-block one (measured on a 0.26M-node slab)
-// and counting the waves of scenes the clusters that fit at once need.
+// Blocks per scene: the caller's choice (the next smaller cluster that can be placed when
+// it cannot, 1 when none can), else clusters for batches of fewer scenes than SMs whose
+// scenes average at least 16384 nodes (a block per scene would leave most SMs idle and each
+// scene latency-bound): 16, 12 or 8 blocks, whichever finishes the batch first, taking a
+// scene's time on 16 / 12 / 8 blocks as 1 / 1.15 / 1.3 (measured on a 0.26M-node slab) and
+// counting the waves of scenes the clusters that fit at once need.
 static int blocks_per_scene(const d2f_scene_desc &d, int nsm, int smem) {
-    const int cs = d.blocks_per_scene;
-    if (cs == 1) return 1;
-    if (cs == 0 && (d.precision != D2F_MIXED || d.n_scenes >= nsm || d.N / d.n_scenes < 16384)) return 1;
-    const int m16 = d2f::max_clusters_mixed(16, smem), m8 = d2f::max_clusters_mixed(8, smem);
-    if (cs == 16 && m16 > 0) return 16;
-    if (cs == 0 && m16 > 0) {
-        const long w16 = (d.n_scenes + m16 - 1) / m16, w8 = m8 > 0 ? (d.n_scenes + m8 - 1) / m8 : 0;
-        if (m8 == 0 || 10 * w16 <= 13 * w8) return 16;
+    const int want = d.blocks_per_scene;
+    if (want == 1) return 1;
+    if (want == 0 && (d.precision != D2F_MIXED || d.n_scenes >= nsm || d.N / d.n_scenes < 16384)) return 1;
+    const int sizes[3] = {16, 12, 8}, cost[3] = {100, 115, 130};
+    int best = 1;
+    long best_t = 0;
+    for (int k = 0; k < 3; ++k) {
+        if (want > 0 && sizes[k] > want) continue;
+        const int m = d2f::max_clusters_mixed(sizes[k], smem);
+        if (m <= 0) continue;
+        if (want > 0) return sizes[k];
+        const long t = (long)((d.n_scenes + m - 1) / m) * cost[k];
+        if (best == 1 || t < best_t) { best = sizes[k]; best_t = t; }
     }
-    return m8 > 0 ? 8 : 1;
+    return best;
 }
 
 // Grid (scene blocks), dynamic shared memory and blocks per scene of a launch on the current

@@ -1412,7 +1412,7 @@ int occupancy_mixed(int nt, int minb, int smem);
 // threads per block of the cluster path (a block per SM: 16 warps to hide the latency of a
 // large scene's passes, 128 registers a thread)
 constexpr int kClusterThreads = 512;
-// the mixed kernel with a cluster of cs (8 or 16) kClusterThreads-thread blocks per scene
+// the mixed kernel with a cluster of cs (8, 12 or 16) kClusterThreads-thread blocks per scene
 // (pncg_mixed_cluster.cu): grid = clusters x cs blocks; max_clusters_mixed = the clusters
 // that fit on the device at once (0: that cluster size cannot be launched)
 cudaError_t launch_mixed_cluster(int cs, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st);

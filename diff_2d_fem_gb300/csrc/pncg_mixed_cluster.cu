@@ -1,6 +1,6 @@
 // pncg_mixed_cluster.cu — the mixed-precision step kernel with one thread-block cluster per
 // scene (pncg_mixed_kernel.cuh, CS > 1), for large scenes: one block cannot keep a scene of
-// 10^5 nodes moving, while a cluster of 8 or 16 blocks on as many SMs splits every phase and
+// 10^5 nodes moving, while a cluster of 8, 12 or 16 blocks on as many SMs splits every phase and
 // combines its reductions through distributed shared memory.
 #include "pncg_mixed_kernel.cuh"
 
@@ -63,12 +63,14 @@ int max_clusters_c(int smem) {
 
 cudaError_t launch_mixed_cluster(int cs, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
     if (cs == 16) return launch_c<16>(d, grid, smem, st);
+    if (cs == 12) return launch_c<12>(d, grid, smem, st);
     if (cs == 8) return launch_c<8>(d, grid, smem, st);
     return cudaErrorInvalidConfiguration;
 }
 
 int max_clusters_mixed(int cs, int smem) {
     if (cs == 16) return max_clusters_c<16>(smem);
+    if (cs == 12) return max_clusters_c<12>(smem);
     if (cs == 8) return max_clusters_c<8>(smem);
     return 0;
 }

@@ -39,7 +39,7 @@ def _ranges(ids, B):
 class DeviceSolver:
     """Binds a problem to device memory and a libd2f handle. `precision`: "fp64" or
     "mixed". threads / blocks_per_sm: the scene-block launch shape (0 = library default).
-    blocks_per_scene (mixed): blocks of one cluster per scene, 1, 8 or 16 (0 = library default)."""
+    blocks_per_scene (mixed): blocks of one cluster per scene, 1, 8, 12 or 16 (0 = library default)."""
 
     def __init__(self, prob, precision="fp64", threads=0, blocks_per_sm=0, device="cuda", stream=None,
                  blocks_per_scene=0):

@@ -13,7 +13,7 @@ New keyword-only options, all off by default:
   gtol        stop an environment once its gradient norm falls below gtol x the norm at
               the step's first iteration (in addition to the reference's tests).
   threads, blocks_per_sm   launch shape of the per-scene kernel (0 = tuned default).
-  blocks_per_scene         mixed precision: a cluster of 8 or 16 blocks per scene for large
+  blocks_per_scene         mixed precision: a cluster of 8, 12 or 16 blocks per scene for large
                            scenes (0 = library default, 1 = a block per scene).
 """
 from __future__ import annotations

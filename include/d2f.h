@@ -137,10 +137,10 @@ typedef struct d2f_scene_desc {
     int32_t line_search;         /* 0 off, 1 on */
     int32_t n_backtrack;         /* halvings tried per iteration */
     int32_t blocks_per_scene;    /* mixed precision: thread blocks working on one scene, as one
-                                    cluster of 512-thread blocks: 1, 8 or 16 (0: a cluster of 16
-                                    or 8, whichever finishes the batch first, when the batch has
-                                    fewer scenes than SMs and at least 16384 nodes per scene;
-                                    else 1) */
+                                    cluster of 512-thread blocks: 1, 8, 12 or 16 (0: a cluster of
+                                    16, 12 or 8, whichever finishes the batch first, when the
+                                    batch has fewer scenes than SMs and at least 16384 nodes per
+                                    scene; else 1) */
     const int32_t *a_ptr;        /* n_aff + 1: affine body b owns entries a_ptr[b] .. a_ptr[b+1]-1 of
                                     a_node / a_grp / a_w (required with affine bodies) */
     /* springs and pins (Springs, implicit/actuation.py:381-476): E = k/2 (|x_a - x_b| - L0)^2,
@@ -221,7 +221,7 @@ int32_t d2f_contact_force(d2f_solver *s, int32_t what, int32_t collider, int32_t
 int32_t d2f_energy(d2f_solver *s, double *out, void *stream);
 
 /* The launch shape d2f_step uses: blocks launched, threads per block, blocks per scene (1: a
- * block per scene; 8 or 16: one cluster per scene). Null outputs are skipped. */
+ * block per scene; 8, 12 or 16: one cluster per scene). Null outputs are skipped. */
 int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads, int32_t *blocks_per_scene);
 
 /* Size of the library's static device scratch used by d2f_step_noalloc (16 MiB). */

@@ -1,4 +1,4 @@
-"""The mixed step with one thread-block cluster per scene (blocks_per_scene 8 or 16): every
+"""The mixed step with one thread-block cluster per scene (blocks_per_scene 8, 12 or 16): every
 phase split over the cluster's blocks, reductions combined through distributed shared memory,
 the contact list compacted across the blocks in pair order, affine bodies spread over the
 cluster's warps and threads.
@@ -41,7 +41,7 @@ def _run(prob, steps, precision, cs=0):
     return out
 
 
-@pytest.mark.parametrize("cs", [8, 16])
+@pytest.mark.parametrize("cs", [8, 12, 16])
 @pytest.mark.parametrize("name", ["strip_small", "grip", "tendon"])
 def test_cluster_matches_fp64_when_converged(name, cs):
     """Ground contact and friction (strip), kinematic grip with IPC contact (grip), tendons
