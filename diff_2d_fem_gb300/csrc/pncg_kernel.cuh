@@ -23,10 +23,9 @@
 // algebraically equal to ddot(dF, nh_d2PsidF2_dir(F, dF)) of core/math.py:84-93 for the
 // rank-one dF = e_c b^T of a unit nodal move.
 //
-// Template parameter R is the element/preconditioner arithmetic type: double for the plain
-// FP64 path, float for the mixed path. Positions, the inertial predictor, the per-scene
-// dot products, energies and step lengths are FP64 in both; the mixed path forms each
-// triangle from FP64 edge differences rounded to FP32.
+// Template parameter R is the element/preconditioner arithmetic type; the library
+// instantiates it with double (the mixed-precision step is pncg_mixed_kernel.cuh). This
+// header also holds the device code both step kernels share.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -139,7 +138,6 @@ __device__ __forceinline__ bool excluded(const d2f_scene_desc &d, int slot, int 
 // ---------------------------------------------------------------------- the kernel
 template <class R, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_constant__ d2f_scene_desc d) {
-    constexpr bool MIXED = sizeof(R) == 4;
     using R2 = typename R2T<R>::T;
     using R4 = typename R4T<R>::T;
     constexpr int NW = NT / 32;
@@ -179,9 +177,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
     const double2 *Tgt = reinterpret_cast<const double2 *>(d.bc_target);
     double2 *Xref = reinterpret_cast<double2 *>(d.xref);
     double2 *Ctr = reinterpret_cast<double2 *>(d.cand_tr);
-    double2 *U = reinterpret_cast<double2 *>(d.xu);                 // x - rest (mixed path)
-    const double2 *Xr = reinterpret_cast<const double2 *>(d.xrest);
-    const R4 *Dmr = reinterpret_cast<const R4 *>(d.Dm);
 
     if (tid < n_col && tid < MAX_COL) {
         const double *c = d.colliders + 8 * tid;
@@ -636,10 +631,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 double2 nx = alpha_s >= 1.0 ? tg : make_double2(x.x + alpha_s * (tg.x - x.x), x.y + alpha_s * (tg.y - x.y));
                 X[n] = nx;
                 Xh[n] = nx;
-                if constexpr (MIXED) {
-                    const double2 xr = Xr[n];
-                    U[n] = make_double2(nx.x - xr.x, nx.y - xr.y);
-                }
             }
             if (tid == 0) S.q_inf = v[0];
             __syncthreads();
@@ -659,13 +650,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             __syncthreads();
         }
 
-        if constexpr (MIXED) {  // displacement from rest, FP64, for the FP32 element routine
-            for (int i = n0 + tid; i < n1; i += NT) {
-                const double2 xi = X[i], xr = Xr[i];
-                U[i] = make_double2(xi.x - xr.x, xi.y - xr.y);
-            }
-            __syncthreads();
-        }
 
         // ================================================================ PNCG iterations
         for (int it = 0; it < d.iter_max; ++it) {
@@ -686,41 +670,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 const R4 B = Bm[t];
                 const R A = Ar[t], mu = Mu[t], la = La[t];
                 R e1x, e1y, e2x, e2y, G00, G01, G10, G11, c1, P00, P01, P10, P11;
-                if constexpr (MIXED) {
-                    // F = I + H, H from FP64 displacement differences: every term of P below
-                    // is O(strain), so FP32 rounding stays relative to the stress, not to mu.
-                    const double2 u0 = U[i0], u1 = U[i1], u2 = U[i2];
-                    const R d1x = R(u1.x - u0.x), d1y = R(u1.y - u0.y), d2x = R(u2.x - u0.x), d2y = R(u2.y - u0.y);
-                    const R4 Dm = Dmr[t];  // rest edge vectors (X1 - X0, X2 - X0)
-                    e1x = Dm.x + d1x; e1y = Dm.y + d1y; e2x = Dm.z + d2x; e2y = Dm.w + d2y;
-                    const R H00 = d1x * B.x + d2x * B.z, H01 = d1x * B.y + d2x * B.w;
-                    const R H10 = d1y * B.x + d2y * B.z, H11 = d1y * B.y + d2y * B.w;
-                    const R dH = H00 * H11 - H01 * H10;
-                    const R Jm1 = (H00 + H11) + dH;                         // J - 1
-                    const R J = R(1) + Jm1;
-                    const R logJ = J > R(1.0e-6) ? log1pf(Jm1) : rlog<R>(R(1.0e-6));
-                    const R iJ = J != R(0) ? R(1) / J : R(0);
-                    G00 = (R(1) + H11) * iJ; G01 = -H10 * iJ; G10 = -H01 * iJ; G11 = (R(1) + H00) * iJ;
-                    c1 = la * logJ - mu;
-                    // mu (F - F^-T) + la log J F^-T with F - F^-T = ((J + 1) H_diag + det H, J H_off + ...) / J
-                    const R onepJ = R(1) + J, ll = la * logJ;
-                    P00 = mu * ((H00 * onepJ + dH) * iJ) + ll * G00;
-                    P01 = mu * ((J * H01 + H10) * iJ) + ll * G01;
-                    P10 = mu * ((J * H10 + H01) * iJ) + ll * G10;
-                    P11 = mu * ((H11 * onepJ + dH) * iJ) + ll * G11;
-                } else {
-                    const double2 x0 = X[i0], x1 = X[i1], x2 = X[i2];
-                    e1x = R(x1.x - x0.x); e1y = R(x1.y - x0.y); e2x = R(x2.x - x0.x); e2y = R(x2.y - x0.y);
-                    const R F00 = e1x * B.x + e2x * B.z, F01 = e1x * B.y + e2x * B.w;
-                    const R F10 = e1y * B.x + e2y * B.z, F11 = e1y * B.y + e2y * B.w;
-                    const R J = F00 * F11 - F10 * F01;
-                    const R logJ = rlog<R>(rmax<R>(J, R(1.0e-6)));
-                    const R iJ = J != R(0) ? R(1) / J : R(0);
-                    G00 = F11 * iJ; G01 = -F10 * iJ; G10 = -F01 * iJ; G11 = F00 * iJ;  // F^-T
-                    c1 = la * logJ - mu;
-                    P00 = mu * F00 + c1 * G00; P01 = mu * F01 + c1 * G01;
-                    P10 = mu * F10 + c1 * G10; P11 = mu * F11 + c1 * G11;
-                }
+                const double2 x0 = X[i0], x1 = X[i1], x2 = X[i2];
+                e1x = R(x1.x - x0.x); e1y = R(x1.y - x0.y); e2x = R(x2.x - x0.x); e2y = R(x2.y - x0.y);
+                const R F00 = e1x * B.x + e2x * B.z, F01 = e1x * B.y + e2x * B.w;
+                const R F10 = e1y * B.x + e2y * B.z, F11 = e1y * B.y + e2y * B.w;
+                const R J = F00 * F11 - F10 * F01;
+                const R logJ = rlog<R>(rmax<R>(J, R(1.0e-6)));
+                const R iJ = J != R(0) ? R(1) / J : R(0);
+                G00 = F11 * iJ; G01 = -F10 * iJ; G10 = -F01 * iJ; G11 = F00 * iJ;  // F^-T
+                c1 = la * logJ - mu;
+                P00 = mu * F00 + c1 * G00; P01 = mu * F01 + c1 * G01;
+                P10 = mu * F10 + c1 * G10; P11 = mu * F11 + c1 * G11;
                 const R hA = rh2 * A;
                 const R g1x = hA * (P00 * B.x + P01 * B.y), g1y = hA * (P10 * B.x + P11 * B.y);
                 const R g2x = hA * (P00 * B.z + P01 * B.w), g2y = hA * (P10 * B.z + P11 * B.w);
@@ -1372,10 +1332,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                         continue;
                     }
                     X[i] = nx;
-                    if constexpr (MIXED) {
-                        const double2 xr = Xr[i];
-                        U[i] = make_double2(nx.x - xr.x, nx.y - xr.y);
-                    }
                 }
                 __syncthreads();
             }
