@@ -295,6 +295,20 @@ def run_ours(args, rank, world):
         tdist.init_process_group("nccl")
     dev = torch.device("cuda", torch.cuda.current_device())
 
+    if args.profile_large:  # the large-scene step alone, for profilers: warmup + steps, nothing else
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            m, kw, dt = workloads.slab_with_holes(args.profile_large, seed=0)
+            prob = scene.solver_problem(m, ImplicitIntegrator(**kw), dt)
+        sol = DeviceSolver(prob, precision="mixed")
+        for _ in range(args.warmup + args.steps):
+            sol.step()
+        torch.cuda.synchronize(dev)
+        it, ac, st = sol.stats()
+        print(json.dumps({"profile_large": True, "scenes": int(prob["B"]), "launch": sol.launch_shape(),
+                          "iters_mean": float(np.mean(it)), "status_ok": bool((st == 0).all())}))
+        return
     m, kw, dt = workloads.rectangles_on_ground(args.scenes, seed=rank)
     integ = ImplicitIntegrator(precision=args.precision, **kw)
     integ.threads, integ.blocks_per_sm = 0, 0
@@ -486,6 +500,8 @@ def main():
     ap.add_argument("--no-grads", action="store_true", help="skip the grads/s measurement")
     ap.add_argument("--no-large", action="store_true", help="skip the large-scene measurement")
     ap.add_argument("--large-steps", type=int, default=3, help="large-scene workload: timed steps")
+    ap.add_argument("--profile-large", type=int, default=0,
+                    help="run only the large-scene step (this many slabs), for profilers")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only warmup + steps of the step kernel (for ncu)")
     args = ap.parse_args()

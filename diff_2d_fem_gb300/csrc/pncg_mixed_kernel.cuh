@@ -229,6 +229,69 @@ constexpr int REL_CAP = 512;
 // of dynamic shared memory the exhaustive build holds its positions in
 static_assert(HASH_MIN_NB >= HASH_B, "hash tables must fit the boundary-position buffer");
 
+// AffineBodies.gather (affine.py:156-175) for bodies b0, b0 + stride, ... < b1: a warp per
+// body over the body's own nodes (lane of 32), J^T g and J^T D J summed in a fixed shuffle
+// tree (FP64). Out of line: its 18 accumulators would otherwise weigh on the register
+// allocation of the whole step kernel, in which affine bodies are a rare path.
+static __device__ __noinline__ void affine_gather(const d2f_scene_desc &d, const float2 *G, const float2 *D, int b0,
+                                                  int b1, int stride, int lane) {
+    for (int b = b0; b < b1; b += stride) {
+        double v[18];
+#pragma unroll
+        for (int q = 0; q < 18; ++q) v[q] = 0.0;
+        const int k1 = d.a_ptr[b + 1];
+        for (int k = d.a_ptr[b] + lane; k < k1; k += 32) {
+            const int i = d.a_node[k];
+            const double *w = d.a_w + 3 * k;
+            const float2 g = G[i], dg = D[i];
+            const double gx = g.x, gy = g.y, dx = dg.x, dy = dg.y;
+            v[0] += gx * w[0]; v[1] += gx * w[1]; v[2] += gx * w[2];
+            v[3] += gy * w[0]; v[4] += gy * w[1]; v[5] += gy * w[2];
+            const double o[6] = {w[0] * w[0], w[0] * w[1], w[0] * w[2], w[1] * w[1], w[1] * w[2], w[2] * w[2]};
+#pragma unroll
+            for (int q = 0; q < 6; ++q) { v[6 + q] += dx * o[q]; v[12 + q] += dy * o[q]; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int q = 0; q < 18; ++q) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+        }
+        if (lane == 0) {
+            for (int q = 0; q < 6; ++q) {
+                d.a_gq_prev[6 * b + q] = d.a_gq[6 * b + q];
+                d.a_gq[6 * b + q] = v[q];
+            }
+            for (int q = 0; q < 12; ++q) d.a_H[18 * b + q] = v[6 + q];
+        }
+    }
+}
+
+// affine_reduce_kernel (affine.py:178-205) for bodies b0, b0 + stride, ... < b1: each body's
+// 6x6 solve by this thread (FP64), its five Dai-Kou terms added to ab (g.z, g.p, g.zy, y.p,
+// y.zy). Out of line for the same reason as affine_gather.
+static __device__ __noinline__ void affine_solve(const d2f_scene_desc &d, double h2, int b0, int b1, int stride,
+                                                 double *ab) {
+    for (int b = b0; b < b1; b += stride) {
+        const double *q = d.a_q + 6 * b;
+        const M2 A{q[1], q[2], q[4], q[5]};
+        const M2 Pm = nh_P(A, d.a_Mu[b], d.a_La[b]);
+        double g[6], y[6], z[6], zy[6], H[6][6], L[6][6];
+        const double hp[6] = {0.0, h2 * Pm.a, h2 * Pm.b, 0.0, h2 * Pm.c, h2 * Pm.d};
+        for (int r = 0; r < 6; ++r) g[r] = d.a_gq[6 * b + r] + hp[r];
+        reduced_hessian(A, d.a_Mu[b], d.a_La[b], h2, d.a_H + 18 * b, H);
+        chol6(H, L);
+        for (int r = 0; r < 6; ++r) y[r] = g[r] - d.a_gq_prev[6 * b + r];
+        chol6_solve(L, g, z);
+        chol6_solve(L, y, zy);
+        const double *pq = d.a_pq + 6 * b;
+        for (int r = 0; r < 6; ++r) {
+            ab[0] += g[r] * z[r]; ab[1] += g[r] * pq[r]; ab[2] += g[r] * zy[r];
+            ab[3] += y[r] * pq[r]; ab[4] += y[r] * zy[r];
+        }
+        for (int r = 0; r < 6; ++r) { d.a_gq[6 * b + r] = g[r]; d.a_zq[6 * b + r] = z[r]; }
+    }
+}
+
 // ---------------------------------------------------------------------- the kernel
 // Device pointers of the per-step scratch parts (host-computed from d2f_scene_desc.mscr).
 struct MixedPtrs {
@@ -1314,37 +1377,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             }
 
             // ---------------------------------------------- A4: body-level modes
-            // AffineBodies.gather, affine.py:156-175: a warp per body over the body's own nodes,
-            // summed in a fixed shuffle tree (FP64)
-            for (int b = sg.aff0 + (gt >> 5); b < sg.aff0 + sg.naff; b += GS / 32) {
-                double v[18];
-#pragma unroll
-                for (int q = 0; q < 18; ++q) v[q] = 0.0;
-                const int k1 = d.a_ptr[b + 1];
-                for (int k = d.a_ptr[b] + (tid & 31); k < k1; k += 32) {
-                    const int i = d.a_node[k];
-                    const double *w = d.a_w + 3 * k;
-                    const float2 g = G[i], dg = D[i];
-                    const double gx = g.x, gy = g.y, dx = dg.x, dy = dg.y;
-                    v[0] += gx * w[0]; v[1] += gx * w[1]; v[2] += gx * w[2];
-                    v[3] += gy * w[0]; v[4] += gy * w[1]; v[5] += gy * w[2];
-                    const double o[6] = {w[0] * w[0], w[0] * w[1], w[0] * w[2], w[1] * w[1], w[1] * w[2], w[2] * w[2]};
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) { v[6 + q] += dx * o[q]; v[12 + q] += dy * o[q]; }
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-                    for (int q = 0; q < 18; ++q) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
-                }
-                if ((tid & 31) == 0) {
-                    for (int q = 0; q < 6; ++q) {
-                        d.a_gq_prev[6 * b + q] = d.a_gq[6 * b + q];
-                        d.a_gq[6 * b + q] = v[q];
-                    }
-                    for (int q = 0; q < 12; ++q) d.a_H[18 * b + q] = v[6 + q];
-                }
-            }
+            // AffineBodies.gather, affine.py:156-175: a warp per body
+            if (sg.naff > 0) affine_gather(d, G, D, sg.aff0 + (gt >> 5), sg.aff0 + sg.naff, GS / 32, tid & 31);
             if (sg.naff > 0) {
                 gsync();
                 for (int k = sg.affn0 + gt; k < sg.affn0 + sg.naffn; k += GS) G[d.a_node[k]] = make_float2(0.f, 0.f);
@@ -1429,25 +1463,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 // (FP64), its five Dai-Kou terms summed over the bodies in a fixed tree
                 double ab[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // gPg, g.p, g.Py, y.p, y.Py of the bodies
                 if (sg.naff > 0) {
-                    for (int b = sg.aff0 + gt; b < sg.aff0 + sg.naff; b += GS) {
-                        const double *q = d.a_q + 6 * b;
-                        const M2 A{q[1], q[2], q[4], q[5]};
-                        const M2 Pm = nh_P(A, d.a_Mu[b], d.a_La[b]);
-                        double g[6], y[6], z[6], zy[6], H[6][6], L[6][6];
-                        const double hp[6] = {0.0, h2 * Pm.a, h2 * Pm.b, 0.0, h2 * Pm.c, h2 * Pm.d};
-                        for (int r = 0; r < 6; ++r) g[r] = d.a_gq[6 * b + r] + hp[r];
-                        reduced_hessian(A, d.a_Mu[b], d.a_La[b], h2, d.a_H + 18 * b, H);
-                        chol6(H, L);
-                        for (int r = 0; r < 6; ++r) y[r] = g[r] - d.a_gq_prev[6 * b + r];
-                        chol6_solve(L, g, z);
-                        chol6_solve(L, y, zy);
-                        const double *pq = d.a_pq + 6 * b;
-                        for (int r = 0; r < 6; ++r) {
-                            ab[0] += g[r] * z[r]; ab[1] += g[r] * pq[r]; ab[2] += g[r] * zy[r];
-                            ab[3] += y[r] * pq[r]; ab[4] += y[r] * zy[r];
-                        }
-                        for (int r = 0; r < 6; ++r) { d.a_gq[6 * b + r] = g[r]; d.a_zq[6 * b + r] = z[r]; }
-                    }
+                    affine_solve(d, h2, sg.aff0 + gt, sg.aff0 + sg.naff, GS, ab);
                     const int ops5[5] = {0, 0, 0, 0, 0};
                     scene_reduce<NT, CS, 5>(ab, ops5, red, cres);
                 }
