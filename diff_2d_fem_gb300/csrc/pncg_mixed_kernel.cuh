@@ -220,8 +220,8 @@ __device__ __forceinline__ double2 tendon_dlen(PosF pos, const int32_t *t_node, 
 constexpr int REBASE = 64;
 // packed per-node flags (NINFO.x): bits 0-1 free mask, then these, bits 4-7 the rigid piece
 constexpr int NI_AFF = 4, NI_RIG = 8;
-// contact candidate lists of scenes with at least HASH_MIN_NB boundary nodes are built through
-// a spatial hash of HASH_B buckets (every other scene tests all edge-node pairs)
+// contact candidate lists of scenes with at least HASH_MIN_NB boundary nodes on a cluster are
+// built through a spatial hash of HASH_B buckets (every other scene tests all edge-node pairs)
 constexpr int HASH_MIN_NB = 4096, HASH_B = 4096;
 // the cluster path's ACCD replay: candidates below the running cap, per block
 constexpr int REL_CAP = 512;
@@ -232,17 +232,19 @@ static_assert(HASH_MIN_NB >= HASH_B, "hash tables must fit the boundary-position
 // AffineBodies.gather (affine.py:156-175) for bodies b0, b0 + stride, ... < b1: a warp per
 // body over the body's own nodes (lane of 32), J^T g and J^T D J summed in a fixed shuffle
 // tree (FP64). Out of line: its 18 accumulators would otherwise weigh on the register
-// allocation of the whole step kernel, in which affine bodies are a rare path.
-static __device__ __noinline__ void affine_gather(const d2f_scene_desc &d, const float2 *G, const float2 *D, int b0,
-                                                  int b1, int stride, int lane) {
+// allocation of the whole step kernel, in which affine bodies are a rare path. (Plain
+// pointers, not the descriptor: a reference to it would copy it into every thread's stack.)
+static __device__ __noinline__ void affine_gather(const int32_t *a_ptr, const int32_t *a_node, const double *a_w,
+                                                  const float2 *G, const float2 *D, double *a_gq, double *a_gq_prev,
+                                                  double *a_H, int b0, int b1, int stride, int lane) {
     for (int b = b0; b < b1; b += stride) {
         double v[18];
 #pragma unroll
         for (int q = 0; q < 18; ++q) v[q] = 0.0;
-        const int k1 = d.a_ptr[b + 1];
-        for (int k = d.a_ptr[b] + lane; k < k1; k += 32) {
-            const int i = d.a_node[k];
-            const double *w = d.a_w + 3 * k;
+        const int k1 = a_ptr[b + 1];
+        for (int k = a_ptr[b] + lane; k < k1; k += 32) {
+            const int i = a_node[k];
+            const double *w = a_w + 3 * k;
             const float2 g = G[i], dg = D[i];
             const double gx = g.x, gy = g.y, dx = dg.x, dy = dg.y;
             v[0] += gx * w[0]; v[1] += gx * w[1]; v[2] += gx * w[2];
@@ -258,10 +260,10 @@ static __device__ __noinline__ void affine_gather(const d2f_scene_desc &d, const
         }
         if (lane == 0) {
             for (int q = 0; q < 6; ++q) {
-                d.a_gq_prev[6 * b + q] = d.a_gq[6 * b + q];
-                d.a_gq[6 * b + q] = v[q];
+                a_gq_prev[6 * b + q] = a_gq[6 * b + q];
+                a_gq[6 * b + q] = v[q];
             }
-            for (int q = 0; q < 12; ++q) d.a_H[18 * b + q] = v[6 + q];
+            for (int q = 0; q < 12; ++q) a_H[18 * b + q] = v[6 + q];
         }
     }
 }
@@ -269,26 +271,28 @@ static __device__ __noinline__ void affine_gather(const d2f_scene_desc &d, const
 // affine_reduce_kernel (affine.py:178-205) for bodies b0, b0 + stride, ... < b1: each body's
 // 6x6 solve by this thread (FP64), its five Dai-Kou terms added to ab (g.z, g.p, g.zy, y.p,
 // y.zy). Out of line for the same reason as affine_gather.
-static __device__ __noinline__ void affine_solve(const d2f_scene_desc &d, double h2, int b0, int b1, int stride,
-                                                 double *ab) {
+static __device__ __noinline__ void affine_solve(const double *a_q, const double *a_Mu, const double *a_La,
+                                                 double *a_gq, const double *a_gq_prev, const double *a_H,
+                                                 const double *a_pq, double *a_zq, double h2, int b0, int b1,
+                                                 int stride, double *ab) {
     for (int b = b0; b < b1; b += stride) {
-        const double *q = d.a_q + 6 * b;
+        const double *q = a_q + 6 * b;
         const M2 A{q[1], q[2], q[4], q[5]};
-        const M2 Pm = nh_P(A, d.a_Mu[b], d.a_La[b]);
+        const M2 Pm = nh_P(A, a_Mu[b], a_La[b]);
         double g[6], y[6], z[6], zy[6], H[6][6], L[6][6];
         const double hp[6] = {0.0, h2 * Pm.a, h2 * Pm.b, 0.0, h2 * Pm.c, h2 * Pm.d};
-        for (int r = 0; r < 6; ++r) g[r] = d.a_gq[6 * b + r] + hp[r];
-        reduced_hessian(A, d.a_Mu[b], d.a_La[b], h2, d.a_H + 18 * b, H);
+        for (int r = 0; r < 6; ++r) g[r] = a_gq[6 * b + r] + hp[r];
+        reduced_hessian(A, a_Mu[b], a_La[b], h2, a_H + 18 * b, H);
         chol6(H, L);
-        for (int r = 0; r < 6; ++r) y[r] = g[r] - d.a_gq_prev[6 * b + r];
+        for (int r = 0; r < 6; ++r) y[r] = g[r] - a_gq_prev[6 * b + r];
         chol6_solve(L, g, z);
         chol6_solve(L, y, zy);
-        const double *pq = d.a_pq + 6 * b;
+        const double *pq = a_pq + 6 * b;
         for (int r = 0; r < 6; ++r) {
             ab[0] += g[r] * z[r]; ab[1] += g[r] * pq[r]; ab[2] += g[r] * zy[r];
             ab[3] += y[r] * pq[r]; ab[4] += y[r] * zy[r];
         }
-        for (int r = 0; r < 6; ++r) { d.a_gq[6 * b + r] = g[r]; d.a_zq[6 * b + r] = z[r]; }
+        for (int r = 0; r < 6; ++r) { a_gq[6 * b + r] = g[r]; a_zq[6 * b + r] = z[r]; }
     }
 }
 
@@ -348,6 +352,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     __shared__ int s_wcnt[NW];
     __shared__ unsigned s_wmask[NW];
     __shared__ double colmu[MAX_COL];
+    __shared__ double s_H6[6][6], s_L6[6][6];  // the batch kernel's affine 6x6 solve (thread 0)
     __shared__ float s_zf[8][3], s_cs[8][2];  // rigid-mode correction of up to 8 pieces, FP32
     __shared__ float colf[MAX_COL][2], colmuf[MAX_COL];  // half-space normals, friction (FP32)
     extern __shared__ float2 pos32[];
@@ -642,7 +647,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             gsync();
             // boundary positions in FP32 relative to the first boundary node: in shared memory
             // (every block its own copy), or for hashed scenes in PB, written once per scene
-            const bool hashed = nbl >= HASH_MIN_NB;
+            // (the hashed build is compiled into the cluster kernels only: the batch kernel, a
+            // block per scene of small scenes, keeps its registers for the iteration)
+            const bool hashed = CL && nbl >= HASH_MIN_NB;
             float2 *P32 = hashed ? PB + sg.bnd0 : pos32;
             const double2 anchor = xpos(d.bnd[sg.bnd0]);
             for (int j = hashed ? gt : tid; j < nbl; j += hashed ? GS : NT) {
@@ -1377,8 +1384,40 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             }
 
             // ---------------------------------------------- A4: body-level modes
-            // AffineBodies.gather, affine.py:156-175: a warp per body
-            if (sg.naff > 0) affine_gather(d, G, D, sg.aff0 + (gt >> 5), sg.aff0 + sg.naff, GS / 32, tid & 31);
+            // AffineBodies.gather, affine.py:156-175: on a cluster a warp per body (out of line);
+            // in the batch kernel the block per body, inline (a call would make every thread
+            // save its registers around it and double the kernel's stack frame)
+            if constexpr (CL) {
+                if (sg.naff > 0)
+                    affine_gather(d.a_ptr, d.a_node, d.a_w, G, D, d.a_gq, d.a_gq_prev, d.a_H, sg.aff0 + (gt >> 5),
+                                  sg.aff0 + sg.naff, GS / 32, tid & 31);
+            } else {
+                for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b) {
+                    double v[18];
+#pragma unroll
+                    for (int q = 0; q < 18; ++q) v[q] = 0.0;
+                    for (int k = d.a_ptr[b] + tid; k < d.a_ptr[b + 1]; k += NT) {
+                        const int i = d.a_node[k];
+                        const double *w = d.a_w + 3 * k;
+                        const float2 g = G[i], dg = D[i];
+                        const double gx = g.x, gy = g.y, dx = dg.x, dy = dg.y;
+                        v[0] += gx * w[0]; v[1] += gx * w[1]; v[2] += gx * w[2];
+                        v[3] += gy * w[0]; v[4] += gy * w[1]; v[5] += gy * w[2];
+                        const double o[6] = {w[0] * w[0], w[0] * w[1], w[0] * w[2], w[1] * w[1], w[1] * w[2], w[2] * w[2]};
+#pragma unroll
+                        for (int q = 0; q < 6; ++q) { v[6 + q] += dx * o[q]; v[12 + q] += dy * o[q]; }
+                    }
+                    const int ops[18] = {0};
+                    block_reduce<NT, 18>(v, ops, red);
+                    if (tid == 0) {
+                        for (int q = 0; q < 6; ++q) {
+                            d.a_gq_prev[6 * b + q] = d.a_gq[6 * b + q];
+                            d.a_gq[6 * b + q] = v[q];
+                        }
+                        for (int q = 0; q < 12; ++q) d.a_H[18 * b + q] = v[6 + q];
+                    }
+                }
+            }
             if (sg.naff > 0) {
                 gsync();
                 for (int k = sg.affn0 + gt; k < sg.affn0 + sg.naffn; k += GS) G[d.a_node[k]] = make_float2(0.f, 0.f);
@@ -1462,10 +1501,33 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 // affine_reduce_kernel, affine.py:178-205: each body's 6x6 solve by one thread
                 // (FP64), its five Dai-Kou terms summed over the bodies in a fixed tree
                 double ab[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // gPg, g.p, g.Py, y.p, y.Py of the bodies
-                if (sg.naff > 0) {
-                    affine_solve(d, h2, sg.aff0 + gt, sg.aff0 + sg.naff, GS, ab);
-                    const int ops5[5] = {0, 0, 0, 0, 0};
-                    scene_reduce<NT, CS, 5>(ab, ops5, red, cres);
+                if constexpr (CL) {  // a thread per body, out of line
+                    if (sg.naff > 0) {
+                        affine_solve(d.a_q, d.a_Mu, d.a_La, d.a_gq, d.a_gq_prev, d.a_H, d.a_pq, d.a_zq, h2, sg.aff0 + gt,
+                                     sg.aff0 + sg.naff, GS, ab);
+                        const int ops5[5] = {0, 0, 0, 0, 0};
+                        scene_reduce<NT, CS, 5>(ab, ops5, red, cres);
+                    }
+                } else if (tid == 0) {  // the batch kernel: thread 0, inline, 6x6 work in shared memory
+                    for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b) {
+                        const double *q = d.a_q + 6 * b;
+                        const M2 A{q[1], q[2], q[4], q[5]};
+                        const M2 Pm = nh_P(A, d.a_Mu[b], d.a_La[b]);
+                        double g[6], y[6], z[6], zy[6];
+                        const double hp[6] = {0.0, h2 * Pm.a, h2 * Pm.b, 0.0, h2 * Pm.c, h2 * Pm.d};
+                        for (int r = 0; r < 6; ++r) g[r] = d.a_gq[6 * b + r] + hp[r];
+                        reduced_hessian(A, d.a_Mu[b], d.a_La[b], h2, d.a_H + 18 * b, s_H6);
+                        chol6(s_H6, s_L6);
+                        for (int r = 0; r < 6; ++r) y[r] = g[r] - d.a_gq_prev[6 * b + r];
+                        chol6_solve(s_L6, g, z);
+                        chol6_solve(s_L6, y, zy);
+                        const double *pq = d.a_pq + 6 * b;
+                        for (int r = 0; r < 6; ++r) {
+                            ab[0] += g[r] * z[r]; ab[1] += g[r] * pq[r]; ab[2] += g[r] * zy[r];
+                            ab[3] += y[r] * pq[r]; ab[4] += y[r] * zy[r];
+                        }
+                        for (int r = 0; r < 6; ++r) { d.a_gq[6 * b + r] = g[r]; d.a_zq[6 * b + r] = z[r]; }
+                    }
                 }
                 if (tid == 0) {  // B2: per-scene scalars, FP64 (every block of a cluster alike)
                     const double gPg = vs[0] + S.gPg + ab[0], g_p = vs[1] + ab[1], g_Py = vs[2] + S.g_Py + ab[2];
