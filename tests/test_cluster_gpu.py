@@ -111,9 +111,9 @@ def test_large_scenes_default_to_clusters():
 
 @pytest.mark.parametrize("cs", [1, 16])
 def test_hashed_contact_list_matches_fp64(cs):
-    """A slab with 4792 boundary nodes (the contact list built through the spatial hash, on a
-    block or a cluster) and six discs resting within the barrier distance on it: three
-    converged steps agree with FP64, whose list is built by testing every edge-node pair."""
+    """A slab with 4792 boundary nodes (the contact list built through the spatial hash on a
+    cluster; by testing every edge-node pair on a block) and six discs resting within the
+    barrier distance on it: three converged steps agree with FP64."""
     from diff_2d_fem_gb300 import workloads, scene, ImplicitIntegrator
     from diff_2d_fem_gb300.device import DeviceSolver
     with warnings.catch_warnings():
