@@ -139,6 +139,22 @@ class ImplicitIntegrator:
                 s.set_springs([k["anchor"] for k in model._springs], [k["length"] for k in model._springs])
             s._ctrl_version = model._ctrl_version
 
+    # ---- contact read-outs (implicit/integrator.py:340-358), computed on the device
+    def collider_force(self, model, index=None, friction=True):
+        """Reaction on the colliders (barrier, + friction unless friction=False) per
+        environment, (B, 2): on collider `index`, or on all of them when index is None."""
+        return model._solver.collider_force(index, include_friction=friction)
+
+    def contact_force(self, model, handle=None, friction=True, colliders=True, bodies=True):
+        """Force contact exerts on each node of a body [N/m], (n_body_nodes, 2), or (N, 2)
+        for every node when handle is None; kinematic nodes included."""
+        f = model._solver.contact_force(friction=friction, colliders=colliders, bodies=bodies)
+        return f if handle is None else f[model.body_nodes(handle)]
+
+    def body_contact_force(self, model, handle, friction=True, colliders=True, bodies=True):
+        """Resultant of contact_force over a body: (fx, fy) [N/m]."""
+        return self.contact_force(model, handle, friction, colliders, bodies).sum(0)
+
     def adjoint(self, model, dt, Emin=1e-3):
         """Adjoint of the implicit solve on this model (implicit/integrator.py:231-250): an
         AdjointPNCG2D over its FP64 solver. Density scales each element's stiffness,

@@ -1,0 +1,104 @@
+"""Physical checks of the device step through the public API, after the reference's
+tests/test_rigid.py and tests/test_scene.py: environments do not interact (bit for bit in
+FP64), a free rigid body falls exactly as backward Euler, a pinned bar swings with the
+period of a physical pendulum."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+G0 = 9.81
+
+
+def _com(model, h):
+    m = np.asarray(model.me.mass, np.float64)[model.body_nodes(h)]
+    return (m[:, None] * model.get_body_x(h)).sum(0) / m.sum()
+
+
+def test_environments_do_not_interact():
+    """A design alone and the same design in a batch of three (the middle one different),
+    pressed by gravity onto a disc: FP64 positions and the disc's reaction identical bit for
+    bit (each scene runs alone in its block, in a fixed order of operations)."""
+    from diff_2d_fem_gb300 import Model, ImplicitIntegrator
+    rng = np.random.default_rng(3)
+    d1 = np.ones((24, 12), np.uint8)
+    d1[6:18, 4:8] = 0
+    d2 = (rng.random((24, 12)) > 0.15).astype(np.uint8)
+    d2[-1] = 1
+    d2[:, 0] = 1
+
+    def run(designs):
+        m = Model()
+        m.add_disc(center=(0.05, 0.030), radius=0.006, mu=0.6)
+        hs = [m.add_soft_body(d, physical_size=(0.012, 0.024), center=(0.05, 0.0495), E=1.0e6, nu=0.40,
+                              density=1100.0, env_id=i) for i, d in enumerate(designs)]
+        m.finalize()
+        m.gravity = (0.0, -G0)
+        integ = ImplicitIntegrator(precision="fp64", threads=128)
+        for _ in range(60):
+            integ.simulate(m, 2e-3)
+        return m, hs, integ
+
+    alone, (ha,), ia = run([d1])
+    batch, hb, ib = run([d1, d2, d1])
+    xa = alone.get_body_x(ha)
+    Fa, Fb = ia.collider_force(alone)[0], ib.collider_force(batch)
+    assert np.linalg.norm(Fa) > 0.1, "no contact developed"
+    for env, h in ((0, hb[0]), (2, hb[2])):
+        assert np.array_equal(batch.get_body_x(h), xa), env
+        assert np.array_equal(Fb[env], Fa), env
+    assert np.abs(batch.get_body_x(hb[1]).mean(0) - xa.mean(0)).max() > 1e-6
+
+
+def test_free_rigid_body_is_exact_backward_euler():
+    """Free fall of an affine block: after n steps of h the drop is g h^2 n (n + 1) / 2 (backward
+    Euler), within 1e-9; a free rigid body converges at once."""
+    from diff_2d_fem_gb300 import Model, ImplicitIntegrator
+    m = Model()
+    m.damping = 0.0
+    h = m.add_affine_body(np.ones((6, 6), np.uint8), physical_size=(0.006, 0.006), center=(0.0, 0.05),
+                          density=1000.0)
+    m.finalize()
+    m.gravity = (0.0, -G0)
+    y0 = _com(m, h)[1]
+    integ = ImplicitIntegrator(self_collision=False, friction=False, precision="fp64")
+    for _ in range(100):
+        integ.simulate(m, 1e-3)
+    err = (y0 - _com(m, h)[1]) / (G0 * 1e-6 * 100 * 101 / 2) - 1
+    assert abs(err) < 1e-9, err
+    assert integ.stats(m)["iters"][0] <= 4
+
+
+def test_pin_makes_a_pendulum():
+    """A rigid bar pinned at one end under gravity 10 degrees off its axis swings with the
+    period of a physical pendulum (within 1 %), and the pin holds (within 1 um)."""
+    from diff_2d_fem_gb300 import Model, ImplicitIntegrator
+    m = Model()
+    m.damping = 0.0
+    h = m.add_affine_body(np.ones((4, 24), np.uint8), physical_size=(0.012, 0.002), center=(0.006, 0.0),
+                          density=1100.0)
+    m.finalize()
+    pin = m.add_pin(h, (0.0, 0.0))
+    X = m.rest_x(h)
+    mass = np.asarray(m.me.mass, np.float64)[m.body_nodes(h)]
+    pivot = X[np.linalg.norm(X, axis=1).argmin()]
+    d = np.linalg.norm((mass[:, None] * X).sum(0) / mass.sum() - pivot)
+    Ip = (mass * ((X - pivot) ** 2).sum(1)).sum()
+    th0 = np.deg2rad(10.0)
+    period = 2 * np.pi * np.sqrt(Ip / (mass.sum() * G0 * d)) * (1 + th0 ** 2 / 16)
+    m.gravity = (G0 * np.cos(th0), -G0 * np.sin(th0))
+    dt = 5e-4
+    integ = ImplicitIntegrator(self_collision=False, friction=False, precision="fp64")
+    ang, gap = [], 0.0
+    for _ in range(int(1.1 * period / dt)):
+        integ.simulate(m, dt)
+        ang.append(m.affine_state(0)["angle"] + th0)
+        gap = max(gap, abs(m.spring_force(pin)[1]))
+    ang = np.array(ang)
+    t = dt * np.arange(1, len(ang) + 1)
+    k = np.where(np.sign(ang[1:]) != np.sign(ang[:-1]))[0]
+    assert len(k) >= 2
+    cross = [t[i] - ang[i] * dt / (ang[i + 1] - ang[i]) for i in k[:2]]
+    got = 2.0 * (cross[1] - cross[0])
+    assert abs(got / period - 1.0) < 0.01, (got, period)
+    assert gap < 1e-6, gap
