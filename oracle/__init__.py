@@ -88,6 +88,8 @@ def lib():
         _LIB.d2o_ipc_energy.restype = None
         _LIB.d2o_term.argtypes = [C.POINTER(_Solver), C.c_int, _PD]
         _LIB.d2o_term.restype = None
+        _LIB.d2o_sdf.argtypes = [C.c_int] + [C.c_double] * 5 + [_PD, C.c_int, _PD]
+        _LIB.d2o_sdf.restype = None
     return _LIB
 
 
@@ -347,6 +349,18 @@ def run(prob: dict, steps: int, commands=None):
         xs.append(s.x.copy())
         its.append(s.state["iters"].copy())
     return s, xs, its
+
+
+def sdf(collider_row, pts):
+    """A collider's level set (row of the problem's `colliders`: kind, cx, cy, rx, ry, rref,
+    r, mu) at points (n, 2): the oracle's sdf_eval, the disc's |x - c| - r."""
+    c = np.asarray(collider_row, np.float64)
+    P = _f64(pts, (-1, 2))
+    d = np.zeros(len(P))
+    kind = int(c[0])
+    rx = c[6] if kind == 0 else c[3]
+    lib().d2o_sdf(kind, c[1], c[2], rx, c[4], c[5], P.ctypes.data_as(_PD), len(P), d.ctypes.data_as(_PD))
+    return d
 
 
 def problem_keys():

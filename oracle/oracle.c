@@ -1158,6 +1158,16 @@ static void set_x_from_x0(d2o_solver *s) {
 }
 
 /* ------------------------------------------------------------------ energy, solver.py:453-498 */
+/* The collider level set at n points (test access): sdf_eval(...).d, or |x - c| - r for a
+   disc (kind 0, radius rx). */
+void d2o_sdf(int kind, double cx, double cy, double rx, double ry, double rref, const double *pts, int n,
+             double *d) {
+    for (int i = 0; i < n; ++i) {
+        v2 x = ld(pts, i);
+        d[i] = kind == 0 ? len(sub(x, V(cx, cy))) - rx : sdf_eval(kind, cx, cy, rx, ry, rref, x).d;
+    }
+}
+
 /* ------------------------------------------------------------------ Springs, implicit/actuation.py:381-476 */
 typedef struct { double ten, kt, len; v2 n; } spring_at_t;
 /* _spring (:396-402): tension k (|d| - L0), tangential stiffness max(k (1 - L0/|d|), 0) */
