@@ -138,3 +138,46 @@ def test_every_shape_develops_contact(shape):
     assert fmax > 1.0, fmax
     row = [m._colliders[0][k] for k in ("kind", "cx", "cy", "rx", "ry", "rref", "r", "mu")]
     assert oracle.sdf(row, x).min() > 0.0
+
+
+PX = 0.5e-3
+
+
+@pytest.mark.parametrize("kind,mu,th_deg", [("rigid", 0.0, 40.0), ("rigid", 0.3, 30.0), ("soft", 0.3, 30.0)])
+def test_slides_at_the_coulomb_speed(kind, mu, th_deg):
+    """A block on a held slab under tilted gravity (contact between bodies with friction mu):
+    it rests within the barrier's reach, then slides at the steady speed
+    g (sin th - mu cos th) / c_e of the damped backward-Euler step (c_e = (1 - e^(-c dt)) / dt),
+    within 1 % (rigid) or 2 % (soft) — after the reference's tests/test_ipc.py."""
+    from diff_2d_fem_gb300 import Model, ImplicitIntegrator
+    c, dt = 200.0, 1e-3
+    ce = (1.0 - np.exp(-dt * c)) / dt
+    th = np.deg2rad(th_deg)
+    m = Model()
+    m.damping = c
+    m.body_friction = mu
+    slab = m.add_soft_body(np.ones((6, 60), np.uint8), physical_size=(60 * PX, 6 * PX), center=(0.0, 0.0),
+                           E=1.0e6, nu=0.40, density=1100.0)
+    at = (-0.010, 0.0015 + 0.002 + 0.9 * PX / 8)
+    if kind == "rigid":
+        block = m.add_affine_body(np.ones((8, 8), np.uint8), physical_size=(8 * PX, 8 * PX), center=at,
+                                  density=1100.0)
+    else:
+        block = m.add_soft_body(np.ones((8, 8), np.uint8), physical_size=(8 * PX, 8 * PX), center=at,
+                                E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    m.set_kinematic_constraint(slab, np.arange(m.body_nodes(slab).size))
+    integ = ImplicitIntegrator(precision="fp64")
+    m.gravity = (0.0, -G0 * np.cos(th))
+    for _ in range(100):
+        integ.simulate(m, dt)
+    gap = m.get_body_x(block)[:, 1].min() - m.get_body_x(slab)[:, 1].max()
+    assert 0.5 * m.dhat < gap < m.dhat, gap / m.dhat
+    m.gravity = (G0 * np.sin(th), -G0 * np.cos(th))
+    xs = []
+    for _ in range(300):
+        integ.simulate(m, dt)
+        xs.append(m.get_body_x(block)[:, 0].mean())
+    v = np.diff(np.array(xs)[-200:]).mean() / dt
+    expect = G0 * (np.sin(th) - mu * np.cos(th)) / ce
+    assert abs(v / expect - 1.0) < (0.01 if kind == "rigid" else 0.02), (v, expect)
