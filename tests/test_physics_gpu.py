@@ -1,7 +1,9 @@
 """Physical checks of the device step through the public API, after the reference's
-tests/test_rigid.py and tests/test_scene.py: environments do not interact (bit for bit in
-FP64), a free rigid body falls exactly as backward Euler, a pinned bar swings with the
-period of a physical pendulum."""
+tests/test_rigid.py, test_scene.py, test_objects.py and test_ipc.py: environments do not
+interact (bit for bit in FP64), a free rigid body falls exactly as backward Euler, a pinned
+bar swings with the period of a physical pendulum, every collider shape develops contact
+without a node inside it, a block slides down a held slab at the Coulomb speed, nothing
+passes through anything, momentum goes through an impact."""
 import numpy as np
 import pytest
 
@@ -181,3 +183,55 @@ def test_slides_at_the_coulomb_speed(kind, mu, th_deg):
     v = np.diff(np.array(xs)[-200:]).mean() / dt
     expect = G0 * (np.sin(th) - mu * np.cos(th)) / ce
     assert abs(v / expect - 1.0) < (0.01 if kind == "rigid" else 0.02), (v, expect)
+
+
+def _throw(other, px_per_step, diagonal=False, steps=120):
+    """A rigid block thrown at another body: (smallest gap over the run in units of dhat,
+    whether a node of the thrown block entered a held block's box, relative momentum change)."""
+    from diff_2d_fem_gb300 import Model, ImplicitIntegrator, scene
+    dt = 2.5e-4
+    v0 = px_per_step * PX / dt
+    m = Model()
+    rigid = lambda c: m.add_affine_body(np.ones((8, 8), np.uint8), physical_size=(8 * PX, 8 * PX), center=c,
+                                        density=1100.0)
+    if diagonal:
+        a, at = rigid((-6 * PX, 6 * PX)), (4 * PX, -4 * PX)
+    else:
+        a, at = rigid((0.0, 0.0)), (13 * PX, 0.8 * PX)
+    b = rigid(at) if other == "rigid" else m.add_soft_body(np.ones((8, 8), np.uint8), physical_size=(8 * PX, 8 * PX),
+                                                           center=at, E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    if other == "held":
+        m.set_kinematic_constraint(b, np.arange(m.body_nodes(b).size))
+    m.set_body_velocity(a, velocity=(v0 / np.sqrt(2.0), -v0 / np.sqrt(2.0)) if diagonal else (v0, 0.0))
+    integ = ImplicitIntegrator(friction=False, precision="fp64")
+    mass = np.asarray(m.me.mass, np.float64)
+    mom = lambda: (mass[:, None] * np.concatenate([m.get_body_v(a), m.get_body_v(b)])).sum(0)
+    p0 = mom()
+    gap, inside = np.inf, False
+    for _ in range(steps):
+        integ.simulate(m, dt)
+        prob = dict(m._solver.prob, x=m.get_x())
+        gap = min(gap, float(scene.min_distance(prob).min()) / m.dhat)
+        if other == "held":
+            xa, xb = m.get_body_x(a), m.rest_x(b)
+            lo, hi = xb.min(0) + 1e-9, xb.max(0) - 1e-9
+            inside |= bool(((xa > lo) & (xa < hi)).all(1).any())
+    assert np.isfinite(m.get_x()).all()
+    return gap, inside, float(np.linalg.norm(mom() - p0) / np.linalg.norm(p0))
+
+
+@pytest.mark.parametrize("other,diagonal", [("soft", False), ("rigid", False), ("held", True), ("held", False)])
+def test_nothing_passes_through(other, diagonal):
+    """A rigid block thrown at 5 pixels a step at a soft, a rigid or a held block, head on and
+    corner to corner: the surfaces never touch and nothing enters the held block — after the
+    reference's tests/test_ipc.py."""
+    gap, inside, _ = _throw(other, 5.0, diagonal)
+    assert gap > 0.0 and not inside, (gap, inside)
+
+
+def test_momentum_goes_through_an_impact():
+    """At half a pixel a step into a free soft block, momentum is kept through the impact
+    (within 2e-3)."""
+    _, _, dp = _throw("soft", 0.5)
+    assert dp < 2e-3, dp
