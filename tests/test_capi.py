@@ -68,3 +68,43 @@ def test_struct_mirrors_header():
         if line:
             sn += [v.strip() for v in re.sub(r"^int32_t\s+", "", line).split(",")]
     assert sn == [n for n, _ in _lib.Seg._fields_]
+
+
+def _valid_desc():
+    """A descriptor that passes every check d2f_create makes before touching a device: one
+    scene of one node and one triangle, every required pointer set (to a dummy address: the
+    checks never dereference them)."""
+    d = _lib.SceneDesc()
+    d.abi_version = _lib.D2F_ABI_VERSION
+    d.precision = _lib.D2F_FP64
+    d.n_scenes, d.N, d.T = 1, 1, 1
+    for name in ("segs", "x", "v", "xn", "xhat", "grad", "grad_prev", "p", "diagH", "mass", "free_mask",
+                 "inc_ptr", "inc", "inc8", "node_bslot", "node_bc", "node_aff", "node_rig", "tri", "Bm", "area",
+                 "mu", "lam", "iters", "active", "status", "escr", "ecache", "work"):
+        setattr(d, name, 64)
+    d.dt, d.iter_max = 1e-3, 1
+    return d
+
+
+@pytest.mark.parametrize("field,value,needle", [
+    ("blocks_per_scene", 5, b"blocks_per_scene"),
+    ("blocks_per_scene", 16, b"mixed precision only"),
+    ("n_sp", 1, b"spring"),
+    ("n_pe", 4, b"pressure"),
+    ("threads", 96, b"threads"),
+    ("line_search", 1, b"xu"),
+])
+def test_create_checks_the_new_fields_without_a_gpu(field, value, needle):
+    """The checks of blocks_per_scene, the spring and pressure arrays, the launch width and
+    the line search's buffer: D2F_EINVAL with a message naming the problem, before any device
+    call (a descriptor that passes them all fails only for want of a device here)."""
+    L = _lib.load()
+    h = C.c_void_p()
+    d = _valid_desc()
+    rc = L.d2f_create(C.byref(d), C.byref(h))
+    assert rc in (0, -2), L.d2f_last_error()          # created on a GPU machine; D2F_ECUDA without one
+    if rc == 0:
+        L.d2f_destroy(h)
+    setattr(d, field, value)
+    assert L.d2f_create(C.byref(d), C.byref(h)) == -1
+    assert needle in L.d2f_last_error(), L.d2f_last_error()
