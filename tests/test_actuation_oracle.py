@@ -230,3 +230,28 @@ def test_active_material_free_growth_oracle():
     assert np.allclose(np.linalg.svd(F)[1], [1.10, 0.85], atol=2e-4)
     f = np.array([np.cos(th), np.sin(th)])
     assert abs(np.linalg.norm(F @ f) - 0.85) < 2e-4
+
+
+def test_chambers_of_random_masks_are_closed_and_oriented():
+    """Random masks with cavities, corner-touching voids and channels to the outside: every
+    sealed cavity becomes a chamber whose walls form closed loops (each node entered as often
+    as left) enclosing exactly its pixels, the outline encloses solid plus cavities, and the
+    void regions that reach the border are no chambers."""
+    rng = np.random.default_rng(11)
+    for trial in range(12):
+        mk = (rng.random((18, 26)) > 0.22).astype(np.uint8)
+        mk[0], mk[-1], mk[:, 0], mk[:, -1] = 1, 1, 1, 1
+        if trial % 3 == 0:
+            mk[9, :6] = 0                                     # a channel to the outside
+        m, h, _ = _model(mk, (0.026, 0.018), center=(0.0, 0.05))
+        lab, sealed = act.enclosed_voids(mk)
+        chambers = m.add_pressure_chambers(h)                 # raises if a loop is open or mis-oriented
+        assert len(chambers) == len(sealed)
+        pw, ph = m.pixel_size(h)
+        for c in chambers:
+            ea, eb = m._chambers[c]["ea"], m._chambers[c]["eb"]
+            assert np.array_equal(np.sort(ea), np.sort(eb))     # closed: in-degree = out-degree
+        total = sum(m._chambers[c]["area0"] for c in chambers)
+        assert abs(total - sum((lab == k).sum() for k in sealed) * pw * ph) < 1e-15
+        amb = m.add_ambient_pressure(h)
+        assert abs(m.chamber_area(amb) - (mk.sum() + sum((lab == k).sum() for k in sealed)) * pw * ph) < 1e-12
