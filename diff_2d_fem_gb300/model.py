@@ -205,6 +205,38 @@ class Model:
         ny = self._bodies[h]["mask"].shape[0]
         return np.asarray(field, np.float64)[q % ny, q // ny]
 
+    def add_affine_region(self, handle, region, E=None, nu=None):
+        """Make part of a soft body rigid (sim_model.py:432-453): the solid pixels of the
+        (H, W) boolean map `region`, laid out like the mask, become one affine piece that
+        shares its interface nodes with the soft material around it. E, nu: the stiffness
+        the piece resists strain with (default model.rigid_young / rigid_nu). Call after
+        finalize() and before the first step; two pieces need at least one soft element
+        between them. Returns the piece's index (as affine_state takes it)."""
+        self._need_mesh()
+        if self._solver is not None:
+            raise RuntimeError("add rigid regions before the first simulate()")
+        elems = self._region_elements(handle, region)
+        mu, lam = _mesh.lame(self.rigid_young if E is None else float(E),
+                             self.rigid_nu if nu is None else float(nu))
+        self.me.mu[elems] = mu
+        self.me.lam[elems] = lam
+        return self._add_affine(handle, elems)
+
+    def _region_elements(self, handle, region):
+        """Global element ids of the solid pixels of an (H, W) map laid out like the body's
+        mask (sim_model.py:1103-1115)."""
+        b = self._bodies[handle]
+        region = np.asarray(region) > 0
+        if region.shape != b["mask"].shape:
+            raise ValueError(f"region is {region.shape}, the mask is {b['mask'].shape}")
+        H = b["mask"].shape[0]
+        tris = self._tri_range[handle]
+        q = np.asarray(self.me.tri_quad)[tris]
+        elems = tris[region[q % H, q // H]]
+        if len(elems) == 0:
+            raise ValueError("the region contains no solid pixel of this body")
+        return elems
+
     def _add_affine(self, handle, elems):
         me = self.me
         mine = self._affine_of.setdefault(handle, [])
@@ -697,16 +729,7 @@ class Model:
         deforming material; fiber None for isotropic change, else an angle [rad] or a
         2-vector along which `stretch` acts. Returns a handle."""
         self._need_mesh()
-        b = self._bodies[handle]
-        region = np.asarray(region) > 0
-        if region.shape != b["mask"].shape:
-            raise ValueError(f"region is {region.shape}, the mask is {b['mask'].shape}")
-        H = b["mask"].shape[0]
-        tris = self._tri_range[handle]
-        q = np.asarray(self.me.tri_quad)[tris]
-        elems = tris[region[q % H, q // H]]
-        if len(elems) == 0:
-            raise ValueError("the region contains no solid pixel of this body")
+        elems = self._region_elements(handle, region)
         mine = self._regions_of.setdefault(handle, [])
         if mine and np.intersect1d(elems, np.concatenate(mine)).size:
             raise ValueError("active regions must not overlap")

@@ -109,5 +109,24 @@ def line_search(ns):
                 dt=2e-3, steps=4, command=None)
 
 
+def rigid_region(ns):
+    """A cantilever whose outer third is a rigid region (an affine piece sharing its interface
+    nodes with the soft root), clamped at its left end and bent by a tip load."""
+    m = ns.Model(device=ns.device); m.damping = 300.0
+    h = m.add_soft_body(np.ones((3, 15), np.uint8), physical_size=(0.0075, 0.0015), center=(0.0, 0.0),
+                        E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    region = np.zeros((3, 15), bool); region[:, 10:] = True
+    m.add_affine_region(h, region)
+    X = m.rest_x(h)
+    m.set_kinematic_constraint(h, np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0])
+    tip = np.where(X[:, 0] > X[:, 0].max() - 1e-9)[0]
+    f = np.zeros_like(X); f[tip, 1] = -1.5 / len(tip)
+    m.set_external_force(h, f)
+    return dict(model=m, integ=ns.ImplicitIntegrator(self_collision=False, friction=False, max_iter=300),
+                dt=2e-3, steps=4, command=None)
+
+
 SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
-          "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1}
+          "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1,
+          "rigid_region": rigid_region}

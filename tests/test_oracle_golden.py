@@ -15,7 +15,8 @@ NAMES = fixtures()
 
 
 def test_fixtures_present():
-    assert {"strip_small", "batch_colliders", "grip", "tendon", "line_search", "strip_cfg1"} <= set(NAMES)
+    assert {"strip_small", "batch_colliders", "grip", "tendon", "line_search", "strip_cfg1",
+            "rigid_region"} <= set(NAMES)
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -45,3 +46,8 @@ def test_fixtures_exercise_contact():
     prob, steps, _ = load_fixture("strip_cfg1")
     y = steps[-1]["x"][:, 1]
     assert y.min() < float(prob["dhat"]), "the strip should have landed within the barrier's reach"
+    prob, steps, _ = load_fixture("rigid_region")
+    q = steps[-1]["q"][0]
+    A = np.array([[q[1], q[2]], [q[4], q[5]]])
+    assert abs(np.arctan2(A[1, 0] - A[0, 1], A[0, 0] + A[1, 1])) > 0.03, "the rigid piece should turn"
+    assert np.abs(A.T @ A - np.eye(2)).max() < 1e-5, "and stay rigid"
