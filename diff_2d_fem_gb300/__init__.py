@@ -14,8 +14,8 @@ include/d2f.h); PyTorch holds the device buffers.
 """
 from .model import Model, SimConfig, DISC, ELLIPSE, BOX, TRIANGLE, HALFSPACE
 from .integrator import ImplicitIntegrator
-from .mesh import Mesh, build_scene, lame
+from .mesh import Mesh, build_scene, check_mesh, lame, mask_to_mesh
 
 __version__ = "0.1.0"
-__all__ = ["Model", "SimConfig", "ImplicitIntegrator", "Mesh", "build_scene", "lame",
+__all__ = ["Model", "SimConfig", "ImplicitIntegrator", "Mesh", "build_scene", "check_mesh", "lame", "mask_to_mesh",
            "DISC", "ELLIPSE", "BOX", "TRIANGLE", "HALFSPACE"]

@@ -176,6 +176,13 @@ class ImplicitIntegrator:
                     f"step. IPC contact needs the bodies to start apart: leave a gap between "
                     f"them (anything from model.dhat = {model.dhat:.3g} m up is out of the "
                     f"barrier's reach).")
+            if any(b.get("mesh") for b in model._bodies) and gap.min() < model.dhat:
+                warnings.warn(
+                    f"two boundaries are {gap.min():.3g} m apart at rest in environment "
+                    f"{int(gap.argmin())}, inside the barrier's reach (model.dhat = "
+                    f"{model.dhat:.3g} m): they push each other apart from the first step. A slit "
+                    f"in a mesh narrower than dhat does this; widen it or lower model.dhat.",
+                    stacklevel=4)
         if model._gravity != (0.0, 0.0) or model._fext is not None:
             loose = [h for h in range(model.n_bodies)
                      if h not in model._constrained or len(model._constrained[h]) == 0]

@@ -72,6 +72,7 @@ class Model:
         self._affine = []
         self._affine_of = {}
         self._extra_excl = []
+        self._mesh_info = {}
         self.body_contact = "ipc"
         self.body_friction = 0.0
         self.body_kappa = None
@@ -170,13 +171,96 @@ class Model:
         self._bodies[h]["kinematic"] = True
         return h
 
+    # ---- bodies given as triangle meshes (sim_model.py:280-338)
+    def add_soft_mesh(self, vertices, triangles, E=None, nu=None, density=None, env_id=0, mu=None):
+        """A soft body given as a triangle mesh: vertices (n, 2) at rest [m], triangles (m, 3)
+        0-based, either winding. Vertex i is node i of the body and triangle j its element j,
+        so node- and element-addressed calls use the mesh's own numbering; per-pixel inputs
+        become per-triangle arrays (E of shape (m,), regions as (m,) booleans or triangle
+        indices) and a hole in the mesh is a pressure chamber. The mesh is validated first
+        (mesh.check_mesh). Returns a handle."""
+        if self.me is not None:
+            raise RuntimeError("add bodies before finalize()")
+        info = self._check_mesh(vertices, triangles)
+        m = len(info["triangles"])
+        if E is not None and not np.isscalar(E):
+            E = np.asarray(E, np.float64)
+            if E.shape != (m,):
+                raise ValueError(f"stiffness per triangle is {E.shape}; the mesh has {m} triangles")
+            if not (np.isfinite(E).all() and (E > 0).all()):
+                raise ValueError("stiffness must be positive and finite on every triangle")
+        if int(env_id) < 0:
+            raise ValueError("env_id must be >= 0")
+        if mu is not None:
+            mu = float(mu)
+            if not (np.isfinite(mu) and mu >= 0.0):
+                raise ValueError(f"mu must be a finite number >= 0, not {mu}")
+        c = self.cfg
+        V = info["vertices"]
+        self._bodies.append(dict(mesh=True, vertices=V, triangles=info["triangles"], h=info["h"],
+                                 h_cfl=info["h_cfl"], L_max=info["L_max"],
+                                 center=tuple(float(v) for v in 0.5 * (V.min(0) + V.max(0))),
+                                 E=(c.young if E is None else (float(E) if np.isscalar(E) else E)),
+                                 nu=float(c.nu if nu is None else nu),
+                                 rho=float(c.rho_mass if density is None else density),
+                                 env=int(env_id), mu=mu))
+        return len(self._bodies) - 1
+
+    def add_affine_mesh(self, vertices, triangles, density=None, env_id=0, E=None, nu=None, mu=None):
+        """A rigid (affine) body given as a triangle mesh. Returns a handle."""
+        h = self.add_soft_mesh(vertices, triangles, E=(self.rigid_young if E is None else E),
+                               nu=(self.rigid_nu if nu is None else nu), density=density,
+                               env_id=env_id, mu=mu)
+        if not np.isscalar(self._bodies[h]["E"]):
+            raise ValueError("a rigid body takes a scalar stiffness")
+        self._bodies[h]["affine"] = True
+        return h
+
+    def add_kinematic_mesh(self, vertices, triangles, env_id=0, mu=None):
+        """A body of prescribed motion given as a triangle mesh. Returns a handle."""
+        h = self.add_soft_mesh(vertices, triangles, env_id=env_id, mu=mu)
+        self._bodies[h]["kinematic"] = True
+        return h
+
+    def _check_mesh(self, vertices, triangles):
+        """check_mesh once per distinct mesh (a batch repeats the same one), warning when the
+        element sizes spread over more than a decade."""
+        import hashlib
+        V = np.ascontiguousarray(vertices, np.float64)
+        T = np.ascontiguousarray(triangles)
+        key = (V.shape, T.shape, str(T.dtype), hashlib.sha1(V.tobytes() + T.tobytes()).hexdigest())
+        cache = self._mesh_info
+        if key not in cache:
+            info = _mesh.check_mesh(V, T)
+            size = np.sqrt(2.0 * info["area"])
+            if size.max() > 10.0 * size.min():
+                warnings.warn(f"this mesh's elements range from {size.min() * 1e3:.3g} to "
+                              f"{size.max() * 1e3:.3g} mm; the iterations a step needs follow the "
+                              f"smallest element, so a few small ones make every step dearer.",
+                              stacklevel=4)
+            cache[key] = info
+        return cache[key]
+
+    def _is_mesh(self, handle):
+        return bool(self._bodies[handle].get("mesh"))
+
+    def _need_pixels(self, handle, what):
+        if self._is_mesh(handle):
+            raise ValueError(f"body {handle} is a mesh body: {what} needs a pixel body. A mesh body "
+                             f"takes per-triangle arrays instead.")
+
     # ---- build (sim_model.py:391-429)
     def finalize(self):
         if not self._bodies:
             raise ValueError("add at least one soft body before finalize()")
         B = self._bodies
-        self.me = _mesh.build_scene([dict(mask_xy=b["mask"].T.copy(), size=b["size"], center=b["center"],
-                                          young=(b["E"] if np.isscalar(b["E"]) else 1.0), nu=b["nu"],
+        # a mesh body's boundary pairs closer than this through the material are excluded
+        # from its self-contact (sim_model.py:396-399)
+        dx = self.dx
+        r_excl = max(2.0 * dx, 16.0 * (self.cfg.ipc_d_hat if self.cfg.ipc_d_hat is not None else dx / 8.0))
+        geom = lambda b: (dict(vertices=b["vertices"], triangles=b["triangles"], excl_radius=r_excl, checked=True)
+                          if b.get("mesh") else dict(mask_xy=b["mask"].T.copy(), size=b["size"], center=b["center"]))
+        self.me = _mesh.build_scene([dict(**geom(b), young=(b["E"] if np.isscalar(b["E"]) else 1.0), nu=b["nu"],
                                           rho=b["rho"], env=b["env"]) for b in B])
         me = self.me
         self._node_range = [np.arange(*me.body_node_range[h]) for h in range(len(B))]
@@ -185,7 +269,7 @@ class Model:
             if np.isscalar(b["E"]):
                 continue
             tris = self._tri_range[h]
-            scale = self._pixel_field(h, b["E"])
+            scale = b["E"] if b.get("mesh") else self._pixel_field(h, b["E"])
             me.mu[tris] = me.mu[tris] * scale
             me.lam[tris] = me.lam[tris] * scale
         self._check_layout()
@@ -223,9 +307,29 @@ class Model:
         return self._add_affine(handle, elems)
 
     def _region_elements(self, handle, region):
-        """Global element ids of the solid pixels of an (H, W) map laid out like the body's
-        mask (sim_model.py:1103-1115)."""
+        """Global element ids of part of a body (sim_model.py:1103-1132): the solid pixels of
+        an (H, W) map laid out like a pixel body's mask; for a mesh body (m,) booleans or
+        distinct triangle indices."""
         b = self._bodies[handle]
+        if b.get("mesh"):
+            tris = self._tri_range[handle]
+            m = len(tris)
+            r = np.asarray(region)
+            if r.dtype == bool:
+                if r.shape != (m,):
+                    raise ValueError(f"region is a boolean array of shape {r.shape}; mesh body {handle} "
+                                     f"has {m} triangles: give ({m},) booleans or triangle indices")
+                loc = np.flatnonzero(r)
+            else:
+                if r.ndim != 1 or not np.issubdtype(r.dtype, np.integer):
+                    raise ValueError(f"region of a mesh body: ({m},) booleans or a 1-D array of triangle "
+                                     f"indices; got {r.dtype} of shape {r.shape}")
+                loc = np.unique(r)
+                if len(loc) != len(r) or (len(loc) and (loc[0] < 0 or loc[-1] >= m)):
+                    raise ValueError(f"triangle indices must be distinct and in 0..{m - 1}")
+            if len(loc) == 0:
+                raise ValueError("the region contains no triangle of this body")
+            return tris[loc]
         region = np.asarray(region) > 0
         if region.shape != b["mask"].shape:
             raise ValueError(f"region is {region.shape}, the mask is {b['mask'].shape}")
@@ -273,7 +377,8 @@ class Model:
         """Contact parameters left unset, from the scene's own scales (sim_model.py:487-497)."""
         c = self.cfg
         soft = [b for b in self._bodies if not b.get("affine") and not b.get("kinematic")]
-        E = min((float(b["E"]) if np.isscalar(b["E"]) else float(b["E"][b["mask"] > 0].min())
+        E = min((float(b["E"]) if np.isscalar(b["E"]) else
+                 float(b["E"].min()) if b.get("mesh") else float(b["E"][b["mask"] > 0].min())
                  for b in soft), default=1.0e6)
         if c.ipc_d_hat is None:
             c.ipc_d_hat = self.dx / 8.0
@@ -289,19 +394,47 @@ class Model:
         envs = {}
         for h, b in enumerate(self._bodies):
             envs.setdefault(b["env"], []).append(h)
+        memo = {}
         for env, hs in envs.items():
             for i, a in enumerate(hs):
                 for c in hs[i + 1:]:
-                    if self._overlap(a, c) or self._overlap(c, a):
+                    if self._is_mesh(a) or self._is_mesh(c):
+                        key = (self._geom_key(a), self._geom_key(c))
+                        if key not in memo:
+                            memo[key] = _mesh.meshes_overlap(*self._body_geometry(a), *self._body_geometry(c))
+                        hit = memo[key]
+                    else:
+                        hit = self._overlap(a, c) or self._overlap(c, a)
+                    if hit:
                         raise ValueError(
                             f"bodies {a} and {c} overlap in environment {env}. Bodies of one "
                             f"environment collide with each other and must start apart; give "
                             f"the members of a batch their own environment with env_id=i.")
+            if any(self._is_mesh(h) for h in hs):
+                sz = [self.element_size(h) for h in hs]
+                if max(sz) > 1.25 * min(sz):
+                    warnings.warn(f"environment {env} mixes element sizes (pixel width, or a mesh body's "
+                                  f"median boundary edge) from {min(sz) * 1e3:.3g} to {max(sz) * 1e3:.3g} "
+                                  f"mm. Contact between bodies has ONE thickness, set by the largest.",
+                                  stacklevel=3)
+                continue
             px = [self.pixel_size(h)[0] for h in hs]
             if max(px) > 1.25 * min(px):
                 warnings.warn(f"environment {env} mixes pixel sizes from {min(px) * 1e3:.3g} to "
                               f"{max(px) * 1e3:.3g} mm. Contact between bodies has ONE thickness, "
                               f"set by the largest. Prefer one pixel size per scene.", stacklevel=3)
+
+    def _geom_key(self, h):
+        b = self._bodies[h]
+        if b.get("mesh"):
+            return ("mesh", id(b["vertices"]), id(b["triangles"]))
+        return ("mask", b["mask"].shape, b["mask"].tobytes(), b["size"], b["center"])
+
+    def _body_geometry(self, h):
+        """A body's rest mesh in its own numbering: (nodes (n, 2), triangles (m, 3))."""
+        nodes = self._node_range[h]
+        s0, s1 = int(nodes[0]), int(nodes[-1]) + 1
+        return np.asarray(self.me.rest_pos[s0:s1], np.float64), np.asarray(self.me.tri)[self._tri_range[h]] - s0
 
     def _overlap(self, a, c):
         A, C = self._bodies[a], self._bodies[c]
@@ -347,19 +480,30 @@ class Model:
         return self._tri_range[handle].copy()
 
     def pixel_size(self, handle):
+        """(width, height) of one pixel of a body [m]; a mesh body has none."""
+        if self._is_mesh(handle):
+            raise ValueError(f"body {handle} is a mesh body: it has no pixels. Its length scale is "
+                             f"element_size({handle}).")
         b = self._bodies[handle]
         H, W = b["mask"].shape
         return b["size"][0] / W, b["size"][1] / H
 
     def element_size(self, handle):
-        return self.pixel_size(handle)[0]
+        """A body's contact length scale [m]: its pixel width, or a mesh body's median
+        boundary-edge length."""
+        b = self._bodies[handle]
+        return float(b["h"]) if b.get("mesh") else self.pixel_size(handle)[0]
 
     def _cfl_length(self, handle):
-        return min(self.pixel_size(handle))
+        """The element size a wave crosses per element: the smaller pixel side, or a mesh
+        body's smallest sqrt(2 x triangle area)."""
+        b = self._bodies[handle]
+        return float(b["h_cfl"]) if b.get("mesh") else min(self.pixel_size(handle))
 
     @property
     def dx(self):
-        """Element size [m]: the largest pixel width over the bodies."""
+        """Element size [m]: the largest over the bodies (it sets the thickness of contact
+        between bodies)."""
         return max(self.element_size(h) for h in range(len(self._bodies)))
 
     def element_areas(self, handle):
@@ -369,13 +513,21 @@ class Model:
         return self.me.rest_pos[self._node_range[handle]].copy()
 
     def to_elements(self, handle, field):
+        """An (H, W) pixel field on each of a body's elements (body_elements order); a mesh
+        body's (m,) field is checked and returned as it is."""
         b = self._bodies[handle]
         field = np.asarray(field, np.float64)
+        if b.get("mesh"):
+            m = len(self._tri_range[handle])
+            if field.shape != (m,):
+                raise ValueError(f"field is {field.shape}; mesh body {handle} has {m} triangles")
+            return field.copy()
         if field.shape != b["mask"].shape:
             raise ValueError(f"field is {field.shape}, the mask is {b['mask'].shape}")
         return self._pixel_field(handle, field)
 
     def to_pixels(self, handle, values):
+        self._need_pixels(handle, "to_pixels")
         H, W = self._bodies[handle]["mask"].shape
         q = np.asarray(self.me.tri_quad)[self._tri_range[handle]]
         out = np.zeros((H, W))
@@ -596,8 +748,15 @@ class Model:
     def add_pressure_chambers(self, handle, min_pixels=1):
         """Make every sealed cavity of a body (a void region enclosed by solid, not reaching the
         edge of the pixel grid) a pressure chamber. Returns their handles, ordered by the
-        cavity's first pixel, bottom row first then left to right."""
+        cavity's first pixel, bottom row first then left to right. On a mesh body every hole
+        of the mesh is a chamber (min_pixels does not apply), ordered by its lowest node,
+        then left to right."""
         self._need_mesh()
+        if self._is_mesh(handle):
+            holes = [lp for lp in self._mesh_loops(handle) if lp[2] > 0]
+            rest = self.me.rest_pos
+            lowest = lambda lp: tuple(rest[lp[0][np.argmin(rest[lp[0], 1])]][::-1])
+            return [self._register_chamber(handle, ea, eb, A, sign=1.0) for ea, eb, A in sorted(holes, key=lowest)]
         mask = self._bodies[handle]["mask"]
         lab, ids = _act.enclosed_voids(mask)
         ids = [k for k in ids if (lab == k).sum() >= min_pixels]
@@ -605,8 +764,15 @@ class Model:
         return [self._add_chamber(handle, lab, k) for k in ids]
 
     def add_pressure_chamber(self, handle, at):
-        """Make the sealed cavity holding the world point `at` a pressure chamber."""
+        """Make the sealed cavity holding the world point `at` a pressure chamber (on a mesh
+        body: the hole of the mesh that holds it)."""
         self._need_mesh()
+        if self._is_mesh(handle):
+            rest = np.asarray(self.me.rest_pos, np.float64)
+            for ea, eb, A in self._mesh_loops(handle):
+                if A > 0 and _act.point_in_loop(at, rest, ea, eb):
+                    return self._register_chamber(handle, ea, eb, A, sign=1.0)
+            raise ValueError(f"point {tuple(at)} is not inside a hole of this mesh body")
         b = self._bodies[handle]
         mask = b["mask"]
         px = _act.pixel_of(at, b["size"], b["center"], mask.shape)
@@ -619,8 +785,14 @@ class Model:
 
     def add_ambient_pressure(self, handle):
         """A pressure on a body's outer surface (its outline, including channels open to the
-        outside); positive squeezes the body. Returns a handle used with set_pressure."""
+        outside); positive squeezes the body. Returns a handle used with set_pressure. On a
+        mesh body: every boundary loop of the mesh that is not a hole."""
         self._need_mesh()
+        if self._is_mesh(handle):
+            out = [lp for lp in self._mesh_loops(handle) if lp[2] < 0]
+            return self._register_chamber(handle, np.concatenate([lp[0] for lp in out]),
+                                          np.concatenate([lp[1] for lp in out]), -sum(lp[2] for lp in out),
+                                          sign=-1.0)
         mask = self._bodies[handle]["mask"]
         lab, ids = _act.enclosed_voids(mask)
         ea, eb = _act.exterior_edges(mask, lab, ids, self._node_of(handle))
@@ -632,6 +804,22 @@ class Model:
         ea, eb = _act.chamber_edges(self._bodies[handle]["mask"], lab, label, self._node_of(handle))
         pw, ph = self.pixel_size(handle)
         return self._register_chamber(handle, ea, eb, int((lab == label).sum()) * pw * ph, sign=1.0)
+
+    def _mesh_loops(self, handle):
+        """A mesh body's boundary loops in global node ids, fluid on the left:
+        [(ea, eb, signed area)], holes > 0, outline < 0 (sim_model.py:881-894). Checked: the
+        outline encloses exactly the material and the holes."""
+        nodes = self._node_range[handle]
+        s0 = int(nodes[0])
+        tri = np.asarray(self.me.tri)[self._tri_range[handle]] - s0
+        rest = np.asarray(self.me.rest_pos, np.float64)[nodes]
+        loops = [(ea + s0, eb + s0, A) for ea, eb, A in _act.mesh_boundary_loops(tri, rest)]
+        outline = -sum(A for _, _, A in loops if A < 0)
+        inside = self.element_areas(handle).sum() + sum(A for _, _, A in loops if A > 0)
+        if abs(outline - inside) > 1e-9 * outline:
+            raise RuntimeError(f"mesh body {handle}: its outline encloses {outline:.9e} m^2, its "
+                               f"material and holes {inside:.9e}")
+        return loops
 
     def _register_chamber(self, handle, ea, eb, expect, sign):
         """sign +1: edges counter-clockwise round a cavity; -1: clockwise round the body. The

@@ -127,6 +127,60 @@ def rigid_region(ns):
                 dt=2e-3, steps=4, command=None)
 
 
+def jittered_grid(nx, ny, size, center, jitter=0.0, seed=0):
+    """A triangle mesh of an (nx, ny)-cell rectangle: interior vertices moved by up to
+    `jitter` cells in each direction, each cell cut along alternating diagonals."""
+    rng = np.random.default_rng(seed)
+    xs = np.linspace(-0.5, 0.5, nx + 1) * size[0] + center[0]
+    ys = np.linspace(-0.5, 0.5, ny + 1) * size[1] + center[1]
+    V = np.stack(np.meshgrid(xs, ys, indexing="ij"), -1).reshape(-1, 2)
+    ix, iy = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), indexing="ij")
+    inner = ((ix > 0) & (ix < nx) & (iy > 0) & (iy < ny)).reshape(-1)
+    V[inner] += jitter * rng.uniform(-1.0, 1.0, (inner.sum(), 2)) * np.array([size[0] / nx, size[1] / ny])
+    T = []
+    for i in range(nx):
+        for j in range(ny):
+            a, b, c, d = i * (ny + 1) + j, (i + 1) * (ny + 1) + j, (i + 1) * (ny + 1) + j + 1, i * (ny + 1) + j + 1
+            T += [[a, b, c], [a, c, d]] if (i + j) % 2 == 0 else [[a, b, d], [b, c, d]]
+    return V, np.asarray(T, np.int64)
+
+
+def mesh_cantilever(ns):
+    """A cantilever given as a jittered triangle mesh, clamped at its left end and sagging
+    under gravity; self-contact on (its exclusion includes pairs close through the material)."""
+    m = ns.Model(device=ns.device)
+    V, T = jittered_grid(12, 3, (0.012, 0.003), (0.0, 0.0), jitter=0.25, seed=1)
+    h = m.add_soft_mesh(V, T, E=0.5e6, nu=0.40, density=1100.0)
+    m.finalize(); m.gravity = (0.0, -9.81)
+    X = m.rest_x(h)
+    m.set_kinematic_constraint(h, np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0])
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=400), dt=2e-3, steps=4, command=None)
+
+
+def mesh_bodies(ns):
+    """Mesh bodies in contact: a jittered soft mesh block (per-triangle stiffness) dropped on a
+    rigid mesh plate lying on the ground, and a kinematic mesh pusher closing in from the
+    side; friction between bodies."""
+    PX = 0.5e-3
+    m = ns.Model(device=ns.device)
+    m.body_friction = 0.5
+    m.add_ground(0.0, mu=0.6)
+    Vp, Tp = jittered_grid(8, 2, (8 * PX, 2 * PX), (0.0, PX + 0.9 * PX / 8))
+    plate = m.add_affine_mesh(Vp, Tp, density=900.0)
+    Vs, Ts = jittered_grid(4, 4, (4 * PX, 4 * PX), (0.0, 2 * PX + 2 * PX + 0.5 * PX / 8 + 0.9 * PX / 8),
+                           jitter=0.2, seed=4)
+    E = np.where(np.arange(len(Ts)) % 3 == 0, 2.0e6, 1.0e6)
+    soft = m.add_soft_mesh(Vs, Ts, E=E, nu=0.40, density=1100.0)
+    Vk, Tk = jittered_grid(2, 3, (2 * PX, 3 * PX), (3.5 * PX, 2 * PX + 2 * PX + 0.9 * PX / 8))
+    pusher = m.add_kinematic_mesh(Vk, Tk)
+    m.finalize(); m.gravity = (0.0, -9.81)
+    X = m.rest_x(pusher)
+
+    def command(k):
+        m.set_kinematic_target(pusher, X - np.array([0.15 * PX * (k + 1), 0.0]))
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=120), dt=1e-3, steps=4, command=command)
+
+
 SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
           "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1,
-          "rigid_region": rigid_region}
+          "rigid_region": rigid_region, "mesh_cantilever": mesh_cantilever, "mesh_bodies": mesh_bodies}
