@@ -12,10 +12,11 @@
 The step is hand-written CUDA for sm_103a (csrc/, bound through the C ABI of
 include/d2f.h); PyTorch holds the device buffers.
 """
-from .model import Model, SimConfig, DISC, ELLIPSE, BOX, TRIANGLE, HALFSPACE
+from .model import Model, SimConfig, Collider, NONE, DISC, ELLIPSE, BOX, TRIANGLE, HALFSPACE
 from .integrator import ImplicitIntegrator
+from .adjoint import AdjointPNCG2D
 from .mesh import Mesh, build_scene, check_mesh, lame, mask_to_mesh
 
 __version__ = "0.1.0"
-__all__ = ["Model", "SimConfig", "ImplicitIntegrator", "Mesh", "build_scene", "check_mesh", "lame", "mask_to_mesh",
-           "DISC", "ELLIPSE", "BOX", "TRIANGLE", "HALFSPACE"]
+__all__ = ["Model", "SimConfig", "Collider", "ImplicitIntegrator", "AdjointPNCG2D", "Mesh", "build_scene", "check_mesh", "lame", "mask_to_mesh",
+           "NONE", "DISC", "ELLIPSE", "BOX", "TRIANGLE", "HALFSPACE"]

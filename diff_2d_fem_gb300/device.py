@@ -415,6 +415,13 @@ class DeviceSolver:
                    "d2f_contact_force")
         return out.cpu().numpy()
 
+    def set_collider_centers(self, centers):
+        """Centres (n_col, 2) of the colliders, in the model's order, read by the next step
+        (and by the contact read-outs)."""
+        c = np.asarray(centers, np.float64).reshape(-1, 2)
+        if len(c):
+            self._t["colliders"][: len(c), 1:3].copy_(torch.as_tensor(c))
+
     def set_pressures(self, p):
         """Gauge pressure of every chamber [Pa], in the model's chamber order."""
         if self.pr is None:

@@ -28,7 +28,7 @@ import numpy as np
 from . import actuators as _act
 from . import mesh as _mesh
 
-DISC, ELLIPSE, BOX, TRIANGLE, HALFSPACE = 0, 1, 2, 3, 4
+NONE, DISC, ELLIPSE, BOX, TRIANGLE, HALFSPACE = -1, 0, 1, 2, 3, 4
 NAMES = {"disc": DISC, "ellipse": ELLIPSE, "box": BOX, "square": BOX, "triangle": TRIANGLE}
 
 
@@ -44,6 +44,24 @@ class SimConfig:
     contact_stiffness: Optional[float] = None
     obstacle_friction: float = 0.5
     obstacle_friction_epsv: float = 1.0e-3
+
+
+@dataclass
+class Collider:
+    """A collider's parameters as the solver reads them: kind (DISC, ELLIPSE, BOX,
+    TRIANGLE, HALFSPACE; NONE for no collider), centre (cx, cy) — a plane's origin — and
+    rx, ry (disc: radius; ellipse / box: half-extents; plane: the unit normal), rref (box,
+    triangle: corner radius; ellipse: level-set scale)."""
+    kind: int = DISC
+    cx: float = 0.0
+    cy: float = 0.0
+    rx: float = 0.0
+    ry: float = 0.0
+    rref: float = 0.0
+
+    @property
+    def c(self):
+        return np.array([self.cx, self.cy])
 
 
 class Model:
@@ -120,6 +138,28 @@ class Model:
         self._colliders.append(dict(kind=int(kind), cx=float(center[0]), cy=float(center[1]),
                                     rx=rx, ry=ry, rref=rref, r=rx, mu=mu))
         return len(self._colliders) - 1
+
+    def set_collider_center(self, index, center):
+        """Move a collider (sim_model.py:176-184). Before the first step this places it;
+        during a rollout it TELEPORTS the shape between steps — the move is not swept, so keep
+        each step's displacement well under the current clearance, and friction treats the
+        collider as stationary."""
+        c = self._colliders[index]
+        c["cx"], c["cy"] = float(center[0]), float(center[1])
+        if self._solver is not None:
+            self._solver.set_collider_centers([[k["cx"], k["cy"]] for k in self._colliders])
+
+    @property
+    def colliders(self):
+        """Every collider as a host-side Collider record (kind, cx, cy, rx, ry, rref)."""
+        return [Collider(kind=c["kind"], cx=c["cx"], cy=c["cy"], rx=c["rx"], ry=c["ry"], rref=c["rref"])
+                for c in self._colliders]
+
+    @property
+    def object(self):
+        """The first collider (kind NONE when the scene has none)."""
+        cs = self.colliders
+        return cs[0] if cs else Collider(kind=NONE)
 
     def set_collider_mu(self, index, mu_per_env):
         """Per-environment Coulomb coefficient of collider `index` ((n_envs,) array). New

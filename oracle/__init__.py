@@ -129,7 +129,7 @@ class OracleSolver:
         B = int(prob["B"])
         Nb = int(np.asarray(prob["bnd"]).shape[0])
         bc_idx = _i32(prob.get("bc_idx", np.zeros(0)))
-        cols = _f64(prob.get("colliders", np.zeros((0, 8))), (-1, 8))
+        cols = _f64(prob.get("colliders", np.zeros((0, 8))), (-1, 8)).copy()   # own copy: movable
         s.N, s.T, s.B, s.Nb, s.n_bc, s.n_col = N, T, B, Nb, len(bc_idx), cols.shape[0]
         self.N, self.B = N, B
         st = self.state = {}
@@ -162,7 +162,7 @@ class OracleSolver:
         s.bc_target = state("bc_target", (len(bc_idx), 2))
         if len(bc_idx):
             st["bc_target"][:] = np.asarray(prob["x"], np.float64)[bc_idx]
-        s.colliders, _ = P(cols)
+        s.colliders, self._cols = P(cols)
         for nm in ("gPg", "g_p", "g_Py", "y_p", "y_Py", "beta", "gTp", "pHp", "alpha", "p_inf",
                    "clr_min", "dE", "dE0", "Ener", "Els_prev", "gn0"):
             setattr(s, nm, state(nm, (B,)))
@@ -297,6 +297,11 @@ class OracleSolver:
             self.state["sp_anchor"][:] = np.asarray(anchor, np.float64).reshape(-1, 2)
         if L0 is not None:
             self.state["sp_L0"][:] = np.asarray(L0, np.float64)
+
+    def set_collider_centers(self, centers):
+        """Move the colliders ((n_col, 2) centres) before the next step."""
+        c = np.asarray(centers, np.float64).reshape(-1, 2)
+        self._cols[: len(c), 1:3] = c
 
     def set_fext(self, f):
         self.state["fext"][:] = np.asarray(f, np.float64).reshape(-1, 2)

@@ -235,3 +235,35 @@ def test_momentum_goes_through_an_impact():
     (within 2e-3)."""
     _, _, dp = _throw("soft", 0.5)
     assert dp < 2e-3, dp
+
+
+def test_a_moved_collider_carries_the_body():
+    """Model.set_collider_center between steps, through the public API: a soft block resting
+    on a disc that is then raised by 0.05 dhat a step. The device step follows the moved disc
+    as the oracle does (FP64; 1e-7 of the coordinates: friction makes this contact run
+    sensitive at 1e-10, while a move that was not applied would differ by 2e-2), and the block
+    has risen with the disc."""
+    import oracle
+    from diff_2d_fem_gb300 import Model, ImplicitIntegrator, scene
+    m = Model()
+    m.add_disc(center=(0.0, 0.0), radius=0.004, mu=0.5)
+    h = m.add_soft_body(np.ones((6, 6), np.uint8), physical_size=(0.003, 0.003),
+                        center=(0.0, 0.004 + 0.0015 + 0.9 * 0.0005 / 8), E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    m.gravity = (0.0, -G0)
+    integ = ImplicitIntegrator(precision="fp64")
+    s = oracle.OracleSolver(scene.solver_problem(m, integ, 1e-3))
+    dy = 0.05 * m.dhat
+    nodes = m.body_nodes(h)
+    y60 = None
+    for k in range(100):
+        if k == 60:
+            y60 = s.x[nodes, 1].mean()
+        if k >= 60:
+            m.set_collider_center(0, (0.0, (k - 59) * dy))
+            s.set_collider_centers([[0.0, (k - 59) * dy]])
+        integ.simulate(m, 1e-3)
+        s.step()
+    x = m.get_x()
+    assert np.abs(x - s.x).max() < 1e-7 * np.abs(s.x).max(), np.abs(x - s.x).max()
+    assert x[nodes, 1].mean() - y60 > 20 * dy

@@ -209,3 +209,38 @@ def test_momentum_goes_through_an_impact_oracle():
     gap, _, dp = _throw("soft", 0.5, steps=80)
     assert gap < 1.0, "the blocks never came within the barrier's reach"
     assert dp < 2e-3, dp
+
+
+def _lift_scene():
+    """A soft block resting on a disc, under gravity."""
+    m = Model()
+    m.add_disc(center=(0.0, 0.0), radius=0.004, mu=0.5)
+    h = m.add_soft_body(np.ones((6, 6), np.uint8), physical_size=(0.003, 0.003),
+                        center=(0.0, 0.004 + 0.0015 + 0.9 * 0.0005 / 8), E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    m.gravity = (0.0, -G0)
+    return m, h
+
+
+def test_a_moved_collider_carries_the_body_oracle():
+    """set_collider_center between steps: the Model's colliders follow, and a disc raised by
+    0.05 dhat a step under a block resting on it carries the block up by as much (within
+    0.1 %) against the same run with the disc left in place (the oracle moves the same disc)."""
+    m, h = _lift_scene()
+    assert m.object.kind == 0 and np.allclose(m.object.c, (0.0, 0.0))
+    integ = ImplicitIntegrator(precision="fp64")
+    prob = _problem(m, integ, 1e-3)
+    s, still = oracle.OracleSolver(prob), oracle.OracleSolver(prob)
+    nodes = m.body_nodes(h)
+    for _ in range(60):
+        s.step()
+        still.step()
+    dy = 0.05 * m.dhat
+    for k in range(1, 41):
+        m.set_collider_center(0, (0.0, k * dy))
+        s.set_collider_centers([[c.cx, c.cy] for c in m.colliders])
+        s.step()
+        still.step()
+    assert np.allclose(m.colliders[0].c, (0.0, 40 * dy))
+    rise = s.x[nodes, 1].mean() - still.x[nodes, 1].mean()
+    assert abs(rise / (40 * dy) - 1.0) < 1e-3, rise / (40 * dy)
