@@ -275,7 +275,7 @@ class OracleSolver:
             self.state["t_L0"][:] = np.asarray(L0, np.float64)
 
     def term(self, which, x, p=None, xn=None):
-        """One actuation term alone (which: "springs" or "pressure") at positions x:
+        """One term alone (which: "springs", "pressure" or "ipc") at positions x:
         (gradient (N, 2), diagonal (N, 2), curvature along p per environment, energy per
         environment) — for derivative checks."""
         st = self.state
@@ -284,7 +284,7 @@ class OracleSolver:
             st["xn"][:] = np.asarray(xn, np.float64)
         st["p"][:] = 0.0 if p is None else np.asarray(p, np.float64)
         E = np.zeros(int(self.s.B))
-        lib().d2o_term(C.byref(self.s), {"springs": 0, "pressure": 1}[which], E.ctypes.data_as(_PD))
+        lib().d2o_term(C.byref(self.s), {"springs": 0, "pressure": 1, "ipc": 2}[which], E.ctypes.data_as(_PD))
         return st["grad"].copy(), st["diagH"].copy(), st["pHp"].copy(), E
 
     def set_pressure(self, p):

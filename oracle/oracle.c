@@ -1320,15 +1320,30 @@ void d2o_ipc_energy(d2o_solver *s, double *buf) {
     ipc_pair(&L);
 }
 
-/* One actuation term alone at s->x (which: 0 Springs, 1 Pressure): its gradient and diagonal
-   into s->grad / s->diagH and its curvature along s->p into s->pHp (all zeroed first), its
-   energy per environment into E — the derivative checks of tests/test_actuation.py. */
+/* One term alone at s->x (which: 0 Springs, 1 Pressure, 2 IPC contact between bodies): its
+   gradient and diagonal into s->grad / s->diagH and its curvature along s->p into s->pHp (all
+   zeroed first), its energy per environment into E — the derivative checks of
+   tests/test_actuation.py and tests/test_ipc.py. For IPC the friction slip is measured from
+   s->xn, and the step caps its curvature pass also computes go to scratch. */
 void d2o_term(d2o_solver *s, int which, double *E) {
     memset(s->grad, 0, sizeof(double) * 2 * s->N);
     memset(s->diagH, 0, sizeof(double) * 2 * s->N);
     for (int e = 0; e < s->B; ++e) { s->pHp[e] = 0.0; E[e] = 0.0; }
     if (which == 0) { spring_grad(s); spring_pHp(s); spring_energy(s, E); }
-    else { pressure_grad(s); pressure_pHp(s); pressure_energy(s, E); }
+    else if (which == 1) { pressure_grad(s); pressure_pHp(s); pressure_energy(s, E); }
+    else if (s->has_ipc) {
+        double *a = (double *)malloc(sizeof(double) * (size_t)s->B);
+        double *c = (double *)malloc(sizeof(double) * (size_t)s->B);
+        for (int e = 0; e < s->B; ++e) { a[e] = 3.0; c[e] = 1.0e30; }
+        ipc_launch L0 = ipc_base(s, 0, s->p, E, c, a);
+        ipc_pair(&L0);
+        ipc_launch L1 = ipc_base(s, 1, s->p, E, c, a);
+        ipc_pair(&L1);
+        ipc_launch L2 = ipc_base(s, 2, s->p, E, c, a);
+        ipc_pair(&L2);
+        free(a);
+        free(c);
+    }
 }
 
 /* ------------------------------------------------------------------ the loop, solver.py:252-425 */
