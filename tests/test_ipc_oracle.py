@@ -1,6 +1,7 @@
 """The oracle's IPC contact between bodies and its rigid-body mechanics on the CPU, after the
 reference's tests/test_ipc.py (the potential itself: flat sliding costs nothing; gradient
-and curvature are the derivatives of the energy) and tests/test_rigid.py (a spinning free
+and curvature are the derivatives of the energy; a prescribed body is swept, not placed)
+and tests/test_rigid.py (a spinning free
 body follows exact rigid backward Euler; the rigid-mode coarse space makes a free soft body
 converge; a block on a slope slides or creeps at the closed-form speed)."""
 import warnings
@@ -195,3 +196,53 @@ def test_block_on_a_slope(kind, th_deg, mu):
     else:
         expect = G0 * np.sin(th) / (mu * G0 * np.cos(th) / m.epsv + ce)
     assert abs(v / expect - 1.0) < 0.01, (v, expect)
+
+
+def _push(px_per_step, wall, steps=30):
+    """A kinematic pusher driven 1.5 pixels a step into a free block, with or without a held
+    wall beyond it: (model, pusher, block, final x, bc lag, smallest gap / dhat, smallest
+    element area / rest area)."""
+    m = Model()
+    m.body_friction = 0.3
+    m.damping = 20.0
+    pusher = _soft(m, (12, 4), (0.0, 0.0))
+    block = _soft(m, (8, 8), (8 * PX, 0.0))                 # two pixels ahead of the pusher
+    if wall:
+        stop = _soft(m, (12, 4), (17 * PX, 0.0))            # a held body, three pixels behind it
+    m.finalize()
+    m.set_kinematic_constraint(pusher, np.arange(m.body_nodes(pusher).size))
+    if wall:
+        m.set_kinematic_constraint(stop, np.arange(m.body_nodes(stop).size))
+    prob = _problem(m, ImplicitIntegrator(), 1e-3)
+    s = oracle.OracleSolver(prob)
+    bc = np.asarray(prob["bc_idx"])
+    gap = np.inf
+    for k in range(1, steps + 1):
+        m.set_kinematic_target(pusher, m.rigid_motion(pusher, (k * px_per_step * PX, 0.0)))
+        s.set_bc_target(m._targets[bc])
+        s.step()
+        gap = min(gap, float(scene.min_distance(dict(prob, x=s.x)).min()) / m.dhat)
+    x, X = s.x, np.asarray(m.me.rest_pos, np.float64)
+    t = np.asarray(m.me.tri)
+    area = lambda P: ((P[t[:, 1], 0] - P[t[:, 0], 0]) * (P[t[:, 2], 1] - P[t[:, 0], 1])
+                      - (P[t[:, 1], 1] - P[t[:, 0], 1]) * (P[t[:, 2], 0] - P[t[:, 0], 0]))
+    lag = float(np.linalg.norm(m._targets[bc] - x[bc], axis=1).max())
+    assert np.isfinite(x).all() and gap > 0.0, gap
+    return m, pusher, block, x, lag, float((area(x) / area(X)).min())
+
+
+def test_a_prescribed_body_is_swept():
+    """A kinematic body is swept to its target, not placed there: with nothing in its way it
+    arrives (lag below 1e-9 pixel) and the block it pushes stays ahead of it unsquashed;
+    against a held wall the target 45 pixels on cannot be reached, the pusher stops short
+    (lag above 25 pixels) and the block is squeezed between the two, never through."""
+    m, pusher, block, x, lag, squash = _push(1.5, wall=False)
+    front = x[m.body_nodes(pusher), 0].max()
+    assert lag < 1e-9 * PX, lag / PX
+    assert x[m.body_nodes(block), 0].min() > front
+    assert squash > 0.9
+    m, pusher, block, x, lag, squash = _push(1.5, wall=True)
+    xb = x[m.body_nodes(block)]
+    assert lag > 25 * PX, lag / PX
+    assert xb[:, 0].max() < 15 * PX and xb[:, 0].min() > x[m.body_nodes(pusher), 0].max()
+    assert 0.05 < squash < 0.9, squash
