@@ -394,3 +394,56 @@ def test_check_mesh_names_each_defect(case):
     V, T, msg = BAD[case]
     with pytest.raises(ValueError, match=msg):
         D.check_mesh(np.asarray(V, np.float64) * 1e-3, T)
+
+
+@pytest.mark.parametrize("mode", ["elastic", "disc"])
+def test_adjoint_on_a_jittered_mesh(mode):
+    """The adjoint oracle on a body of jittered triangles, its top driven down and sideways
+    for 12 steps, without and with a frictionless disc in contact: dJ/d(density) against
+    central differences of the forward oracle along the gradient and along a random
+    direction (reference tests/test_mesh.py:242-288 bounds these at 2 % and 1 %)."""
+    from oracle import adjoint as OA
+    T_, DT, Emin = 12, 2.0e-4, 1e-3
+    m = Model()
+    m.add_disc(center=(0.05, -1.0 if mode == "elastic" else 0.0335), radius=0.006, mu=0.0)
+    V, Tr = _jittered(6, 10, (0.012, 0.024), origin=(0.044, 0.040), seed=2)
+    h = m.add_soft_mesh(V, Tr, E=E, nu=NU, density=RHO)
+    m.finalize()
+    x0 = m.rest_x(h)
+    top = np.where(x0[:, 1] > x0[:, 1].max() - 1e-9)[0]
+    m.set_kinematic_constraint(h, top)
+    prob = _problem(m, ImplicitIntegrator(max_iter=3000, eps=1e-14, tol_x=1e-8, conv_check=8,
+                                          self_collision=False, friction=False), DT)
+    prob["eps"], prob["iter_max"], prob["tol_x"] = 1e-16, 20000, 0.0
+    bc = np.asarray(prob["bc_idx"])
+    targets = []
+    for t in range(1, T_ + 1):
+        tg = np.asarray(m.me.rest_pos, np.float64).copy()
+        tg[top, 1] -= 0.003 * t / T_
+        tg[top, 0] += 0.002 * t / T_
+        targets.append(tg[bc])
+    rng = np.random.default_rng(0)
+    rho0 = 0.45 + 0.5 * rng.random(len(Tr))
+    low = np.where(x0[:, 1] < np.median(x0[:, 1]))[0]
+    c = np.zeros((m.n_nodes, 2))
+    c[low, 0] = 1.0 / len(low)
+
+    def rollout(rho):
+        p = dict(prob)
+        Em = Emin + rho * (1.0 - Emin)
+        p["mu"], p["lam"] = Em * prob["mu"], Em * prob["lam"]
+        _, xs, _ = oracle.run(p, T_, lambda k: dict(bc_target=targets[k]))
+        return [np.asarray(prob["x"], np.float64)] + xs
+
+    xs = rollout(rho0)
+    if mode == "disc":
+        assert xs[-1][:, 1].min() < 0.0335 + 0.006 + m.dhat, "no contact with the disc"
+    res = OA.rollout_adjoint(prob, xs, {T_: c}, E=Emin + rho0 * (1.0 - Emin))
+    g = res["dE"] * (1.0 - Emin)
+    assert np.isfinite(g).all() and np.linalg.norm(g) > 0
+    J = lambda rho: float((c * rollout(rho)[-1]).sum())
+    for d in (g / np.abs(g).max(), rng.standard_normal(len(Tr))):
+        d = d / np.abs(d).max()
+        fd = (J(rho0 + 0.05 * d) - J(rho0 - 0.05 * d)) / 0.1
+        assert abs(g @ d - fd) < 1e-3 * np.linalg.norm(g) * np.linalg.norm(d), (g @ d, fd)
+        assert abs(g @ d - fd) < 1e-2 * abs(fd), (g @ d, fd)
