@@ -90,6 +90,10 @@ def lib():
         _LIB.d2o_term.restype = None
         _LIB.d2o_sdf.argtypes = [C.c_int] + [C.c_double] * 5 + [_PD, C.c_int, _PD]
         _LIB.d2o_sdf.restype = None
+        _LIB.d2o_affine_hessian.argtypes = [_PD, C.c_double, C.c_double, C.c_double, _PD, _PD, _PD]
+        _LIB.d2o_affine_hessian.restype = None
+        _LIB.d2o_chol6_solve.argtypes = [_PD, _PD, _PD]
+        _LIB.d2o_chol6_solve.restype = None
     return _LIB
 
 
@@ -366,6 +370,29 @@ def sdf(collider_row, pts):
     rx = c[6] if kind == 0 else c[3]
     lib().d2o_sdf(kind, c[1], c[2], rx, c[4], c[5], P.ctypes.data_as(_PD), len(P), d.ctypes.data_as(_PD))
     return d
+
+
+def affine_hessian(A, Mu, La, h2=1.0, Hx=None, Hy=None):
+    """The 6x6 reduced Hessian of an affine region (q = t_x, A11, A12, t_y, A21, A22) at the
+    2x2 map A with the region's summed moduli: the mass blocks Hx, Hy (3x3, default 0) plus
+    h2 times the elastic block, its negative twist curvature removed (the oracle's
+    reduced_hessian)."""
+    A4 = _f64(np.asarray(A, np.float64).reshape(4))
+    Hx = _f64(np.zeros(9) if Hx is None else np.asarray(Hx, np.float64).reshape(9))
+    Hy = _f64(np.zeros(9) if Hy is None else np.asarray(Hy, np.float64).reshape(9))
+    out = np.zeros(36)
+    lib().d2o_affine_hessian(A4.ctypes.data_as(_PD), float(Mu), float(La), float(h2), Hx.ctypes.data_as(_PD),
+                             Hy.ctypes.data_as(_PD), out.ctypes.data_as(_PD))
+    return out.reshape(6, 6)
+
+
+def chol6_solve(H, b):
+    """x with H x = b by the oracle's 6x6 Cholesky (diagonal fallback when H is not SPD)."""
+    H36 = _f64(np.asarray(H, np.float64).reshape(36))
+    bb = _f64(np.asarray(b, np.float64).reshape(6))
+    x = np.zeros(6)
+    lib().d2o_chol6_solve(H36.ctypes.data_as(_PD), bb.ctypes.data_as(_PD), x.ctypes.data_as(_PD))
+    return x
 
 
 def problem_keys():

@@ -729,6 +729,21 @@ static void chol6_solve(const m6 *L, const double b[6], double x[6]) {
         x[i] = s / L->m[i][i];
     }
 }
+/* The 6x6 block algebra alone, for tests/test_rigid.py:62-94's checks: H (36, row-major) =
+   reduced_hessian(A (a11 a12 a21 a22), Mu, La, h2, Hx, Hy (9 each)); x = chol6_solve(chol6(H), b). */
+void d2o_affine_hessian(const double *A4, double Mu, double La, double h2, const double *Hx, const double *Hy,
+                        double *H36) {
+    m6 H = reduced_hessian(M(A4[0], A4[1], A4[2], A4[3]), Mu, La, h2, Hx, Hy);
+    for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) H36[6 * r + c] = H.m[r][c];
+}
+void d2o_chol6_solve(const double *H36, const double *b, double *x) {
+    m6 H;
+    for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) H.m[r][c] = H36[6 * r + c];
+    m6 L = chol6(&H);
+    chol6_solve(&L, b, x);
+}
 static inline double dot6(const double *a, const double *b) {
     double s = a[0] * b[0];
     for (int k = 1; k < 6; ++k) s = s + a[k] * b[k];

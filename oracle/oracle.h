@@ -103,6 +103,9 @@ void d2o_ipc_energy(d2o_solver *s, double *buf);
 /* One actuation term (0 Springs, 1 Pressure) alone at s->x: gradient, diagonal, curvature
    along s->p, energy per environment (test access). */
 void d2o_term(d2o_solver *s, int which, double *E);
+void d2o_affine_hessian(const double *A4, double Mu, double La, double h2, const double *Hx, const double *Hy,
+                        double *H36);
+void d2o_chol6_solve(const double *H36, const double *b, double *x);
 /* A collider's level set at n points (x, y pairs) into d (test access). */
 void d2o_sdf(int kind, double cx, double cy, double rx, double ry, double rref, const double *pts, int n,
              double *d);

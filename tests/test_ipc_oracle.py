@@ -246,3 +246,33 @@ def test_a_prescribed_body_is_swept():
     assert lag > 25 * PX, lag / PX
     assert xb[:, 0].max() < 15 * PX and xb[:, 0].min() > x[m.body_nodes(pusher), 0].max()
     assert 0.05 < squash < 0.9, squash
+
+
+def test_block_algebra():
+    """The oracle's 6x6 affine algebra (reference tests/test_rigid.py:62-94): the Cholesky
+    solve against numpy (1e-10); the reduced elastic Hessian symmetric and positive
+    semi-definite at rotations and at strained, partly compressed states, where turning
+    further costs nothing at a pure rotation (one null direction) and straining does."""
+    rng = np.random.default_rng(0)
+    n = 300
+    M = rng.normal(size=(n, 6, 6))
+    H = M @ M.transpose(0, 2, 1) + 0.1 * np.eye(6)
+    b = rng.normal(size=(n, 6))
+    x = np.stack([oracle.chol6_solve(H[k], b[k]) for k in range(n)])
+    ref = np.linalg.solve(H, b[:, :, None])[:, :, 0]
+    assert np.abs(x - ref).max() / np.abs(ref).max() < 1e-10
+    th = rng.uniform(0, 2 * np.pi, n)
+    c, s = np.cos(th), np.sin(th)
+    R = np.stack([np.stack([c, -s], -1), np.stack([s, c], -1)], 1)
+    S = np.eye(2) + 0.02 * rng.uniform(-1, 1, (n, 2, 2))
+    S = 0.5 * (S + S.transpose(0, 2, 1))
+    assert (np.linalg.det(R @ S) < 1).sum() > n // 4, "the sample should include compressed states"
+    for name, A in (("rotation", R), ("strained", R @ S)):
+        Hq = np.stack([oracle.affine_hessian(A[k], 1.0, 2.5) for k in range(n)])
+        H4 = Hq[:, [1, 2, 4, 5]][:, :, [1, 2, 4, 5]]
+        w = np.linalg.eigvalsh(H4)
+        assert np.abs(H4 - H4.transpose(0, 2, 1)).max() < 1e-9 * w.max(), name
+        assert (w[:, 0] > -1e-9 * w[:, -1]).all(), name
+        if name == "rotation":
+            assert (np.abs(w[:, 0]) < 1e-9 * w[:, -1]).all()
+            assert (w[:, 1] > 0.1 * w[:, -1]).all()
