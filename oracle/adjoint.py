@@ -12,6 +12,10 @@ it directly (scipy), so its solution carries no Krylov tolerance:
   element force        drho_kernel              implicit/adjoint.py:164-178 (nh_dPsidF,
                                                 core/math.py:76-81)
   recursion            transient_adjoint        implicit/adjoint.py:371-399
+  IPC tangent          ipc_pair_kernel terms    implicit/ipc_contact.py:174-296: barrier
+                                                terms frozen at x, frictionless, exact
+                                                Hessian of each distance; not in the
+                                                reference's adjoint, which refuses IPC
   tendon tangent       pHp_tendon_kernel        implicit/actuation.py:229-248 (tension-
                                                 controlled: T / len (I - d d^T) per segment);
                                                 not in the reference's adjoint, which refuses
@@ -125,6 +129,91 @@ def collider_blocks(x, prob):
     return out
 
 
+def _line_ddd(ab, w, Ll, c0, v):
+    """Directional second derivative of the point-line distance |cross(ab, w)| / |ab| along
+    v = (v_p, v_a, v_b) (the curvature of the oracle's pHp mode 1, ipc_contact.py:150-160) —
+    a quadratic form in v."""
+    vp, va, vb = v[0:2], v[2:4], v[4:6]
+    de, dw = vb - va, vp - va
+    cr = lambda u, q: u[0] * q[1] - u[1] * q[0]
+    c1 = cr(de, w) + cr(ab, dw)
+    c2 = 2.0 * cr(de, dw)
+    L1 = float(ab @ de) / Ll
+    Lq = (float(de @ de) - L1 * L1) / Ll
+    s0 = c0 / Ll
+    s1 = (c1 - s0 * L1) / Ll
+    ddd = (c2 - 2.0 * s1 * L1 - s0 * Lq) / Ll
+    return -ddd if c0 < 0.0 else ddd
+
+
+def ipc_terms(x, prob):
+    """The frozen-active-set tangent of the IPC barrier between bodies, frictionless: every
+    barrier term the pair loop evaluates (ipc_contact.py:174-296 — the edge interior with
+    weights (1 - t, t), and each end with its vertex-correction coefficient) as
+    (node ids, coef kappa (b'' g g^T + b' H_d)), g = grad d and H_d its exact Hessian (the
+    interior's by polarisation of the directional second derivative). Not in the
+    reference's adjoint, which refuses IPC contact."""
+    ipc = prob.get("ipc")
+    if ipc is None or len(ipc.get("ea", [])) == 0:
+        return []
+    ea, eb = np.asarray(ipc["ea"], np.int64), np.asarray(ipc["eb"], np.int64)
+    ela, elb = np.asarray(ipc["ela"], np.int64), np.asarray(ipc["elb"], np.int64)
+    e2env = np.asarray(ipc["e2env"], np.int64)
+    ca, cb = np.asarray(ipc["ca"], np.float64), np.asarray(ipc["cb"], np.float64)
+    bstart, bpe = np.asarray(ipc["bstart"], np.int64), np.asarray(ipc["bpe"], np.int64)
+    ptr, idx = np.asarray(ipc["excl_ptr"], np.int64), np.asarray(ipc["excl_idx"], np.int64)
+    bnd, b2e = np.asarray(prob["bnd"], np.int64), np.asarray(prob["b2e"], np.int64)
+    dhat, kappa, reach = float(ipc["dhat"]), float(ipc["kappa"]), float(ipc["reach"])
+    dlo = 1.0e-9 * dhat
+    excl = lambda jb, loc: loc in set(idx[ptr[jb]:ptr[jb + 1]].tolist())
+    eye = np.eye(6)
+    out = []
+
+    def point_term(nodes, coef, wv, d):
+        dd = max(d, dlo)
+        n = wv / dd
+        K = (np.eye(2) - np.outer(n, n)) / dd
+        g = np.concatenate([n, -n])
+        Hd = np.block([[K, -K], [-K, K]])
+        out.append((nodes, coef * kappa * (bpp(dd, dhat) * np.outer(g, g) + bp(dd, dhat) * Hd)))
+
+    for k in range(len(ea)):
+        a, b, e = int(ea[k]), int(eb[k]), int(e2env[k])
+        xa, xb = x[a], x[b]
+        ab = xb - xa
+        L2 = max(float(ab @ ab), 1.0e-30)
+        Ll = np.sqrt(L2)
+        for jb in range(int(bstart[e]), int(bstart[e]) + int(bpe[e])):
+            pn = int(bnd[jb])
+            if b2e[jb] != e or pn == a or pn == b or excl(jb, int(ela[k])) or excl(jb, int(elb[k])):
+                continue
+            w = x[pn] - xa
+            tt = float(w @ ab) / L2
+            dvec = w if tt <= 0.0 else (x[pn] - xb if tt >= 1.0 else w - tt * ab)
+            if not np.linalg.norm(dvec) < reach:
+                continue
+            d = float(np.linalg.norm(dvec))
+            if 0.0 < tt < 1.0 and d < dhat:
+                dd = max(d, dlo)
+                n = dvec / dd
+                g = np.concatenate([n, -(1.0 - tt) * n, -tt * n])
+                c0 = ab[0] * w[1] - ab[1] * w[0]
+                q = [_line_ddd(ab, w, Ll, c0, eye[i]) for i in range(6)]
+                Hd = np.diag(q)
+                for i in range(6):
+                    for j in range(i + 1, 6):
+                        Hd[i, j] = Hd[j, i] = 0.5 * (_line_ddd(ab, w, Ll, c0, eye[i] + eye[j]) - q[i] - q[j])
+                out.append(((pn, a, b), kappa * (bpp(dd, dhat) * np.outer(g, g) + bp(dd, dhat) * Hd)))
+            coef_a = -ca[k] + (1.0 if tt <= 0.0 else 0.0)
+            if coef_a != 0.0 and np.linalg.norm(w) < dhat:
+                point_term((pn, a), coef_a, w, float(np.linalg.norm(w)))
+            wb = x[pn] - xb
+            coef_b = -cb[k] + (1.0 if tt >= 1.0 else 0.0)
+            if coef_b != 0.0 and np.linalg.norm(wb) < dhat:
+                point_term((pn, b), coef_b, wb, float(np.linalg.norm(wb)))
+    return out
+
+
 def tendon_segments(prob):
     """(a, b, tendon) node pairs of every tendon segment (eyelet -> next eyelet)."""
     td = prob.get("tendon")
@@ -170,6 +259,9 @@ def assemble(x, prob, tension=None, mu=None, lam=None):
             for a in range(2):
                 for b in range(2):
                     rows.append(2 * na + a); cols.append(2 * nb + b); vals.append(sg * h2 * k[:, a, b])
+    for nodes, blk in ipc_terms(x, prob):
+        dof = np.array([2 * n + c for n in nodes for c in range(2)])
+        rows.append(np.repeat(dof, len(dof))); cols.append(np.tile(dof, len(dof))); vals.append(h2 * blk.ravel())
     H = sp.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
                       shape=(2 * N, 2 * N)).tocsr()
     return H

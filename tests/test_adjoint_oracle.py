@@ -97,3 +97,102 @@ def test_adjoint_oracle_matches_central_differences():
     for name, eps, L, adj in cases:
         fd = (L(eps) - L(-eps)) / (2 * eps)
         assert abs(fd - adj) <= FD_TOL * abs(adj), (name, fd, adj)
+
+
+def test_ipc_tangent_is_the_derivative_of_the_contact_force():
+    """The adjoint oracle's frozen-set IPC tangent against central differences of the forward
+    oracle's own IPC gradient, at a tilted, roughened contact state (1e-7)."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator, Model, scene
+    px = 0.5e-3
+    m = Model()
+    m.add_soft_body(np.ones((4, 40), np.uint8), physical_size=(40 * px, 4 * px), center=(0.0, -2 * px),
+                    E=1.0e6, nu=0.40, density=1100.0)
+    blk = m.add_soft_body(np.ones((8, 12), np.uint8), physical_size=(12 * px, 8 * px),
+                          center=(0.0, 4 * px + 0.5 * px / 8), E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    prob = scene.solver_problem(m, ImplicitIntegrator(friction=False), 1e-3)
+    s = oracle.OracleSolver(prob)
+    rng = np.random.default_rng(0)
+    x = np.asarray(m.me.rest_pos, np.float64).copy()
+    nodes = m.body_nodes(blk)
+    c = x[nodes].mean(0)
+    th = 0.004
+    R = np.array([[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]])
+    x[nodes] = (x[nodes] - c) @ R.T + c + np.array([0.13 * px, 0.2 * m.dhat])
+    x += 0.02 * m.dhat * rng.standard_normal(x.shape)
+    N = x.shape[0]
+    K = np.zeros((2 * N, 2 * N))
+    terms = OA.ipc_terms(x, prob)
+    assert len(terms) > 20
+    for nd, b in terms:
+        dof = np.array([2 * n + k for n in nd for k in range(2)])
+        K[np.ix_(dof, dof)] += b
+    assert np.abs(K - K.T).max() <= 1e-12 * np.abs(K).max()
+    g0 = s.term("ipc", x, xn=x)[0]
+    v = np.zeros_like(x)
+    act = np.where(np.abs(g0).sum(1) > 0)[0]
+    v[act] = rng.standard_normal((len(act), 2))
+    hh = 1e-7 * m.dhat
+    fd = (s.term("ipc", x + hh * v, xn=x + hh * v)[0] - s.term("ipc", x - hh * v, xn=x - hh * v)[0]) / (2 * hh)
+    an = float(prob["dt"]) ** 2 * (K @ v.ravel()).reshape(-1, 2)
+    assert rel_err(an, fd) < 1e-7
+
+
+def test_adjoint_oracle_through_contact_between_bodies():
+    """A soft block pressed by its kinematic top onto a held slab for 8 steps, IPC contact
+    between the bodies active, friction off: the gradient of L = w . x_T with respect to the
+    per-element moduli, x0 and v0, along random directions, against central differences of
+    the forward oracle (1e-4) — an extension beyond the reference, which refuses IPC."""
+    from diff_2d_fem_gb300 import ImplicitIntegrator, Model, scene
+    px = 0.5e-3
+    m = Model()
+    m.damping = 50.0
+    slab = m.add_soft_body(np.ones((3, 16), np.uint8), physical_size=(16 * px, 3 * px), center=(0.0, -1.5 * px),
+                           E=1.0e6, nu=0.40, density=1100.0)
+    blk = m.add_soft_body(np.ones((6, 6), np.uint8), physical_size=(6 * px, 6 * px),
+                          center=(0.3 * px, 3 * px + 0.6 * px / 8), E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    m.set_kinematic_constraint(slab, np.arange(m.body_nodes(slab).size))
+    Xb = m.rest_x(blk)
+    top = np.where(Xb[:, 1] > Xb[:, 1].max() - 1e-9)[0]
+    m.set_kinematic_constraint(blk, top)
+    prob = scene.solver_problem(m, ImplicitIntegrator(friction=False, max_iter=20000), 1e-3)
+    prob = dict(prob, eps=1e-16, tol_x=0.0)
+    bc = np.asarray(prob["bc_idx"])
+    T = 8
+    targets = []
+    for k in range(1, T + 1):
+        tg = np.asarray(m.me.rest_pos, np.float64).copy()
+        tg[m.body_nodes(blk)[top], 1] -= 0.08 * px * k
+        targets.append(tg[bc])
+    rng = np.random.default_rng(3)
+    E = 0.8 + 0.4 * rng.random(len(prob["mu"]))
+    N = np.asarray(prob["x"]).shape[0]
+    w = rng.standard_normal((N, 2))
+
+    def loss(E_, x0=None, v0=None):
+        p = dict(prob)
+        p["mu"], p["lam"] = E_ * prob["mu"], E_ * prob["lam"]
+        if x0 is not None:
+            p["x"] = x0
+        if v0 is not None:
+            p["v"] = v0
+        _, xs, _ = oracle.run(p, T, lambda k: dict(bc_target=targets[k]))
+        return float((w * xs[-1]).sum()), [np.asarray(p["x"], np.float64)] + xs
+
+    _, xs = loss(E)
+    assert len(OA.ipc_terms(xs[-1], prob)) > 5, "no contact between the bodies"
+    res = OA.rollout_adjoint(prob, xs, {T: w}, E=E)
+    free = np.asarray(prob["free"], np.float64)
+    dE = rng.standard_normal(len(E))
+    dx = rng.standard_normal((N, 2)) * free * 1e-5
+    dv = rng.standard_normal((N, 2)) * free * 1e-2
+    v0 = np.asarray(prob["v"], np.float64)
+    # the block forgets x0 and v0 within the 8 damped steps: their effect on L is ~1e-12 of it,
+    # where central differences are good to ~1e-4 only (the loss's own rounding)
+    for name, eps, tol, L, adj in (
+            ("E", 1e-3, FD_TOL, lambda e: loss(E * (1 + e * dE))[0], float((res["dE"] * E * dE).sum())),
+            ("x0", 1.0, 1e-3, lambda e: loss(E, x0=np.asarray(prob["x"]) + e * dx)[0], float((res["dx0"] * dx).sum())),
+            ("v0", 1.0, 1e-3, lambda e: loss(E, v0=v0 + e * dv)[0], float((res["dv0"] * dv).sum()))):
+        fd = (L(eps) - L(-eps)) / (2 * eps)
+        assert abs(fd - adj) <= tol * abs(adj), (name, fd, adj)
