@@ -12,6 +12,11 @@ it directly (scipy), so its solution carries no Krylov tolerance:
   element force        drho_kernel              implicit/adjoint.py:164-178 (nh_dPsidF,
                                                 core/math.py:76-81)
   recursion            transient_adjoint        implicit/adjoint.py:371-399
+  affine bodies        AffineBodies             implicit/affine.py:60-101, 156-269: the
+                                                system in the reduced coordinates (x = J q
+                                                on a region's nodes) plus each region's
+                                                exact elastic block; not in the reference's
+                                                adjoint, which refuses affine bodies
   IPC tangent          ipc_pair_kernel terms    implicit/ipc_contact.py:174-296: barrier
                                                 terms frozen at x, frictionless, exact
                                                 Hessian of each distance; not in the
@@ -271,13 +276,78 @@ def free_dofs(prob):
     return np.asarray(prob["free"], np.float64).reshape(-1) > 0.5
 
 
-def adjoint_solve(x, prob, rhs, tension=None, mu=None, lam=None):
-    """Solve H(x) lam = rhs on the free DOFs (direct); lam = 0 on the held DOFs."""
-    import scipy.sparse.linalg as spl
+def _nh_dP(A, dA, mu, la):
+    """Directional derivative of the Neo-Hookean P at A along dA (moduli mu, la)."""
+    J = A[0, 0] * A[1, 1] - A[0, 1] * A[1, 0]
+    G = np.linalg.inv(A).T
+    logJ = np.log(max(J, LOG_EPS))
+    return mu * dA + la * float((G * dA).sum()) * G - (la * logJ - mu) * (G @ dA.T @ G)
+
+
+def affine_reduction(x, prob):
+    """The affine bodies' reduced coordinates at the state x (AffineBodies, implicit/
+    affine.py:60-101, 156-269): S (2N x n_u, sparse) maps the unknowns u — every free DOF of a
+    node no rigid region owns, then q = (t_x, A11, A12, t_y, A21, A22) of each region — to
+    node displacements (x = J q on a region's nodes); and each region's exact elastic block
+    d2 Psi / dq2 at its current A with the region's summed moduli (6x6, in q), to be added
+    times h^2. q is recovered from the region's node positions (x = J q holds exactly)."""
+    import scipy.sparse as sp
+    af = prob["affine"]
+    node, grp = np.asarray(af["node"], np.int64), np.asarray(af["grp"], np.int64)
+    w = np.asarray(af["w"], np.float64).reshape(-1, 3)
+    Mu, La = np.asarray(af["Mu"], np.float64), np.asarray(af["La"], np.float64)
+    N = x.shape[0]
+    nreg = len(Mu)
     ff = free_dofs(prob)
-    H = assemble(x, prob, tension, mu, lam)[ff][:, ff]
+    slaved = np.zeros(2 * N, bool)
+    slaved[2 * node], slaved[2 * node + 1] = True, True
+    plain = np.flatnonzero(ff & ~slaved)
+    nu = len(plain) + 6 * nreg
+    rows = [plain]
+    cols = [np.arange(len(plain))]
+    vals = [np.ones(len(plain))]
+    base = len(plain) + 6 * grp
+    for c in range(3):
+        rows += [2 * node, 2 * node + 1]
+        cols += [base + c, base + 3 + c]
+        vals += [w[:, c], w[:, c]]
+    S = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(2 * N, nu))
+    blocks = []
+    idx = (1, 2, 4, 5)
+    for b in range(nreg):
+        k = grp == b
+        sol = np.linalg.lstsq(w[k], x[node[k]], rcond=None)[0]          # (3, 2): q_x, q_y columns
+        A = np.array([[sol[1, 0], sol[2, 0]], [sol[1, 1], sol[2, 1]]])
+        K = np.zeros((6, 6))
+        for j in range(4):
+            dA = np.zeros(4)
+            dA[j] = 1.0
+            dP = _nh_dP(A, dA.reshape(2, 2), Mu[b], La[b]).reshape(4)
+            for r in range(4):
+                K[idx[r], idx[j]] = dP[r]
+        blocks.append((len(plain) + 6 * b, K))
+    return S, blocks
+
+
+def adjoint_solve(x, prob, rhs, tension=None, mu=None, lam=None):
+    """Solve H(x) lam = rhs on the free DOFs (direct); lam = 0 on the held DOFs. With affine
+    bodies the system is solved in the reduced coordinates, S^T H S + h^2 K_A, and mapped
+    back: lam = S u."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    H = assemble(x, prob, tension, mu, lam)
+    b = np.asarray(rhs, np.float64).reshape(-1)
+    if prob.get("affine") is not None and len(prob["affine"].get("Mu", [])):
+        S, blocks = affine_reduction(x, prob)
+        Hr = (S.T @ H @ S).tolil()
+        h2 = float(prob["dt"]) ** 2
+        for o, K in blocks:
+            Hr[o:o + 6, o:o + 6] = Hr[o:o + 6, o:o + 6].toarray() + h2 * K
+        u = spl.spsolve(sp.csc_matrix(Hr), S.T @ b)
+        return (S @ u).reshape(-1, 2)
+    ff = free_dofs(prob)
     out = np.zeros(2 * x.shape[0])
-    out[ff] = spl.spsolve(H.tocsc(), np.asarray(rhs, np.float64).reshape(-1)[ff])
+    out[ff] = spl.spsolve(H[ff][:, ff].tocsc(), b[ff])
     return out.reshape(-1, 2)
 
 

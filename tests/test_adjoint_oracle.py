@@ -196,3 +196,56 @@ def test_adjoint_oracle_through_contact_between_bodies():
             ("v0", 1.0, 1e-3, lambda e: loss(E, v0=v0 + e * dv)[0], float((res["dv0"] * dv).sum()))):
         fd = (L(eps) - L(-eps)) / (2 * eps)
         assert abs(fd - adj) <= tol * abs(adj), (name, fd, adj)
+
+
+def test_adjoint_oracle_with_a_rigid_region():
+    """A cantilever whose outer third is a rigid region (an affine body sharing its interface
+    nodes), tip-loaded, 6 steps: the gradient of L = w . x_T with respect to the soft
+    elements' moduli and to v0, along random directions, against central differences of the
+    forward oracle (1e-4) — the reduced-coordinate adjoint, beyond the reference, which
+    refuses affine bodies."""
+    import warnings
+    from diff_2d_fem_gb300 import ImplicitIntegrator, Model, scene
+    m = Model()
+    m.damping = 300.0
+    h = m.add_soft_body(np.ones((3, 15), np.uint8), physical_size=(0.0075, 0.0015), center=(0.0, 0.0),
+                        E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    region = np.zeros((3, 15), bool)
+    region[:, 10:] = True
+    m.add_affine_region(h, region)
+    X = m.rest_x(h)
+    m.set_kinematic_constraint(h, np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0])
+    tip = np.where(X[:, 0] > X[:, 0].max() - 1e-9)[0]
+    f = np.zeros_like(X)
+    f[tip, 1] = -1.5 / len(tip)
+    m.set_external_force(h, f)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        prob = scene.solver_problem(m, ImplicitIntegrator(self_collision=False, friction=False, max_iter=20000), 2e-3)
+    prob = dict(prob, eps=1e-16, tol_x=0.0)
+    T = 6
+    rng = np.random.default_rng(5)
+    E = np.where(np.asarray(prob["mu"]) > 0, 0.8 + 0.4 * rng.random(len(prob["mu"])), 1.0)
+    N = np.asarray(prob["x"]).shape[0]
+    w = rng.standard_normal((N, 2))
+
+    def loss(E_, v0=None):
+        p = dict(prob)
+        p["mu"], p["lam"] = E_ * prob["mu"], E_ * prob["lam"]
+        if v0 is not None:
+            p["v"] = v0
+        _, xs, _ = oracle.run(p, T)
+        return float((w * xs[-1]).sum()), [np.asarray(p["x"], np.float64)] + xs
+
+    _, xs = loss(E)
+    res = OA.rollout_adjoint(prob, xs, {T: w}, E=E)
+    free = np.asarray(prob["free"], np.float64)
+    dE = rng.standard_normal(len(E)) * (np.asarray(prob["mu"]) > 0)
+    dv = rng.standard_normal((N, 2)) * free * 1e-2
+    v0 = np.asarray(prob["v"], np.float64)
+    for name, eps, L, adj in (
+            ("E", 1e-3, lambda e: loss(E * (1 + e * dE))[0], float((res["dE"] * E * dE).sum())),
+            ("v0", 1.0, lambda e: loss(E, v0=v0 + e * dv)[0], float((res["dv0"] * dv).sum()))):
+        fd = (L(eps) - L(-eps)) / (2 * eps)
+        assert abs(fd - adj) <= FD_TOL * abs(adj), (name, fd, adj)
