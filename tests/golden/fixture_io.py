@@ -4,7 +4,7 @@ from __future__ import annotations
 
 import numpy as np
 
-SUBS = ("ipc", "tendon", "affine", "rigid")
+SUBS = ("ipc", "tendon", "affine", "rigid", "springs", "pressure")
 
 
 def pack(prob: dict, steps: list, meta: dict | None = None) -> dict:

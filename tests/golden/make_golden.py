@@ -55,11 +55,18 @@ def extract_problem(R, model, s):
     assert s.self_stiffness == 0.0, "the 'node' contact is out of scope"
     # terms, in the reference's order
     kinds = [type(t).__name__ for t in s.terms]
-    order = [k for k in ("ExternalForce", "AffineBodies", "IPCContact", "Tendon") if k in kinds]
+    order = [k for k in ("ExternalForce", "AffineBodies", "IPCContact", "Springs", "Pressure", "Tendon")
+             if k in kinds]
     assert kinds == order, f"unexpected term order {kinds}"
     for t in s.terms:
         if isinstance(t, A.ExternalForce):
             prob["fext"] = _np(t.f)
+        elif isinstance(t, A.Springs):
+            prob["springs"] = dict(a=_np(t.na), b=_np(t.nb), k=_np(t.k), L0=_np(t.L0), anchor=_np(t.anchor),
+                                   env=_np(t.s2env))
+        elif isinstance(t, A.Pressure):
+            prob["pressure"] = dict(ea=_np(t.ea), eb=_np(t.eb), ch=_np(t.ech), ch2env=_np(t.ch2env),
+                                    p=_np(t.p), ref=_np(t.cref))
         elif isinstance(t, A.Tendon):
             prob["tendon"] = dict(node=_np(t.node), prv=_np(t.prv), nxt=_np(t.nxt), tid=_np(t.tid),
                                   t2env=_np(t.t2env), stiff=_np(t.stiff), L0=_np(t.L0),

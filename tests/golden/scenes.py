@@ -181,6 +181,28 @@ def mesh_bodies(ns):
     return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=120), dt=1e-3, steps=4, command=command)
 
 
+def actuators(ns):
+    """A soft block with a sealed cavity on the ground: the cavity pressurised and the
+    outline under an ambient pressure, the lower half actively contracting, a corner pinned
+    to the world and another corner on a world spring, under gravity."""
+    PX = 0.5e-3
+    m = ns.Model(device=ns.device)
+    m.add_ground(0.0, mu=0.6)
+    mk = np.ones((8, 8), np.uint8); mk[3:6, 2:6] = 0
+    h = m.add_soft_body(mk, physical_size=(8 * PX, 8 * PX), center=(0.0, 4 * PX + 0.9 * PX / 8),
+                        E=0.5e6, nu=0.40, density=1100.0)
+    m.finalize(); m.gravity = (0.0, -9.81)
+    ch = m.add_pressure_chambers(h)
+    m.set_pressure(ch[0], 3.0e4)
+    m.set_pressure(m.add_ambient_pressure(h), 5.0e3)
+    region = np.zeros((8, 8), bool); region[:4] = True
+    m.set_activation(m.add_active_region(h, region), 0.97)
+    m.add_pin(h, (-4 * PX, 8 * PX + 0.9 * PX / 8), stiffness=1.0e6)
+    m.add_spring(h, (4 * PX, 8 * PX + 0.9 * PX / 8), point_b=(6 * PX, 10 * PX), stiffness=2.0e4, rest_length=PX)
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=200), dt=2e-3, steps=4, command=None)
+
+
 SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
           "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1,
-          "rigid_region": rigid_region, "mesh_cantilever": mesh_cantilever, "mesh_bodies": mesh_bodies}
+          "rigid_region": rigid_region, "mesh_cantilever": mesh_cantilever, "mesh_bodies": mesh_bodies,
+          "actuators": actuators}

@@ -33,7 +33,7 @@ def test_problem_matches_reference(name):
     ref, _, _ = load_fixture(name)
     mine, _ = _build(name)
     for key, val in ref.items():
-        if key in ("ipc", "tendon", "affine", "rigid"):
+        if key in ("ipc", "tendon", "affine", "rigid", "springs", "pressure"):
             assert mine.get(key) is not None, f"{key} missing"
             for kk, vv in val.items():
                 if vv is None:
@@ -43,7 +43,7 @@ def test_problem_matches_reference(name):
             assert float(mine[key]) == float(val), f"{key}: {mine[key]} vs {val}"
         else:
             _same(mine[key], val, key)
-    for key in ("ipc", "tendon", "affine", "rigid", "fext"):
+    for key in ("ipc", "tendon", "affine", "rigid", "fext", "springs", "pressure"):
         assert (key in ref) == (mine.get(key) is not None), f"{key} presence differs"
 
 
