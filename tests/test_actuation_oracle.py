@@ -2,10 +2,11 @@
 spring and pressure terms against finite differences of their own energy, and closed-form
 states solved by the oracle (the reference's tests/test_actuation.py cases 1 and 2).
 
-The reference's CPU path needs warp-lang, absent here, so no golden vectors of these terms
-exist; the oracle is pinned instead by the derivative identities (gradient = d energy,
-curvature = d gradient, diagonal = the true second derivative) and by states with exact
-answers: a hydrostatic pressure compresses any body uniformly, a fully active body takes the
+Besides the golden fixture tests/golden/actuators.npz (recorded from the reference's own
+kernels through the serial Warp stand-in, reproduced bit for bit in test_oracle_golden.py),
+the oracle is pinned here by the derivative identities (gradient = d energy, curvature =
+d gradient, diagonal = the true second derivative) and by states with exact answers: a
+hydrostatic pressure compresses any body uniformly, a fully active body takes the
 prescribed shape stress-free.
 """
 import warnings
