@@ -202,7 +202,29 @@ def actuators(ns):
     return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=200), dt=2e-3, steps=4, command=None)
 
 
+def body_mu(ns):
+    """Friction per body (the harmonic mean of the two bodies' mu at every pair) and a
+    stiffness map: in each of two environments a block slides down a slab held at its base
+    under tilted gravity; the slab's lower rows are four times stiffer."""
+    PX = 0.5e-3
+    m = ns.Model(device=ns.device)
+    Emap = np.full((3, 16), 0.5e6); Emap[0] = 2.0e6
+    for env, mu_b in enumerate((0.2, 0.6)):
+        m.add_soft_body(np.ones((3, 16), np.uint8), physical_size=(16 * PX, 3 * PX), center=(0.0, -1.5 * PX),
+                        E=Emap, nu=0.40, density=1100.0, env_id=env, mu=0.8)
+        m.add_soft_body(np.ones((4, 4), np.uint8), physical_size=(4 * PX, 4 * PX),
+                        center=(-2 * PX, 2 * PX + 0.9 * PX / 8), E=1.0e6, nu=0.40, density=1100.0,
+                        env_id=env, mu=mu_b)
+    m.finalize()
+    for h in (0, 2):
+        X = m.rest_x(h)
+        m.set_kinematic_constraint(h, np.where(X[:, 1] < X[:, 1].min() + 1e-9)[0])
+    th = np.deg2rad(25.0)
+    m.gravity = (9.81 * np.sin(th), -9.81 * np.cos(th))
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=150), dt=1e-3, steps=5, command=None)
+
+
 SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
           "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1,
           "rigid_region": rigid_region, "mesh_cantilever": mesh_cantilever, "mesh_bodies": mesh_bodies,
-          "actuators": actuators}
+          "actuators": actuators, "body_mu": body_mu}
