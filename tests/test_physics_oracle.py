@@ -244,3 +244,78 @@ def test_a_moved_collider_carries_the_body_oracle():
     assert np.allclose(m.colliders[0].c, (0.0, 40 * dy))
     rise = s.x[nodes, 1].mean() - still.x[nodes, 1].mean()
     assert abs(rise / (40 * dy) - 1.0) < 1e-3, rise / (40 * dy)
+
+
+def test_import_surface():
+    """The names a user of the reference imports (its objects, viz and Renderer modules are
+    plotting and windowing, not part of this package)."""
+    import diff_2d_fem_gb300 as D
+    for name in ("Model", "SimConfig", "Mesh", "build_scene", "check_mesh", "mask_to_mesh",
+                 "ImplicitIntegrator", "AdjointPNCG2D"):
+        assert hasattr(D, name), name
+
+
+def _cantilever(m, E_, center, size=(0.020, 0.004), shape=(6, 30), env_id=0, density=1100.0):
+    return m.add_soft_body(np.ones(shape, np.uint8), physical_size=size, center=center, E=E_, nu=0.40,
+                           density=density, env_id=env_id)
+
+
+def _clamp_droop(m, hs, steps=60):
+    for h in hs:
+        X = m.rest_x(h)
+        m.set_kinematic_constraint(h, np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0])
+    m.gravity = (0.0, -G0)
+    m.damping = 100.0
+    _, xs, _ = oracle.run(_problem(m, ImplicitIntegrator(max_iter=120, self_collision=False, friction=False), 1e-3),
+                          steps)
+    return xs[-1]
+
+
+def test_bodies_keep_their_own_geometry_and_material():
+    """A cantilever alone and beside a softer, heavier one on another grid in the same scene:
+    each body's mass is its own density times its area (1e-9), the shared body droops as it
+    does alone (1e-3 of the sag: the two share one environment's step length until both have
+    converged), and the softer, heavier one sags more — after the reference's
+    tests/test_scene.py:40-78."""
+    one = Model()
+    h1 = _cantilever(one, 4.0e6, (0.0, 0.0))
+    one.finalize()
+    xa = _clamp_droop(one, [h1])[one.body_nodes(h1)]
+    two = Model()
+    hs = _cantilever(two, 1.0e6, (0.0, 0.03), size=(0.016, 0.004), shape=(8, 32), density=2000.0)
+    hb = _cantilever(two, 4.0e6, (0.0, 0.0))
+    with pytest.warns(UserWarning, match="mixes pixel sizes"):
+        two.finalize()
+    mass = np.asarray(two.me.mass)
+    assert np.isclose(mass[two.body_nodes(hs)].sum(), 2000.0 * 0.016 * 0.004, rtol=1e-9)
+    assert np.isclose(mass[two.body_nodes(hb)].sum(), 1100.0 * 0.020 * 0.004, rtol=1e-9)
+    x2 = _clamp_droop(two, [hs, hb])
+    sag = np.abs(xa - one.rest_x(h1)).max()
+    assert sag > 1e-5
+    assert np.abs(xa - x2[two.body_nodes(hb)]).max() / sag < 1e-3
+    assert np.abs(x2[two.body_nodes(hs)] - two.rest_x(hs)).max() > 2.0 * sag
+
+
+def test_contact_scales_and_overlap():
+    """Contact parameters left unset are scaled to the scene (reach 1/8 pixel, kappa and the
+    body stiffness from the softest modulus), and two bodies in one place are refused unless
+    they live in different environments — after the reference's tests/test_scene.py:111-151."""
+    m = Model()
+    m.add_ground(height=0.0, mu=0.6)
+    block = np.ones((12, 16), np.uint8)
+    reach = 0.5e-3 / 8
+    m.add_soft_body(block, physical_size=(0.008, 0.006), E=1.0e6, nu=0.40, density=1100.0,
+                    center=(0.0, 0.003 + 0.9 * reach))
+    m.add_soft_body(block, physical_size=(0.008, 0.006), E=1.0e6, nu=0.40, density=1100.0,
+                    center=(0.0, 0.003 + 0.9 * reach + 0.0068))
+    m.finalize()
+    assert np.isclose(m.dhat, reach) and np.isclose(m.kappa, 3.2e4) and np.isclose(m.self_stiffness, 2.0e5)
+    bad = Model()
+    for _ in range(2):
+        bad.add_soft_body(np.ones((8, 8), np.uint8), physical_size=(0.008, 0.008), center=(0.0, 0.0))
+    with pytest.raises(ValueError, match="env_id"):
+        bad.finalize()
+    ok = Model()
+    for i in range(2):
+        ok.add_soft_body(np.ones((8, 8), np.uint8), physical_size=(0.008, 0.008), center=(0.0, 0.0), env_id=i)
+    assert ok.finalize().n_envs == 2
