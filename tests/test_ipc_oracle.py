@@ -276,3 +276,44 @@ def test_block_algebra():
         if name == "rotation":
             assert (np.abs(w[:, 0]) < 1e-9 * w[:, -1]).all()
             assert (w[:, 1] > 0.1 * w[:, -1]).all()
+
+
+def _pinch_and_lift(mu, lift=2.0e-3, n_close=50, n_lift=100, n_hold=25):
+    """Two soft pads driven by their backs close on a rigid block on the ground, lift and
+    hold: the block's rise as a fraction of the lift."""
+    m = Model()
+    m.body_friction = mu
+    m.add_ground(0.0, mu=0.5)
+    blk = m.add_affine_body(np.ones((8, 8), np.uint8), physical_size=(8 * PX, 8 * PX),
+                            center=(0.0, 4 * PX + 0.9 * PX / 8), density=600.0)
+    pads = [_soft(m, (8, 4), (sgn * 7 * PX, 4 * PX + 0.4e-3)) for sgn in (-1, +1)]
+    m.finalize()
+    m.gravity = (0.0, -G0)
+    for sgn, h in zip((-1, +1), pads):
+        X = m.rest_x(h)
+        back = X[:, 0].min() if sgn < 0 else X[:, 0].max()
+        m.set_kinematic_constraint(h, np.where(np.abs(X[:, 0] - back) < 1e-9)[0])
+    prob = _problem(m, ImplicitIntegrator(), 1e-3)
+    bc = np.asarray(prob["bc_idx"])
+    s = oracle.OracleSolver(prob)
+    nb = m.body_nodes(blk)
+    y0 = s.x[nb, 1].mean()
+    for k in range(1, n_close + n_lift + n_hold + 1):
+        a, b = min(k / n_close, 1.0), min(max(k - n_close, 0) / n_lift, 1.0)
+        for sgn, h in zip((-1, +1), pads):
+            X = m.rest_x(h)
+            X[:, 0] -= sgn * 1.125 * PX * a
+            X[:, 1] += lift * b
+            m.set_kinematic_target(h, X)
+        s.set_bc_target(m._targets[bc])
+        s.step()
+    assert np.isfinite(s.x).all() and scene.min_distance(dict(prob, x=s.x)).min() > 0.0
+    return (s.x[nb, 1].mean() - y0) / lift
+
+
+def test_a_grip_needs_friction():
+    """Pads pinching a rigid block lift it only through friction between the bodies: without
+    friction it stays on the ground (below 5 % of the lift), with mu = 0.8 it comes up (above
+    95 %) — after the reference's tests/test_ipc.py:185-212, at half its size."""
+    assert abs(_pinch_and_lift(0.0)) < 0.05
+    assert _pinch_and_lift(0.8) > 0.95
