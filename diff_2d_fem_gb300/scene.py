@@ -388,7 +388,54 @@ def subset_problem(prob, envs):
         kn = np.nonzero(pmap[grp] >= 0)[0]
         kn = kn[np.argsort(pmap[grp[kn]], kind="stable")]
         out["rigid"] = dict(node=nmap[np.asarray(rg["node"], np.int64)[kn]], grp=pmap[grp[kn]], env=newenv[renv[kp]])
-    for key in ("affine", "tendon", "springs", "pressure"):
-        if prob.get(key) is not None:
-            raise NotImplementedError(f"subset_problem: {key} terms are not sliced")
+    def pick(env_of):
+        """Items whose environment is kept, in the new environment order (stable), and the
+        old -> new item map."""
+        env_of = np.asarray(env_of, np.int64)
+        k = np.nonzero(newenv[env_of] >= 0)[0]
+        k = k[np.argsort(newenv[env_of[k]], kind="stable")]
+        m = np.full(len(env_of), -1, np.int64)
+        m[k] = np.arange(len(k))
+        return k, m
+
+    def members(owner, omap):
+        """Entries whose owner is kept, grouped in the owners' new order (stable)."""
+        owner = np.asarray(owner, np.int64)
+        k = np.nonzero(omap[owner] >= 0)[0]
+        return k[np.argsort(omap[owner[k]], kind="stable")]
+
+    remap = lambda ids: np.where(np.asarray(ids, np.int64) >= 0, nmap[np.asarray(ids, np.int64)], -1)
+    if prob.get("affine") is not None:
+        af = prob["affine"]
+        kr, rmap = pick(af["env"])
+        ke = members(af["grp"], rmap)
+        out["affine"] = dict(node=nmap[np.asarray(af["node"], np.int64)[ke]], grp=rmap[np.asarray(af["grp"], np.int64)[ke]],
+                             env=newenv[np.asarray(af["env"], np.int64)[kr]],
+                             w=np.asarray(af["w"], np.float64).reshape(-1, 3)[ke],
+                             Mu=np.asarray(af["Mu"])[kr], La=np.asarray(af["La"])[kr],
+                             q=np.asarray(af["q"], np.float64).reshape(-1, 6)[kr])
+    if prob.get("tendon") is not None:
+        td = prob["tendon"]
+        kt, tmap = pick(td["t2env"])
+        kj = members(td["tid"], tmap)
+        jmap = np.full(len(np.asarray(td["tid"])), -1, np.int64)
+        jmap[kj] = np.arange(len(kj))
+        link = lambda a: np.where(np.asarray(a, np.int64)[kj] >= 0, jmap[np.asarray(a, np.int64)[kj]], -1)
+        out["tendon"] = dict(node=nmap[np.asarray(td["node"], np.int64)[kj]], prv=link(td["prv"]), nxt=link(td["nxt"]),
+                             tid=tmap[np.asarray(td["tid"], np.int64)[kj]], t2env=newenv[np.asarray(td["t2env"], np.int64)[kt]],
+                             stiff=np.asarray(td["stiff"])[kt], L0=np.asarray(td["L0"])[kt], Tcmd=np.asarray(td["Tcmd"])[kt])
+    if prob.get("springs") is not None:
+        sp = prob["springs"]
+        ks, _ = pick(sp["env"])
+        out["springs"] = dict(a=nmap[np.asarray(sp["a"], np.int64)[ks]], b=remap(np.asarray(sp["b"], np.int64)[ks]),
+                              k=np.asarray(sp["k"])[ks], L0=np.asarray(sp["L0"])[ks],
+                              anchor=np.asarray(sp["anchor"], np.float64).reshape(-1, 2)[ks],
+                              env=newenv[np.asarray(sp["env"], np.int64)[ks]])
+    if prob.get("pressure") is not None:
+        pr = prob["pressure"]
+        kc, cmap = pick(pr["ch2env"])
+        kq = members(pr["ch"], cmap)
+        out["pressure"] = dict(ea=nmap[np.asarray(pr["ea"], np.int64)[kq]], eb=nmap[np.asarray(pr["eb"], np.int64)[kq]],
+                               ch=cmap[np.asarray(pr["ch"], np.int64)[kq]], ch2env=newenv[np.asarray(pr["ch2env"], np.int64)[kc]],
+                               p=np.asarray(pr["p"])[kc], ref=np.asarray(pr["ref"], np.float64).reshape(-1, 2)[kc])
     return out
