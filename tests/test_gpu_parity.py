@@ -15,7 +15,10 @@ from helpers import fixtures, load_fixture, package_ns, rel_err
 
 pytestmark = pytest.mark.gpu
 
-GPU_SCENES = fixtures()
+# simplest scenes first, so that the first failure points at the least machinery
+_ORDER = ["strip_small", "strip_cfg1", "tendon", "line_search", "batch_colliders", "grip", "rigid_region",
+          "actuators", "body_mu", "mesh_cantilever", "mesh_bodies"]
+GPU_SCENES = [n for n in _ORDER if n in fixtures()] + [n for n in fixtures() if n not in _ORDER]
 TOL_FP64 = 1e-9
 TOL_MIXED = 1e-6
 
