@@ -224,7 +224,27 @@ def body_mu(ns):
     return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=150), dt=1e-3, steps=5, command=None)
 
 
+def kinematic_pose(ns):
+    """A kinematic body (add_kinematic_body) turned and moved by set_kinematic_pose presses a
+    soft block against a disc; a tendon in the block is tightened step by step."""
+    PX = 0.5e-3
+    m = ns.Model(device=ns.device)
+    m.add_disc(center=(0.0, -0.004), radius=0.004, mu=0.4)
+    blk = m.add_soft_body(np.ones((4, 6), np.uint8), physical_size=(6 * PX, 4 * PX),
+                          center=(0.0, 2 * PX + 0.9 * PX / 8), E=1.0e6, nu=0.40, density=1100.0)
+    jaw = m.add_kinematic_body(np.ones((2, 8), np.uint8), physical_size=(8 * PX, 2 * PX),
+                               center=(0.0, 4 * PX + 1 * PX + 0.5e-3))
+    m.finalize()
+    X = m.rest_x(blk)
+    cable = m.add_tendon(blk, through=[(x, X[:, 1].max() - PX) for x in np.unique(np.round(X[:, 0], 9))])
+
+    def command(k):
+        m.set_kinematic_pose(jaw, translation=(0.1 * PX * (k + 1), -0.3 * PX * (k + 1)), angle=0.02 * (k + 1))
+        m.set_tendon_tension(cable, 0.5 * (k + 1))
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=1000), dt=1e-3, steps=3, command=command)
+
+
 SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
           "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1,
           "rigid_region": rigid_region, "mesh_cantilever": mesh_cantilever, "mesh_bodies": mesh_bodies,
-          "actuators": actuators, "body_mu": body_mu}
+          "actuators": actuators, "body_mu": body_mu, "kinematic_pose": kinematic_pose}

@@ -47,6 +47,23 @@ def test_problem_matches_reference(name):
         assert (key in ref) == (mine.get(key) is not None), f"{key} presence differs"
 
 
+@pytest.mark.parametrize("name", [n for n in NAMES if scenes.SCENES[n](package_ns(device="cpu"))["command"]])
+def test_commands_match_reference(name):
+    """The per-step commands this package's Model produces for the scene (kinematic targets
+    from set_kinematic_target / set_kinematic_pose, tendon tensions) are the reference's,
+    step by step, bit for bit."""
+    ref, steps, _ = load_fixture(name)
+    sc = scenes.SCENES[name](package_ns(device="cpu"))
+    m = sc["model"]
+    bc = np.asarray(ref["bc_idx"], np.int64)
+    for k, st in enumerate(steps):
+        sc["command"](k)
+        if "bc_target" in st:
+            _same(np.asarray(m._targets, np.float64)[bc], st["bc_target"], f"step {k} bc_target")
+        if "Tcmd" in st:
+            _same(np.array([t["tension"] for t in m._tendons]), st["Tcmd"], f"step {k} Tcmd")
+
+
 def test_min_distance_refuses_touching_bodies():
     """Touching bodies are refused before the first step (implicit/integrator.py:288-294)."""
     import diff_2d_fem_gb300 as D
