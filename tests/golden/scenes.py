@@ -244,7 +244,31 @@ def kinematic_pose(ns):
     return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=1000), dt=1e-3, steps=3, command=command)
 
 
+def mesh_chamber(ns):
+    """A ring meshed in polar coordinates with its hole pressurised and an ambient pressure on
+    its outline, resting on the ground under gravity."""
+    ri, ro, n_t, n_r = 0.002, 0.004, 16, 2
+    r = np.linspace(ri, ro, n_r + 1)
+    th = 2.0 * np.pi * np.arange(n_t) / n_t
+    V = np.array([(rk * np.cos(t), rk * np.sin(t) + ro + 0.5e-3 / 8) for rk in r for t in th])
+    T = []
+    for k in range(n_r):
+        for j in range(n_t):
+            a, b = k * n_t + j, k * n_t + (j + 1) % n_t
+            c, d = a + n_t, b + n_t
+            T += [(a, b, d), (a, d, c)] if (j + k) % 2 else [(a, b, c), (b, d, c)]
+    m = ns.Model(device=ns.device)
+    m.add_ground(0.0, mu=0.6)
+    h = m.add_soft_mesh(V, np.array(T), E=0.5e6, nu=0.40, density=1100.0)
+    m.finalize(); m.gravity = (0.0, -9.81)
+    ch = m.add_pressure_chamber(h, at=(0.0, ro + 0.5e-3 / 8))
+    m.set_pressure(ch, 2.0e4)
+    m.set_pressure(m.add_ambient_pressure(h), 5.0e3)
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=400), dt=2e-3, steps=3, command=None)
+
+
 SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
           "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1,
           "rigid_region": rigid_region, "mesh_cantilever": mesh_cantilever, "mesh_bodies": mesh_bodies,
-          "actuators": actuators, "body_mu": body_mu, "kinematic_pose": kinematic_pose}
+          "actuators": actuators, "body_mu": body_mu, "kinematic_pose": kinematic_pose,
+          "mesh_chamber": mesh_chamber}
