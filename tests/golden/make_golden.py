@@ -134,7 +134,8 @@ def record(R, model, integ, dt, n_steps, command=None, name=""):
 
 # ----------------------------------------------------------------------------- scenes
 def run_scene(R, name):
-    ns = types.SimpleNamespace(Model=R.Model, ImplicitIntegrator=R.ImplicitIntegrator, device="cpu")
+    ns = types.SimpleNamespace(Model=R.Model, ImplicitIntegrator=R.ImplicitIntegrator, device="cpu",
+                               mask_to_mesh=R.mesh.mask_to_mesh)
     sc = scenes.SCENES[name](ns)
     return record(R, sc["model"], sc["integ"], sc["dt"], sc["steps"], sc["command"], name=name)
 

@@ -267,8 +267,24 @@ def mesh_chamber(ns):
     return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=400), dt=2e-3, steps=3, command=None)
 
 
+def tilted_plane(ns):
+    """A soft block on a plane tilted by 30 degrees (add_plane with a turned normal), placed
+    there as a turned mesh (mask_to_mesh), friction 0.3, under gravity: it slides."""
+    th = np.deg2rad(30.0)
+    n = np.array([-np.sin(th), np.cos(th)])
+    PX = 0.5e-3
+    V, T, _ = ns.mask_to_mesh(np.ones((4, 4), np.uint8), (4 * PX, 4 * PX), (0.0, 0.0))
+    R = np.array([[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]])
+    m = ns.Model(device=ns.device)
+    m.add_plane(normal=n, origin=(0.0, 0.0), mu=0.3)
+    m.add_soft_mesh(V @ R.T + (2 * PX + 0.9 * PX / 8) * n, T, E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    m.gravity = (0.0, -9.81)
+    return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=200), dt=2e-3, steps=4, command=None)
+
+
 SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
           "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1,
           "rigid_region": rigid_region, "mesh_cantilever": mesh_cantilever, "mesh_bodies": mesh_bodies,
           "actuators": actuators, "body_mu": body_mu, "kinematic_pose": kinematic_pose,
-          "mesh_chamber": mesh_chamber}
+          "mesh_chamber": mesh_chamber, "tilted_plane": tilted_plane}

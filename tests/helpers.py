@@ -24,7 +24,8 @@ def load_fixture(name):
 
 def package_ns(device="cuda"):
     import diff_2d_fem_gb300 as D
-    return types.SimpleNamespace(Model=D.Model, ImplicitIntegrator=D.ImplicitIntegrator, device=device)
+    return types.SimpleNamespace(Model=D.Model, ImplicitIntegrator=D.ImplicitIntegrator, device=device,
+                                 mask_to_mesh=D.mask_to_mesh)
 
 
 def rel_err(a, b):
