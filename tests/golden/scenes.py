@@ -283,8 +283,27 @@ def tilted_plane(ns):
     return dict(model=m, integ=ns.ImplicitIntegrator(max_iter=200), dt=2e-3, steps=4, command=None)
 
 
+def tendon_length(ns):
+    """A clamped cantilever bent by a length-controlled tendon (a stiff cable shortened to 97 %
+    of its built length), together with a tension-controlled one below the mid-line."""
+    m = ns.Model(device=ns.device); m.damping = 50.0
+    h = m.add_soft_body(np.ones((3, 16), np.uint8), physical_size=(0.008, 0.0015), center=(0.0, 0.0),
+                        E=1.0e6, nu=0.40, density=1100.0)
+    m.finalize()
+    X = m.rest_x(h)
+    m.set_kinematic_constraint(h, np.where(X[:, 0] < X[:, 0].min() + 1e-9)[0])
+    cols = np.unique(np.round(X[:, 0], 9))
+    top = m.add_tendon(h, through=[(x, 0.0005) for x in cols], stiffness=2.0e4)
+    m.set_tendon_length(top, 0.97 * m.tendon_length(top))
+    low = m.add_tendon(h, through=[(x, -0.0005) for x in cols])
+    m.set_tendon_tension(low, 3.0)
+    return dict(model=m, integ=ns.ImplicitIntegrator(self_collision=False, friction=False, max_iter=400),
+                dt=1e-3, steps=2, command=None)
+
+
 SCENES = {"strip_small": strip_small, "batch_colliders": batch_colliders, "grip": grip,
           "tendon": tendon, "line_search": line_search, "strip_cfg1": strip_cfg1,
           "rigid_region": rigid_region, "mesh_cantilever": mesh_cantilever, "mesh_bodies": mesh_bodies,
           "actuators": actuators, "body_mu": body_mu, "kinematic_pose": kinematic_pose,
-          "mesh_chamber": mesh_chamber, "tilted_plane": tilted_plane}
+          "mesh_chamber": mesh_chamber, "tilted_plane": tilted_plane,
+          "tendon_length": tendon_length}

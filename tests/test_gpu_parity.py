@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 # simplest scenes first, so that the first failure points at the least machinery
 _ORDER = ["strip_small", "strip_cfg1", "tendon", "line_search", "batch_colliders", "grip", "rigid_region",
-          "actuators", "body_mu", "kinematic_pose", "tilted_plane", "mesh_cantilever", "mesh_bodies", "mesh_chamber"]
+          "actuators", "body_mu", "kinematic_pose", "tilted_plane", "tendon_length", "mesh_cantilever", "mesh_bodies", "mesh_chamber"]
 GPU_SCENES = [n for n in _ORDER if n in fixtures()] + [n for n in fixtures() if n not in _ORDER]
 TOL_FP64 = 1e-9
 TOL_MIXED = 1e-6

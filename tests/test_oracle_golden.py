@@ -16,7 +16,7 @@ NAMES = fixtures()
 
 def test_fixtures_present():
     assert {"strip_small", "batch_colliders", "grip", "tendon", "line_search", "strip_cfg1",
-            "rigid_region", "mesh_cantilever", "mesh_bodies", "actuators", "body_mu", "kinematic_pose", "mesh_chamber", "tilted_plane"} <= set(NAMES)
+            "rigid_region", "mesh_cantilever", "mesh_bodies", "actuators", "body_mu", "kinematic_pose", "mesh_chamber", "tilted_plane", "tendon_length"} <= set(NAMES)
 
 
 @pytest.mark.parametrize("name", NAMES)
