@@ -90,6 +90,8 @@ def lib():
         _LIB.d2o_term.restype = None
         _LIB.d2o_sdf.argtypes = [C.c_int] + [C.c_double] * 5 + [_PD, C.c_int, _PD]
         _LIB.d2o_sdf.restype = None
+        _LIB.d2o_sdf_full.argtypes = [C.c_int] + [C.c_double] * 5 + [_PD, C.c_int, _PD, _PD, _PD]
+        _LIB.d2o_sdf_full.restype = None
         _LIB.d2o_affine_hessian.argtypes = [_PD, C.c_double, C.c_double, C.c_double, _PD, _PD, _PD]
         _LIB.d2o_affine_hessian.restype = None
         _LIB.d2o_chol6_solve.argtypes = [_PD, _PD, _PD]
@@ -370,6 +372,17 @@ def sdf(collider_row, pts):
     rx = c[6] if kind == 0 else c[3]
     lib().d2o_sdf(kind, c[1], c[2], rx, c[4], c[5], P.ctypes.data_as(_PD), len(P), d.ctypes.data_as(_PD))
     return d
+
+
+def sdf_full(collider_row, pts):
+    """A collider's level set with its gradient and Hessian at points (n, 2): (d (n,),
+    g (n, 2), H (n, 2, 2)) — the oracle's sdf_eval (any kind but the disc's closed form)."""
+    c = np.asarray(collider_row, np.float64)
+    P = _f64(pts, (-1, 2))
+    d, g, H = np.zeros(len(P)), np.zeros((len(P), 2)), np.zeros((len(P), 4))
+    lib().d2o_sdf_full(int(c[0]), c[1], c[2], c[3], c[4], c[5], P.ctypes.data_as(_PD), len(P),
+                       d.ctypes.data_as(_PD), g.ctypes.data_as(_PD), H.ctypes.data_as(_PD))
+    return d, g, H.reshape(-1, 2, 2)
 
 
 def affine_hessian(A, Mu, La, h2=1.0, Hx=None, Hy=None):

@@ -8,7 +8,7 @@ it directly (scipy), so its solution carries no Krylov tolerance:
   element tangent      assemble_Ke_kernel       implicit/adjoint.py:145-160 (nh_d2PsidF2_dir,
                                                 core/math.py:85-93)
   collider tangent     chvp_disc_kernel /       implicit/adjoint.py:88-114, frozen gate
-                       chvp_sdf_kernel          d in (0, dhat); disc and half-space here
+                       chvp_sdf_kernel          d in (0, dhat); every collider kind
   element force        drho_kernel              implicit/adjoint.py:164-178 (nh_dPsidF,
                                                 core/math.py:76-81)
   recursion            transient_adjoint        implicit/adjoint.py:371-399
@@ -107,7 +107,8 @@ def element_hessians(x, prob, mu=None, lam=None):
 
 def collider_blocks(x, prob):
     """(Nb, 2, 2): kappa (b'' g g^T + b' H_phi) per boundary node summed over the colliders,
-    gate frozen at d in (0, dhat). Disc (kind 0) and half-space (kind 4)."""
+    gate frozen at d in (0, dhat). Every collider kind: the disc and the half-space in closed
+    form, the other shapes through the oracle's level set, gradient and Hessian."""
     bnd = np.asarray(prob["bnd"], np.int64)
     dhat, kappa = float(prob["dhat"]), float(prob["kappa"])
     out = np.zeros((len(bnd), 2, 2))
@@ -124,8 +125,9 @@ def collider_blocks(x, prob):
             n = np.broadcast_to(c[3:5], p.shape)
             d = (p - c[1:3]) @ c[3:5]
             Hphi = np.zeros((len(p), 2, 2))
-        else:
-            raise NotImplementedError("collider kinds other than disc and half-space")
+        else:  # any other level set: kappa (b'' g g^T + b' H_phi), chvp_sdf_kernel (:101-114)
+            from . import sdf_full
+            d, n, Hphi = sdf_full(c, p)
         on = (d > 0.0) & (d < dhat)
         dd = np.where(on, d, dhat * 0.5)
         blk = kappa * (bpp(dd, dhat)[:, None, None] * n[:, :, None] * n[:, None, :]

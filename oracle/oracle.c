@@ -1183,6 +1183,18 @@ void d2o_sdf(int kind, double cx, double cy, double rx, double ry, double rref, 
     }
 }
 
+/* sdf_eval with its gradient (n x 2) and Hessian (n x 4, row-major) at each point, for the
+   adjoint oracle's collider tangent (chvp_sdf_kernel, implicit/adjoint.py:101-114) */
+void d2o_sdf_full(int kind, double cx, double cy, double rx, double ry, double rref, const double *pts, int n,
+                  double *d, double *g, double *H) {
+    for (int i = 0; i < n; ++i) {
+        sdfhit h = sdf_eval(kind, cx, cy, rx, ry, rref, ld(pts, i));
+        d[i] = h.d;
+        g[2 * i] = h.g.x; g[2 * i + 1] = h.g.y;
+        H[4 * i] = h.H.a; H[4 * i + 1] = h.H.b; H[4 * i + 2] = h.H.c; H[4 * i + 3] = h.H.d;
+    }
+}
+
 /* ------------------------------------------------------------------ Springs, implicit/actuation.py:381-476 */
 typedef struct { double ten, kt, len; v2 n; } spring_at_t;
 /* _spring (:396-402): tension k (|d| - L0), tangential stiffness max(k (1 - L0/|d|), 0) */

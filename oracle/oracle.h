@@ -107,6 +107,8 @@ void d2o_affine_hessian(const double *A4, double Mu, double La, double h2, const
                         double *H36);
 void d2o_chol6_solve(const double *H36, const double *b, double *x);
 /* A collider's level set at n points (x, y pairs) into d (test access). */
+void d2o_sdf_full(int kind, double cx, double cy, double rx, double ry, double rref, const double *pts, int n,
+                  double *d, double *g, double *H);
 void d2o_sdf(int kind, double cx, double cy, double rx, double ry, double rref, const double *pts, int n,
              double *d);
 

@@ -249,3 +249,54 @@ def test_adjoint_oracle_with_a_rigid_region():
             ("v0", 1.0, lambda e: loss(E, v0=v0 + e * dv)[0], float((res["dv0"] * dv).sum()))):
         fd = (L(eps) - L(-eps)) / (2 * eps)
         assert abs(fd - adj) <= FD_TOL * abs(adj), (name, fd, adj)
+
+
+def test_adjoint_oracle_through_a_level_set_collider():
+    """A soft block pressed by its kinematic top onto a rounded box (and, in a second run, an
+    ellipse) for 10 steps, frictionless: dL/dE along a random direction against central
+    differences of the forward oracle (3e-4) — the collider tangent through the level set's
+    gradient and Hessian (chvp_sdf_kernel, implicit/adjoint.py:101-114)."""
+    import warnings
+    from diff_2d_fem_gb300 import ImplicitIntegrator, Model, scene
+    for shape, kw in (("box", dict(rx=0.004, ry=0.002, corner_radius=0.0015)), ("ellipse", dict(rx=0.005, ry=0.003))):
+        m = Model()
+        m.add_object(shape, center=(0.0, 0.0), mu=0.0, **kw)
+        h = m.add_soft_body(np.ones((8, 6), np.uint8), physical_size=(0.003, 0.004),
+                            center=(0.0005, kw.get("ry", 0.0) + 0.002 + 0.2e-3), E=1.0e6, nu=0.40, density=1100.0)
+        m.finalize()
+        X = m.rest_x(h)
+        top = np.where(X[:, 1] > X[:, 1].max() - 1e-9)[0]
+        m.set_kinematic_constraint(h, top)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            prob = scene.solver_problem(m, ImplicitIntegrator(friction=False, self_collision=False, max_iter=20000), 1e-3)
+        prob = dict(prob, eps=1e-16, tol_x=0.0)
+        bc = np.asarray(prob["bc_idx"])
+        T = 10
+        targets = []
+        for k in range(1, T + 1):
+            tg = np.asarray(m.me.rest_pos, np.float64).copy()
+            tg[top, 1] -= 0.03e-3 * k
+            targets.append(tg[bc])
+        rng = np.random.default_rng(11)
+        E = 0.8 + 0.4 * rng.random(len(prob["mu"]))
+        N = np.asarray(prob["x"]).shape[0]
+        w = rng.standard_normal((N, 2))
+
+        def loss(E_):
+            p = dict(prob)
+            p["mu"], p["lam"] = E_ * prob["mu"], E_ * prob["lam"]
+            _, xs, _ = oracle.run(p, T, lambda k: dict(bc_target=targets[k]))
+            return float((w * xs[-1]).sum()), [np.asarray(p["x"], np.float64)] + xs
+
+        _, xs = loss(E)
+        d, _, _ = oracle.sdf_full(prob["colliders"][0], xs[-1][np.asarray(prob["bnd"])])
+        assert (d < m.dhat).sum() >= 2, f"{shape}: no contact"
+        res = OA.rollout_adjoint(prob, xs, {T: w}, E=E)
+        dE = rng.standard_normal(len(E))
+        # the forward steps stop at a floor of ~1e-12 of the loss (the level set's contact
+        # slows the last iterations): central differences at 3e-3 sit between that noise and
+        # their own O(h^2) error, good to ~1e-4 (the reference bounds this case at 3 %)
+        fd = (loss(E * (1 + 3e-3 * dE))[0] - loss(E * (1 - 3e-3 * dE))[0]) / 6e-3
+        adj = float((res["dE"] * E * dE).sum())
+        assert abs(fd - adj) <= 3e-4 * abs(adj), (shape, fd, adj)
