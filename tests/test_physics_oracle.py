@@ -319,3 +319,26 @@ def test_contact_scales_and_overlap():
     for i in range(2):
         ok.add_soft_body(np.ones((8, 8), np.uint8), physical_size=(0.008, 0.008), center=(0.0, 0.0), env_id=i)
     assert ok.finalize().n_envs == 2
+
+
+def test_collider_centres_reach_the_solver_buffer():
+    """DeviceSolver.set_collider_centers writes the centres into columns 1-2 of the collider
+    rows the step kernels read, leaving every other parameter as it was (host logic, on a CPU
+    tensor standing in for the device buffer)."""
+    import types
+    import torch
+    from diff_2d_fem_gb300.device import DeviceSolver
+    rows = torch.arange(24, dtype=torch.float64).reshape(3, 8)
+    fake = types.SimpleNamespace(_t={"colliders": rows.clone()})
+    DeviceSolver.set_collider_centers(fake, [[0.5, -0.25], [1.5, 2.5], [7.0, 8.0]])
+    got = fake._t["colliders"]
+    assert torch.equal(got[:, 1:3], torch.tensor([[0.5, -0.25], [1.5, 2.5], [7.0, 8.0]], dtype=torch.float64))
+    keep = [0, 3, 4, 5, 6, 7]
+    assert torch.equal(got[:, keep], rows[:, keep])
+    m = Model()
+    m.add_disc((0.0, 0.0), 0.01)
+    m.add_object("box", (0.1, 0.2), 0.02, 0.01, corner_radius=0.003)
+    m.add_ground(0.0)
+    assert [c.kind for c in m.colliders] == [0, 2, 4] and Model().object.kind == -1
+    m.set_collider_center(1, (0.3, 0.4))
+    assert np.allclose(m.colliders[1].c, (0.3, 0.4)) and m.colliders[1].rref == 0.003
