@@ -447,3 +447,25 @@ def test_adjoint_on_a_jittered_mesh(mode):
         fd = (J(rho0 + 0.05 * d) - J(rho0 - 0.05 * d)) / 0.1
         assert abs(g @ d - fd) < 1e-3 * np.linalg.norm(g) * np.linalg.norm(d), (g @ d, fd)
         assert abs(g @ d - fd) < 1e-2 * abs(fd), (g @ d, fd)
+
+
+def test_mesh_warnings():
+    """Slivers and a wide spread of element sizes are accepted with a warning, and a mesh
+    body near another one at rest is warned about before the first step."""
+    V = np.array([[0, 0], [1, 0], [0.5, 0.01], [0.5, -1]], float) * 1e-3
+    with pytest.warns(UserWarning, match="slivers"):
+        D.check_mesh(V, np.array([[0, 1, 2], [0, 3, 1]]))
+    Vr, Tr = _polar_ring(0.0001, 0.010, n_t=32)
+    with pytest.warns(UserWarning, match="the smallest element"):
+        Model().add_soft_mesh(Vr, Tr, E=E, nu=NU, density=RHO)
+    m = Model()
+    Va, Ta = _jittered(2, 2, (0.002, 0.002))
+    m.add_soft_mesh(Va, Ta, E=E, nu=NU, density=RHO)
+    m.add_soft_mesh(Va + np.array([0.002 + 0.3 * 0.25e-3 / 8, 0.0]), Ta, E=E, nu=NU, density=RHO)
+    m.finalize()
+    integ = ImplicitIntegrator()
+    with pytest.warns(UserWarning, match="inside the barrier's reach"):
+        try:
+            integ._build(m, 1e-3)
+        except RuntimeError:                 # no CUDA device here: the warning comes first
+            pass
