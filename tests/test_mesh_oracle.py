@@ -469,3 +469,24 @@ def test_mesh_warnings():
             integ._build(m, 1e-3)
         except RuntimeError:                 # no CUDA device here: the warning comes first
             pass
+
+
+def test_a_mesh_block_rests_on_a_pixel_slab():
+    """A jittered mesh block dropped on a pixel slab lying on the ground (contact between a
+    mesh body and a pixel body): it comes to rest within the barrier's reach of the slab —
+    after the reference's tests/test_mesh.py:322-340."""
+    m = Model()
+    m.damping = 60.0
+    m.add_ground(height=0.0, mu=0.6)
+    slab = m.add_soft_body(np.ones((4, 16), np.uint8), physical_size=(16 * PX, 4 * PX),
+                           center=(0.0, 2 * PX + 0.9 * PX / 8), E=E, nu=NU, density=RHO)
+    V, T = _jittered(6, 6, (6 * PX, 6 * PX), origin=(-3 * PX, 4 * PX + 0.6 * PX), seed=3)
+    block = m.add_soft_mesh(V, T, E=E, nu=NU, density=RHO)
+    m.finalize()
+    m.gravity = (0.0, -G0)
+    prob = _problem(m, ImplicitIntegrator(), 2e-3)
+    s, xs, _ = oracle.run(prob, 200)
+    gap = float(scene.min_distance(dict(prob, x=xs[-1])).min())
+    assert 0.0 < gap < m.dhat, gap / m.dhat
+    assert np.abs(s.v[m.body_nodes(block)]).max() < 2e-3
+    assert xs[-1][m.body_nodes(block), 1].min() > xs[-1][m.body_nodes(slab), 1].max()
