@@ -1,6 +1,8 @@
 """Golden vectors of the reference's adjoint — the script that made tests/golden/adjoint_*.npz.
 
-    python tests/golden/make_adjoint_golden.py [/path/to/Diff_2D_FEM]
+    python tests/golden/make_adjoint_golden.py /path/to/Diff_2D_FEM
+
+(or the checkout in the DIFF2DFEM_REFERENCE environment variable; there is no default)
 
 Runs the reference's own forward solve and its AdjointPNCG2D.transient_adjoint
 (implicit/adjoint.py:371-399) on the serial Warp stand-in (warp_shim.py), on a scene the
@@ -70,7 +72,9 @@ def press_disc(R, steps=4, dt=2.0e-4, seed=0):
 
 
 def main(argv):
-    ref = argv[0] if argv else "/root/reference"
+    ref = argv[0] if argv else os.environ.get("DIFF2DFEM_REFERENCE")
+    if not ref:
+        sys.exit("give the reference checkout as an argument or in DIFF2DFEM_REFERENCE")
     R = refload.load(ref)
     t0 = time.time()
     prob, steps, meta = press_disc(R)

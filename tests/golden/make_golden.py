@@ -1,6 +1,9 @@
 """Golden vectors from the reference's own solver code — the script that made tests/golden/*.npz.
 
-    python tests/golden/make_golden.py [/path/to/Diff_2D_FEM] [scene ...]
+    python tests/golden/make_golden.py /path/to/Diff_2D_FEM [scene ...]
+
+The reference checkout is the first argument that names a directory, or else the
+DIFF2DFEM_REFERENCE environment variable; there is no default.
 
 Each scene is built with the reference's own Model and ImplicitIntegrator, executed by the
 serial Warp stand-in in warp_shim.py (the reference's kernel source runs unchanged, in
@@ -141,13 +144,15 @@ def run_scene(R, name):
 
 
 def main(argv):
-    ref = "/root/reference"
+    ref = os.environ.get("DIFF2DFEM_REFERENCE")
     names = []
     for a in argv:
         if os.path.isdir(a):
             ref = a
         else:
             names.append(a)
+    if not ref:
+        sys.exit("give the reference checkout as an argument or in DIFF2DFEM_REFERENCE")
     R = refload.load(ref)
     for name in (names or list(scenes.SCENES)):
         t0 = time.time()
