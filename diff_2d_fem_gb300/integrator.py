@@ -76,19 +76,7 @@ class ImplicitIntegrator:
         model.time += dt
 
     def cfl_number(self, model, dt):
-        me = model.me
-        mu, lam = np.asarray(me.mu, np.float64), np.asarray(me.lam, np.float64)
-        soft = np.ones(len(mu), bool)
-        for a in model._affine:
-            soft[a["elems"]] = False
-        C = 0.0
-        for h, b in enumerate(model._bodies):
-            el = model._tri_range[h]
-            el = el[soft[el]]
-            if len(el) and not b.get("kinematic"):
-                cp = np.sqrt((lam[el] + 2.0 * mu[el]).max() / b["rho"])
-                C = max(C, cp * dt / model._cfl_length(h))
-        return float(C)
+        return _scene.cfl_number(model, dt)
 
     def stats(self, model):
         s = model._solver
@@ -130,13 +118,13 @@ class ImplicitIntegrator:
             if f is not None:
                 s.set_fext(f)
             if model._chambers:
-                s.set_pressures([c["pressure"] for c in model._chambers])
+                s.set_pressures([c.pressure for c in model._chambers])
             if model._tendons:
-                s.set_tendons([t["tension"] for t in model._tendons], [t["length"] for t in model._tendons])
+                s.set_tendons([t.tension for t in model._tendons], [t.length for t in model._tendons])
             if model._regions:
                 s.set_rest_shape(*_scene.rest_shape(model))
             if model._springs:
-                s.set_springs([k["anchor"] for k in model._springs], [k["length"] for k in model._springs])
+                s.set_springs([k.anchor for k in model._springs], [k.length for k in model._springs])
             s._ctrl_version = model._ctrl_version
 
     # ---- contact read-outs (implicit/integrator.py:340-358), computed on the device
@@ -176,7 +164,7 @@ class ImplicitIntegrator:
                     f"step. IPC contact needs the bodies to start apart: leave a gap between "
                     f"them (anything from model.dhat = {model.dhat:.3g} m up is out of the "
                     f"barrier's reach).")
-            if any(b.get("mesh") for b in model._bodies) and gap.min() < model.dhat:
+            if any(b.is_mesh for b in model._bodies) and gap.min() < model.dhat:
                 warnings.warn(
                     f"two boundaries are {gap.min():.3g} m apart at rest in environment "
                     f"{int(gap.argmin())}, inside the barrier's reach (model.dhat = "

@@ -17,24 +17,32 @@ from scipy.sparse import coo_matrix
 from scipy.sparse.csgraph import connected_components
 
 
+def cfl_number(model, dt):
+    """The acoustic CFL number of a step: the largest c_p dt / h over the bodies that are
+    not kinematic, c_p = sqrt((lambda + 2 mu) / rho) of their stiffest non-rigid element and
+    h the body's CFL length (implicit/integrator.py:88-122)."""
+    me = model.me
+    wave = (np.asarray(me.lam, np.float64) + 2.0 * np.asarray(me.mu, np.float64))
+    rigid = np.zeros(len(wave), bool)
+    for piece in model._affine:
+        rigid[piece.elems] = True
+    C = 0.0
+    for h, b in enumerate(model._bodies):
+        el = model._tri_range[h]
+        el = el[~rigid[el]]
+        if b.role == "kinematic" or not len(el):
+            continue
+        C = max(C, np.sqrt(wave[el].max() / b.rho) * dt / model._cfl_length(h))
+    return float(C)
+
+
 def iters_for(model, integ, dt):
     """Iteration budget of a step (implicit/integrator.py:88-122): iters_per_cfl x the
     acoustic CFL number of the stiffest soft body, clipped to [40 (120 with IPC contact
     between bodies), max_iter_cap]. Batch-global, as in the reference."""
     if integ.max_iter is not None:
         return int(integ.max_iter)
-    me = model.me
-    mu, lam = np.asarray(me.mu, np.float64), np.asarray(me.lam, np.float64)
-    soft = np.ones(len(mu), bool)
-    for a in model._affine:
-        soft[a["elems"]] = False
-    C = 0.0
-    for h, b in enumerate(model._bodies):
-        el = model._tri_range[h]
-        el = el[soft[el]]
-        if len(el) and not b.get("kinematic"):
-            cp = np.sqrt((lam[el] + 2.0 * mu[el]).max() / b["rho"])
-            C = max(C, cp * dt / model._cfl_length(h))
+    C = cfl_number(model, dt)
     n = int(np.ceil(integ.iters_per_cfl * C))
     lo = 120 if integ.self_collision and model.body_contact == "ipc" else 40
     return int(np.clip(n, lo, integ.max_iter_cap))
@@ -52,7 +60,7 @@ def _affine_arrays(model, mu_s, lam_s, free, x):
     node, grp, w, Mu, La, env = [], [], [], [], [], []
     owner = np.full(X.shape[0], -1)
     for b, g in enumerate(model._affine):
-        el = np.asarray(g["elems"], np.int64)
+        el = np.asarray(g.elems, np.int64)
         nd = np.unique(tri[el].reshape(-1))
         if (owner[nd] >= 0).any():
             raise ValueError("two rigid regions share a node; merge them or leave a gap of "
@@ -127,10 +135,10 @@ def _ipc_arrays(model, integ):
     ptr, idx = model.exclusion_csr()
     friction = integ.friction
     mu_node = None
-    if friction and any(b.get("mu") is not None for b in model._bodies):
+    if friction and any(b.mu is not None for b in model._bodies):
         mu_node = np.zeros(N, np.float64)
         for h, b in enumerate(model._bodies):
-            mu_node[model._node_range[h]] = model.body_friction if b.get("mu") is None else b["mu"]
+            mu_node[model._node_range[h]] = model.body_friction if b.mu is None else b.mu
     return dict(ea=edges[:, 0], eb=edges[:, 1], ela=pos[edges[:, 0]], elb=pos[edges[:, 1]], e2env=env,
                 ca=share[edges[:, 0]], cb=share[edges[:, 1]],
                 bstart=np.asarray(me.boundary_starts[:-1], np.int64),
@@ -143,39 +151,39 @@ def _ipc_arrays(model, integ):
 def _tendon_arrays(model):
     node, prv, nxt, tid = [], [], [], []
     for i, t in enumerate(model._tendons):
-        o, n = len(node), len(t["nodes"])
-        node += list(t["nodes"])
+        o, n = len(node), len(t.nodes)
+        node += list(t.nodes)
         tid += [i] * n
         prv += [-1] + list(range(o, o + n - 1))
         nxt += list(range(o + 1, o + n)) + [-1]
     T = model._tendons
     return dict(node=np.asarray(node, np.int64), prv=np.asarray(prv, np.int64), nxt=np.asarray(nxt, np.int64),
-                tid=np.asarray(tid, np.int64), t2env=np.asarray([model.body_env(t["body"]) for t in T], np.int64),
-                stiff=np.asarray([t["stiffness"] for t in T], np.float64),
-                L0=np.asarray([t["length"] for t in T], np.float64),
-                Tcmd=np.asarray([t["tension"] for t in T], np.float64))
+                tid=np.asarray(tid, np.int64), t2env=np.asarray([model.body_env(t.body) for t in T], np.int64),
+                stiff=np.asarray([t.stiffness for t in T], np.float64),
+                L0=np.asarray([t.length for t in T], np.float64),
+                Tcmd=np.asarray([t.tension for t in T], np.float64))
 
 
 def _spring_arrays(model):
     """Springs and pins (implicit/actuation.py:381-476): node b = -1 ties node a to `anchor`."""
     S = model._springs
-    return dict(a=np.asarray([k["a"] for k in S], np.int64), b=np.asarray([k["b"] for k in S], np.int64),
-                k=np.asarray([k["stiffness"] for k in S], np.float64),
-                L0=np.asarray([k["length"] for k in S], np.float64),
-                anchor=np.asarray([k["anchor"] for k in S], np.float64).reshape(-1, 2),
-                env=np.asarray([k["env"] for k in S], np.int64))
+    return dict(a=np.asarray([k.a for k in S], np.int64), b=np.asarray([k.b for k in S], np.int64),
+                k=np.asarray([k.stiffness for k in S], np.float64),
+                L0=np.asarray([k.length for k in S], np.float64),
+                anchor=np.asarray([k.anchor for k in S], np.float64).reshape(-1, 2),
+                env=np.asarray([k.env for k in S], np.int64))
 
 
 def _pressure_arrays(model):
     """Pressure boundaries (implicit/actuation.py:80-152): every chamber's directed edges
     (fluid on the left), its environment, gauge pressure and shoelace reference point."""
     Cs = model._chambers
-    return dict(ea=np.concatenate([c["ea"] for c in Cs]).astype(np.int64),
-                eb=np.concatenate([c["eb"] for c in Cs]).astype(np.int64),
-                ch=np.concatenate([np.full(len(c["ea"]), i) for i, c in enumerate(Cs)]).astype(np.int64),
-                ch2env=np.asarray([model.body_env(c["body"]) for c in Cs], np.int64),
-                p=np.asarray([c["pressure"] for c in Cs], np.float64),
-                ref=np.asarray([c["ref"] for c in Cs], np.float64).reshape(-1, 2))
+    return dict(ea=np.concatenate([c.ea for c in Cs]).astype(np.int64),
+                eb=np.concatenate([c.eb for c in Cs]).astype(np.int64),
+                ch=np.concatenate([np.full(len(c.ea), i) for i, c in enumerate(Cs)]).astype(np.int64),
+                ch2env=np.asarray([model.body_env(c.body) for c in Cs], np.int64),
+                p=np.asarray([c.pressure for c in Cs], np.float64),
+                ref=np.asarray([c.ref for c in Cs], np.float64).reshape(-1, 2))
 
 
 def rest_shape(model):
@@ -191,10 +199,10 @@ def rest_shape(model):
     tri = np.asarray(me.tri, np.int64)
     e1, e2 = rest[tri[:, 1]] - rest[tri[:, 0]], rest[tri[:, 2]] - rest[tri[:, 0]]
     for r in model._regions:
-        A = np.asarray(r["A"], np.float64)
+        A = np.asarray(r.A, np.float64)
         if np.array_equal(A, np.eye(2)):
             continue
-        el = r["elems"]
+        el = r.elems
         Bm[el] = Bm[el] @ np.linalg.inv(A)
         area[el] = area[el] * np.linalg.det(A)
         e1[el], e2[el] = e1[el] @ A.T, e2[el] @ A.T
@@ -237,8 +245,7 @@ def solver_problem(model, integ, dt):
         mu=mu_s, lam=lam_s, tri2env=np.asarray(me.tri2env, np.int64),
         bnd=np.asarray(me.boundary_nodes, np.int64), b2e=np.asarray(me.boundary2env, np.int64),
         bc_idx=np.asarray(bc, np.int64),
-        colliders=np.array([[c["kind"], c["cx"], c["cy"], c["rx"], c["ry"], c["rref"], c["r"], c["mu"]]
-                            for c in model._colliders], np.float64).reshape(-1, 8),
+        colliders=np.array([c.row() for c in model._colliders], np.float64).reshape(-1, 8),
         dt=float(dt), drag=math.exp(-float(dt) * cfg.damping), dhat=float(cfg.ipc_d_hat),
         kappa=float(cfg.obstacle_stiffness), epsv=float(cfg.obstacle_friction_epsv), eps=integ.eps,
         tol_x=integ.tol_x, near_factor=integ.near_factor, alpha_max=integ.alpha_max,

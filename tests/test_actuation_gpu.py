@@ -22,7 +22,7 @@ def _actuated(with_strain=True):
     m.set_pressure(m.add_pressure_chambers(h)[0], 2.0e4)
     m.set_pressure(m.add_ambient_pressure(h), 4.0e3)
     s1 = m.add_spring(h, (0.024, 0.059), h2, (0.029, 0.064), stiffness=2.0e4)
-    m.set_spring_length(s1, 0.8 * m._springs[s1]["length"])
+    m.set_spring_length(s1, 0.8 * m._springs[s1].length)
     m.add_spring(h, (0.036, 0.041), None, (0.040, 0.035), stiffness=3.0e4, rest_length=0.004)
     m.add_pin(h, (0.024, 0.041), stiffness=5.0e4)
     if with_strain:
@@ -98,10 +98,10 @@ def test_commands_reach_the_device():
         o.step()
     assert rel_err(xg[-1], o.x) < 1e-9
     m.set_pressure(0, 3.5e4)
-    m.set_spring_length(0, 0.7 * m._springs[0]["length"])
+    m.set_spring_length(0, 0.7 * m._springs[0].length)
     m.set_spring_anchor(1, (0.041, 0.034))
     o.set_pressure([3.5e4, 4.0e3])
-    o.set_springs(anchor=[s["anchor"] for s in m._springs], L0=[s["length"] for s in m._springs])
+    o.set_springs(anchor=[s.anchor for s in m._springs], L0=[s.length for s in m._springs])
     xg = _simulate(m, integ, 2)
     for _ in range(2):
         o.step()
@@ -110,8 +110,8 @@ def test_commands_reach_the_device():
     Bm, area, _ = scene.rest_shape(m)
     p2 = dict(prob, x=m.get_x(), v=m._solver.get_v(), Bm=Bm, area=area)
     p2["pressure"] = dict(prob["pressure"], p=np.array([3.5e4, 4.0e3]))
-    p2["springs"] = dict(prob["springs"], L0=np.array([s["length"] for s in m._springs]),
-                         anchor=np.array([s["anchor"] for s in m._springs]))
+    p2["springs"] = dict(prob["springs"], L0=np.array([s.length for s in m._springs]),
+                         anchor=np.array([s.anchor for s in m._springs]))
     _, xo, _ = oracle.run(p2, 2)
     xg = _simulate(m, integ, 2)
     assert rel_err(xg[-1], xo[-1]) < 1e-9
@@ -188,7 +188,7 @@ def test_pin_holds_a_hanging_body():
     for _ in range(200):
         integ.simulate(m, 1e-2)
     x = m.get_x()
-    a = m._springs[pin]["a"]
+    a = m._springs[pin].a
     W = float(np.asarray(m.me.mass).sum()) * 9.81
     assert np.linalg.norm(x[a] - np.array([-0.003, 0.003])) < 5 * W / 1.0e7
     c = x.mean(0)
@@ -231,7 +231,7 @@ def test_adjoint_pressure_and_springs_match_central_differences():
         m.set_pressure(m.add_ambient_pressure(h), p_amb)
         m.add_pin(h, (0.024, 0.041), stiffness=5.0e4)
         s2 = m.add_spring(h, (0.036, 0.059), None, (0.040, 0.066), stiffness=3.0e4)
-        m.set_spring_length(s2, 0.5 * m._springs[s2]["length"])
+        m.set_spring_length(s2, 0.5 * m._springs[s2].length)
         m.gravity = (0.0, -9.81)
         integ = ImplicitIntegrator(precision="fp64", max_iter=20000, eps=0.0, self_collision=False)
         s = integ.attach(m, DT)

@@ -62,7 +62,7 @@ def test_chamber_geometry():
     amb = m.add_ambient_pressure(h)
     assert abs(m.chamber_area(amb) - 280 * pw * ph) < 1e-12        # outline encloses solid + cavity
     c = m._chambers[ch[0]]
-    assert len(c["ea"]) == 2 * (10 + 6)                              # the cavity's perimeter in pixels
+    assert len(c.ea) == 2 * (10 + 6)                              # the cavity's perimeter in pixels
     with pytest.raises(ValueError):
         m.add_pressure_chamber(h, at=(0.0, 0.0))                      # off the body
     mk = np.ones((20, 14), np.uint8)
@@ -87,7 +87,7 @@ def test_activation_matrix_and_region():
     mk[5:9, 3:7] = 0
     m, h, _ = _model(mk, (0.010, 0.016))
     r = m.add_active_region(h, np.ones_like(mk))
-    assert len(m._regions[r]["elems"]) == 2 * int(mk.sum())
+    assert len(m._regions[r].elems) == 2 * int(mk.sum())
     with pytest.raises(ValueError):
         m.add_active_region(h, np.ones_like(mk))                      # overlaps
     m.set_activation(r, 1.08)
@@ -104,8 +104,8 @@ def test_spring_api():
     m, h, h2 = _cavity_block(second=(0.03, 0.065))
     s1 = m.add_spring(h, (0.024, 0.059), h2, (0.029, 0.064), stiffness=2.0e4)
     pin = m.add_pin(h, (0.036, 0.041))
-    assert m._springs[pin]["b"] == -1 and m._springs[pin]["length"] == 0.0
-    assert m._springs[s1]["length"] > 0.0
+    assert m._springs[pin].b == -1 and m._springs[pin].length == 0.0
+    assert m._springs[s1].length > 0.0
     t, ln = m.spring_force(s1)
     assert abs(t) < 1e-9 and ln > 0
     with pytest.raises(NotImplementedError):
@@ -165,7 +165,7 @@ def test_spring_derivatives():
     m.set_spring_length(s2, 0.003)
     # stretched springs only: a compressed one's tangential stiffness is clamped at zero in
     # the diagonal and in p^T H p (actuation.py:391-393), which no derivative reproduces
-    m.set_spring_length(s1, 0.5 * m._springs[s1]["length"])
+    m.set_spring_length(s1, 0.5 * m._springs[s1].length)
     prob = _prob(m, _integ(max_iter=1), 1e-3)
     sp = prob["springs"]
     assert list(sp["b"][1:]) == [-1, -1] and sp["L0"][1] == 0.003
@@ -204,7 +204,7 @@ def test_hydrostatic_state_is_exact_oracle():
     assert dev < 1e-4 * np.ptp(X[:, 1])
     # the cavities' sign flipped: nowhere near hydrostatic, so the test can fail
     for i, c in enumerate(m._chambers):
-        m.set_pressure(i, -p if c["sign"] > 0 else p)
+        m.set_pressure(i, -p if c.sign > 0 else p)
     _, xs, _ = oracle.run(_prob(m, _integ(max_iter=2000), 5e-3), 30)
     x = xs[-1]
     assert np.abs((x - x.mean(0)) - s_exact * Xc).max() > 100 * dev
@@ -250,9 +250,9 @@ def test_chambers_of_random_masks_are_closed_and_oriented():
         assert len(chambers) == len(sealed)
         pw, ph = m.pixel_size(h)
         for c in chambers:
-            ea, eb = m._chambers[c]["ea"], m._chambers[c]["eb"]
+            ea, eb = m._chambers[c].ea, m._chambers[c].eb
             assert np.array_equal(np.sort(ea), np.sort(eb))     # closed: in-degree = out-degree
-        total = sum(m._chambers[c]["area0"] for c in chambers)
+        total = sum(m._chambers[c].area0 for c in chambers)
         assert abs(total - sum((lab == k).sum() for k in sealed) * pw * ph) < 1e-15
         amb = m.add_ambient_pressure(h)
         assert abs(m.chamber_area(amb) - (mk.sum() + sum((lab == k).sum() for k in sealed)) * pw * ph) < 1e-12

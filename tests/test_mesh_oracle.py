@@ -150,8 +150,8 @@ def test_mesh_pressure_boundaries_are_the_pixel_ones():
         models.append((m, ch))
     (mp, cp), (mm, cm) = models
     for i, j in zip(cp, cm):
-        ep = set(zip(mp._chambers[i]["ea"].tolist(), mp._chambers[i]["eb"].tolist()))
-        em = set(zip(mm._chambers[j]["ea"].tolist(), mm._chambers[j]["eb"].tolist()))
+        ep = set(zip(mp._chambers[i].ea.tolist(), mp._chambers[i].eb.tolist()))
+        em = set(zip(mm._chambers[j].ea.tolist(), mm._chambers[j].eb.tolist()))
         assert ep == em, f"chamber {i}: the mesh's boundary is not the pixel one"
         assert abs(mp.chamber_area(i) - mm.chamber_area(j)) <= 1e-12 * mp.chamber_area(i)
     xs = [oracle.run(_problem(m, _integ(max_iter=300), 5e-3), 8)[1][-1] for m, _ in models]
@@ -328,7 +328,7 @@ def test_a_ring_under_internal_pressure():
     _, xs, _ = oracle.run(_problem(m, _integ(max_iter=4000, tol_x=0.0), 5e-3), 25)
     c = m._chambers[ch]
     from diff_2d_fem_gb300 import actuators as act
-    A1 = c["sign"] * act.loop_area(xs[-1], c["ea"], c["eb"], c["ref"])
+    A1 = c.sign * act.loop_area(xs[-1], c.ea, c.eb, c.ref)
     a = np.sqrt(A0 / np.pi)
     b = np.sqrt((m.element_areas(h).sum() + A0) / np.pi)
     ua = (1 + NU) / E * p * a * a / (b * b - a * a) * ((1 - 2 * NU) * a + b * b / a)

@@ -138,7 +138,7 @@ def test_every_shape_develops_contact(shape):
     x = m.get_body_x(h)
     assert np.all(np.isfinite(x))
     assert fmax > 1.0, fmax
-    row = [m._colliders[0][k] for k in ("kind", "cx", "cy", "rx", "ry", "rref", "r", "mu")]
+    row = m._colliders[0].row()
     assert oracle.sdf(row, x).min() > 0.0
 
 

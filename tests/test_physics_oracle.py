@@ -106,12 +106,12 @@ def test_pin_makes_a_pendulum_oracle():
     _, xs, _ = oracle.run(_problem(m, integ, dt), int(1.1 * period / dt))
     sp = m._springs[pin]
     far = nodes[np.linalg.norm(X - pivot, axis=1).argmax()]
-    r0 = m.get_x()[far] - m.get_x()[sp["a"]]
+    r0 = m.get_x()[far] - m.get_x()[sp.a]
     ang, gap = [], 0.0
     for x in xs:
-        r = x[far] - x[sp["a"]]
+        r = x[far] - x[sp.a]
         ang.append(np.arctan2(r0[0] * r[1] - r0[1] * r[0], r0 @ r) + th0)
-        gap = max(gap, float(np.linalg.norm(x[sp["a"]] - sp["anchor"])))
+        gap = max(gap, float(np.linalg.norm(x[sp.a] - sp.anchor)))
     ang = np.array(ang)
     t = dt * np.arange(1, len(ang) + 1)
     k = np.where(np.sign(ang[1:]) != np.sign(ang[:-1]))[0]

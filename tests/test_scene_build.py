@@ -61,7 +61,7 @@ def test_commands_match_reference(name):
         if "bc_target" in st:
             _same(np.asarray(m._targets, np.float64)[bc], st["bc_target"], f"step {k} bc_target")
         if "Tcmd" in st:
-            _same(np.array([t["tension"] for t in m._tendons]), st["Tcmd"], f"step {k} Tcmd")
+            _same(np.array([t.tension for t in m._tendons]), st["Tcmd"], f"step {k} Tcmd")
 
 
 def test_min_distance_refuses_touching_bodies():

@@ -126,7 +126,7 @@ def test_tendon_bends_a_cantilever_like_newton():
         m, h, X, left = _cantilever(ny, aspect, hb)
         td = m.add_tendon(h, through=[(xx, e) for xx in np.unique(np.round(X[:, 0], 9))])
         m.set_tendon_tension(td, T)
-        return m, X, left, m._tendons[td]["nodes"]
+        return m, X, left, m._tendons[td].nodes
 
     kr = {}
     for ny in (8, 16):
