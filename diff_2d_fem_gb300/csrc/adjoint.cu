@@ -39,7 +39,7 @@ __device__ __forceinline__ void bsum(double (&v)[NV], double *red) {
         const double t = wsum(v[k]);
         if (lane == 0) red[warp * NV + k] = t;
     }
-    __syncthreads();
+    block_barrier();
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
@@ -48,10 +48,10 @@ __device__ __forceinline__ void bsum(double (&v)[NV], double *red) {
             if (lane == 0) red[NW * NV + k] = t;
         }
     }
-    __syncthreads();
+    block_barrier();
 #pragma unroll
     for (int k = 0; k < NV; ++k) v[k] = red[NW * NV + k];
-    __syncthreads();
+    block_barrier();
 }
 
 // collider Hessian (2x2, frozen gate) and its clamped diagonal at x, for one boundary node
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
 
     for (;;) {
         if (tid == 0) sc_next = atomicAdd(d.work + 1, 1);
-        __syncthreads();
+        block_barrier();
         const int sc = sc_next;
         if (sc >= d.n_scenes) break;
         const d2f_seg sg = d.segs[sc];
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                 e[1].x = h1x; e[1].y = h1y;
                 e[2].x = h2x; e[2].y = h2y;
             }
-            __syncthreads();
+            block_barrier();
             // node pass: inertia + gathered corners (ascending triangle) + frozen collider barrier
             for (int i = n0 + tid; i < n1; i += NT) {
                 const double2 pi = V[i];
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                 }
                 AP[i] = make_double2(ax, ay);
             }
-            __syncthreads();
+            block_barrier();
             if (sg.nten > 0) {
                 // tendon (tension-controlled): geometric stiffness T/len (I - d d^T) per segment,
                 // the term of pHp_tendon_kernel (implicit/actuation.py:229-248)
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                     atomicAdd(&AP[n].x, h2 * ax);
                     atomicAdd(&AP[n].y, h2 * ay);
                 }
-                __syncthreads();
+                block_barrier();
             }
             if (sg.nsp > 0 || sg.npe > 0) {
                 // springs: h^2 (k n n^T + k (1 - L0/|d|) (I - n n^T)) on the ends' difference
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                     atomicAdd(&AP[a].x, sp * ty); atomicAdd(&AP[a].y, -sp * tx);
                     atomicAdd(&AP[b].x, sp * ty); atomicAdd(&AP[b].y, -sp * tx);
                 }
-                __syncthreads();
+                block_barrier();
             }
         };
 
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
             }
         }
         if (tid == 0) { s_stop = 0; s_status = 0; }
-        __syncthreads();
+        block_barrier();
         // ---- the Jacobi preconditioner; the initial guess (0, or lam as given with warm)
         for (int i = n0 + tid; i < n1; i += NT) {
             const double m = d.mass[i];
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
             }
             DI[i] = make_double2(dx, dy);
         }
-        __syncthreads();
+        block_barrier();
         for (int k = sg.sp0 + tid; k < sg.sp0 + sg.nsp; k += NT) {  // springs' diagonal (clamped, as the step's)
             const int a = d.sp_a[k], b = d.sp_b[k];
             const double2 xa = XL[a], xb = b >= 0 ? XL[b] : make_double2(d.sp_anchor[2 * k], d.sp_anchor[2 * k + 1]);
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
             atomicAdd(&DI[a].x, hx); atomicAdd(&DI[a].y, hy);
             if (b >= 0) { atomicAdd(&DI[b].x, hx); atomicAdd(&DI[b].y, hy); }
         }
-        __syncthreads();
+        block_barrier();
         for (int i = n0 + tid; i < n1; i += NT) {
             const uint8_t fm = d.free_mask[i];
             const double2 dd = DI[i];
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
             LAM[i] = l0;
             P[i] = l0;
         }
-        __syncthreads();
+        block_barrier();
         if (warm) hvp(P);  // A lam0
         // r = b - A lam0 on the free DOFs, z = D^-1 r, p = z
         double acc[3] = {0.0, 0.0, 0.0};
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
         bsum<NT, 3>(acc, red);
         const double bb = acc[2];
         if (tid == 0) s_rz = acc[0];
-        __syncthreads();
+        block_barrier();
         int it = 0;
         double rr = acc[1];
         for (; it < max_iter; ++it) {
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                 if (!(pa[0] > 0.0)) { s_stop = 1; s_status = D2F_ENAN; }  // not positive definite along p
                 s_alpha = pa[0] > 0.0 ? s_rz / pa[0] : 0.0;
             }
-            __syncthreads();
+            block_barrier();
             if (s_stop) break;
             const double al = s_alpha;
             double nr[2] = {0.0, 0.0};
@@ -341,19 +341,19 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
             bsum<NT, 2>(nr, red);
             rr = nr[1];
             if (tid == 0) { s_beta = nr[0] / s_rz; s_rz = nr[0]; }
-            __syncthreads();
+            block_barrier();
             const double be = s_beta;
             for (int i = n0 + tid; i < n1; i += NT) {
                 const double2 zi = Z[i], pi = P[i];
                 P[i] = make_double2(zi.x + be * pi.x, zi.y + be * pi.y);
             }
-            __syncthreads();
+            block_barrier();
         }
         if (tid == 0) {
             iters_out[sc] = it;
             status_out[sc] = s_status ? s_status : (rr > rtol * rtol * bb ? 1 : 0);
         }
-        __syncthreads();
+        block_barrier();
     }
 }
 

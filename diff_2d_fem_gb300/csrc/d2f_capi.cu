@@ -262,8 +262,14 @@ int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads,
 // that loads this library holds that array (D2F_NOALLOC_SCRATCH_BYTES) until the process
 // exits. The array is shared by every call on a device and keeps the last call's contents;
 // the queue head is cleared on each call and everything else is rewritten before it is
-// read, so no state carries over. Calls whose work overlaps on the GPU (different streams,
-// or different threads) race on it: serialise them.
+// read, so no state carries over. That holds for the contact-candidate lists and their
+// reference positions only because both step kernels rebuild the list at the start of
+// every step (S.rebuild = 1 in the step setup): a kernel that kept a list from one step to
+// the next would read another call's list here. Calls whose work overlaps on the GPU
+// (different streams, or different threads) race on it: serialise them. The array's device
+// address is looked up once per device, on the first call with that device current; after
+// cudaDeviceReset on that device the looked-up address belongs to the old context, so the
+// entry point must not be called again in that process.
 #include <mutex>
 
 static __device__ __align__(256) unsigned char d2f_noalloc_scratch[D2F_NOALLOC_SCRATCH_BYTES];

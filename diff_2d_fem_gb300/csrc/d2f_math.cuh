@@ -11,6 +11,19 @@
 
 namespace d2f {
 
+// Barriers of the thread group working on one scene. Both use the non-aligned PTX forms,
+// which count every thread on its own: a warp whose lanes arrive at different times (after
+// loops whose trip counts differ lane by lane) is waited for in full. The aligned block
+// barrier that __syncthreads() emits let warps through before slower warps of the same
+// block had arrived on this GB300 build (measured: up to 3e5 cycles of skew after a loop of
+// uneven trip counts), after which block reductions read shared values of another phase;
+// these kernels therefore never use it.
+__device__ __forceinline__ void block_barrier() { asm volatile("barrier.sync 0;" ::: "memory"); }
+// The whole thread-block cluster: arrive (release) and wait (acquire), non-aligned.
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
 __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
 __device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
 __device__ __forceinline__ double dabs(double a) { return a >= 0.0 ? a : -a; }

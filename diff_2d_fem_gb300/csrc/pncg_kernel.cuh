@@ -77,7 +77,7 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const int (&ops)[N
         double t = ops[k] == 0 ? warp_sum(v[k]) : (ops[k] == 1 ? warp_max(v[k]) : warp_min(v[k]));
         if (lane == 0) red[warp * NV + k] = t;
     }
-    __syncthreads();
+    block_barrier();
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
@@ -87,10 +87,10 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const int (&ops)[N
             if (lane == 0) red[NW * NV + k] = t;
         }
     }
-    __syncthreads();
+    block_barrier();
 #pragma unroll
     for (int k = 0; k < NV; ++k) v[k] = red[NW * NV + k];
-    __syncthreads();
+    block_barrier();
 }
 
 // ---------------------------------------------------------------------- per-scene shared state
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
 
     for (;;) {
         if (tid == 0) sc_next = atomicAdd(d.work, 1);
-        __syncthreads();
+        block_barrier();
         const int sc = sc_next;
         if (sc >= d.n_scenes) break;
         const d2f_seg sg = d.segs[sc];
@@ -215,14 +215,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             S.alpha = d.alpha_max; S.pHp = 0.0; S.q_inf = 0.0; S.alpha_s = 1.0;
             S.ncand = 0; S.rebuild = 1; S.gn0 = 0.0; S.beta = 0.0;
         }
-        __syncthreads();
+        block_barrier();
         if (!scene_ipc && !eread) {  // apply_bc_kernel, kernels.py:53-59
             for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
                 int n = d.bc_idx[b];
                 X[n] = Tgt[b];
                 Xh[n] = Tgt[b];
             }
-            __syncthreads();
+            block_barrier();
         }
 
         // ---------------------------------------------------------------- contact candidates
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 pos32[j] = make_float2((float)(xb.x - anchor.x), (float)(xb.y - anchor.y));
             }
             if (tid == 0) S.count = 0;
-            __syncthreads();
+            block_barrier();
             const float rad = (float)(d.reach + d.skin);
             const float slack = 1.0e-5f * rad;
             const long npair = (long)sg.ne * nbl;
@@ -290,17 +290,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 const unsigned bal = __ballot_sync(0xffffffffu, keep);
                 const int lane = tid & 31, warp = tid >> 5;
                 if (lane == 0) s_wcnt[warp] = __popc(bal);
-                __syncthreads();                      // s_wcnt and S.count readable
+                block_barrier();                      // s_wcnt and S.count readable
                 int off = S.count + __popc(bal & ((1u << lane) - 1u)), tot = 0;
                 for (int w = 0; w < NW; ++w) {
                     if (w < warp) off += s_wcnt[w];
                     tot += s_wcnt[w];
                 }
                 if (keep && off < sg.ncap) d.cand[sg.cand0 + off] = (int)(((unsigned)k << 16) | (unsigned)j);
-                __syncthreads();                      // every thread has read them
+                block_barrier();                      // every thread has read them
                 if (tid == 0) S.count += tot;         // read after the next chunk's first barrier
             }
-            __syncthreads();
+            block_barrier();
             double vm[1] = {(double)dmn};
             const int opm[1] = {2};
             block_reduce<NT, 1>(vm, opm, red);
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 S.rebuild = 0;
                 S.dmin_c = vm[0] - 1.0e-4 * (double)rad;  // FP32 rounding of the build distances
             }
-            __syncthreads();
+            block_barrier();
             ipc_far = S.dmin_c >= d.reach;
         };
 
@@ -485,7 +485,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 const bool rel = c < nc && Ctr[sg.cand0 + c].x < m0;
                 const unsigned bal = __ballot_sync(0xffffffffu, rel);
                 if ((tid & 31) == 0) s_wmask[tid >> 5] = bal;
-                __syncthreads();
+                block_barrier();
                 if (tid == 0) {
                     for (int w = 0; w < NW; ++w) {
                         unsigned msk = s_wmask[w];
@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                         }
                     }
                 }
-                __syncthreads();
+                block_barrier();
             }
             return m;
         };
@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 if (v[0] > 0.0) a_s = dmin(a_s, 0.45 * d.reach / v[0]);
                 S.alpha_s = a_s;
             }
-            __syncthreads();
+            block_barrier();
             const double alpha_s = S.alpha_s;
             for (int b = sg.bc0 + tid; b < sg.bc0 + sg.nbc; b += NT) {
                 int n = d.bc_idx[b];
@@ -633,21 +633,21 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 Xh[n] = nx;
             }
             if (tid == 0) S.q_inf = v[0];
-            __syncthreads();
+            block_barrier();
         };
 
         if (eread) {  // PNCG2DSolver.energy (solver.py:453-502): every term at x, nothing moved
             if (scene_ipc) ipc_refresh(true);
             const double e = scene_energy();
             if (tid == 0) d.energy_out[sc] = e;
-            __syncthreads();
+            block_barrier();
             continue;
         }
 
         if (scene_ipc && sg.nbc > 0) {  // IPCContact.advance_bc, ipc_contact.py:465-473
             sweep();
             if (tid == 0) S.pending = !(S.alpha_s >= 1.0);
-            __syncthreads();
+            block_barrier();
         }
 
 
@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                     if (S.q_inf > 0.0) S.active = 1;
                     if (it % 8 == 7) S.pending = !(S.alpha_s >= 1.0);
                 }
-                __syncthreads();
+                block_barrier();
             }
             if (!S.active && !S.pending) break;  // nothing can move this scene any more
             if (S.status != 0) break;
@@ -705,7 +705,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 ec[0] = G00; ec[1] = G01; ec[2] = G10; ec[3] = G11; ec[4] = c1;
                 ec[5] = e1x; ec[6] = e1y; ec[7] = e2x; ec[8] = e2y;
             }
-            __syncthreads();
+            block_barrier();
 
             // ---------------------------------------------- A2: node pass (gather + colliders + friction + force)
             for (int i = n0 + tid; i < n1; i += NT) {
@@ -813,14 +813,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 G[i] = mk2<R>(gx, gy);
                 D[i] = mk2<R>(dx, dy);
             }
-            __syncthreads();
+            block_barrier();
 
             // ---------------------------------------------- A3: contact between bodies, tendons
             if (scene_ipc) {
                 ipc_refresh(false);
                 double z0 = 0.0;
                 ipc_pairs(0, z0, 0.0);
-                __syncthreads();
+                block_barrier();
             }
             if (sg.nsp > 0 || sg.npe > 0) {
                 for (int k = sg.sp0 + tid; k < sg.sp0 + sg.nsp; k += NT) {  // Springs.grad_diag, actuation.py:405-424
@@ -847,7 +847,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                     atomicAdd(ga, R(gx)); atomicAdd(ga + 1, R(gy));
                     atomicAdd(gb, R(gx)); atomicAdd(gb + 1, R(gy));
                 }
-                __syncthreads();
+                block_barrier();
             }
             if (sg.nten > 0) {  // Tendon.grad_diag, actuation.py:169-212, 298-303
                 for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
@@ -871,7 +871,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                     double *ts = d.t_state + 4 * k;
                     ts[0] = L; ts[2] = tau; ts[3] = keff;
                 }
-                __syncthreads();
+                block_barrier();
                 for (int j = sg.tent0 + tid; j < sg.tent0 + sg.ntent; j += NT) {
                     int n = d.t_node[j], k = d.t_tid[j];
                     double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3];
@@ -898,7 +898,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                     atomicAdd(dp_, R(h2 * (tau * geox + keff * gLx * gLx)));
                     atomicAdd(dp_ + 1, R(h2 * (tau * geoy + keff * gLy * gLy)));
                 }
-                __syncthreads();
+                block_barrier();
             }
 
             // ---------------------------------------------- A4: body-level modes gather
@@ -930,7 +930,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 }
             }
             if (sg.naff > 0) {
-                __syncthreads();
+                block_barrier();
                 for (int k = sg.affn0 + tid; k < sg.affn0 + sg.naffn; k += NT) G[d.a_node[k]] = mk2<R>(R(0), R(0));
             }
             // RigidModes.gather (affine.py:404-453): centroid, B^T g, B^T g_prev, B^T D' B
@@ -993,7 +993,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                     S.g_Py += g[0] * zy[0] + g[1] * zy[1] + g[2] * zy[2];
                     S.y_Py += y[0] * zy[0] + y[1] * zy[1] + y[2] * zy[2];
                 }
-                __syncthreads();
+                block_barrier();
             }
 
             // ---------------------------------------------- B1: mask + Dai-Kou dot products
@@ -1058,7 +1058,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                     for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
                         for (int r = 0; r < 6; ++r) d.a_pq[6 * b + r] = -d.a_zq[6 * b + r] + bta * d.a_pq[6 * b + r];
                 }
-                __syncthreads();
+                block_barrier();
             }
 
             // ---------------------------------------------- B3: direction + node curvature and caps
@@ -1153,7 +1153,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                     }
                 }
             }
-            __syncthreads();
+            block_barrier();
 
             // ---------------------------------------------- B4: triangle pass (curvature + inversion cap)
             {
@@ -1284,7 +1284,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                         for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
                             for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
                 }
-                __syncthreads();
+                block_barrier();
             }
 
             // ---------------------------------------------- D1: update x (update_x_kernel + expand),
@@ -1295,7 +1295,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 double2 *__restrict__ X0 = reinterpret_cast<double2 *>(d.xu);
                 const double E0 = scene_energy();
                 for (int i = n0 + tid; i < n1; i += NT) X0[i] = X[i];
-                __syncthreads();
+                block_barrier();
                 auto trial = [&]() {  // set_x_from_x0_kernel, solver.py:52-60
                     if (S.active) {
                         const double al = S.alpha;
@@ -1305,14 +1305,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                             X[i] = make_double2(x0.x + al * double(pp.x), x0.y + al * double(pp.y));
                         }
                     }
-                    __syncthreads();
+                    block_barrier();
                 };
                 for (int bt = 0; bt < d.n_backtrack; ++bt) {
                     trial();
                     if (scene_ipc) ipc_refresh(false);
                     const double E = scene_energy();
                     if (tid == 0 && S.active && E > E0 + d.ls_tol * (dabs(E0) + 1.0)) S.alpha *= 0.5;
-                    __syncthreads();
+                    block_barrier();
                 }
                 trial();
             } else {
@@ -1333,7 +1333,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                     }
                     X[i] = nx;
                 }
-                __syncthreads();
+                block_barrier();
             }
         }
 
@@ -1347,7 +1347,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             d.active[sc] = S.active;
             d.status[sc] = S.status;
         }
-        __syncthreads();
+        block_barrier();
     }
 }
 

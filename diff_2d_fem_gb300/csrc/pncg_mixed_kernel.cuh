@@ -84,7 +84,7 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
 #pragma unroll
         for (int k = 0; k < NM; ++k) w[2 * NS + k] = m[k];
     }
-    __syncthreads();
+    block_barrier();
     // the per-warp partials: sum k by thread k (FP64), extremum k by thread NS + k
     {
         const int k = threadIdx.x;
@@ -102,7 +102,7 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
             mres[j] = a;
         }
     }
-    __syncthreads();
+    block_barrier();
 #pragma unroll
     for (int k = 0; k < NS; ++k) out_s[k] = dres[k];
 #pragma unroll
@@ -125,7 +125,7 @@ __device__ __forceinline__ void scene_reduce(double (&v)[NV], const int (&ops)[N
         cg::cluster_group cl = cg::this_cluster();
         constexpr int NW = NT / 32;
         double *mine = red + NW * NV;  // the block result, kept by block_reduce
-        cl.sync();
+        cluster_barrier();
         if (threadIdx.x < NV) {
             const int k = threadIdx.x;
             double a = cl.map_shared_rank(mine, 0)[k];
@@ -135,7 +135,7 @@ __device__ __forceinline__ void scene_reduce(double (&v)[NV], const int (&ops)[N
             }
             cres[k] = a;
         }
-        cl.sync();  // cres ready, and every remote read of `red` done before it is reused
+        cluster_barrier();  // cres ready, and every remote read of `red` done before it is reused
 #pragma unroll
         for (int k = 0; k < NV; ++k) v[k] = cres[k];
     }
@@ -149,7 +149,7 @@ __device__ __forceinline__ void scene_reduce_mx(FF (&s)[NS], float (&m)[NM], con
     if constexpr (CS > 1) {
         namespace cg = cooperative_groups;
         cg::cluster_group cl = cg::this_cluster();
-        cl.sync();
+        cluster_barrier();
         const int k = threadIdx.x;
         if (k < NS) {
             double a = 0.0;
@@ -164,7 +164,7 @@ __device__ __forceinline__ void scene_reduce_mx(FF (&s)[NS], float (&m)[NM], con
             }
             cmres[j] = a;
         }
-        cl.sync();
+        cluster_barrier();
 #pragma unroll
         for (int q = 0; q < NS; ++q) out_s[q] = cres[q];
 #pragma unroll
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     const int crank = CL ? (int)cg::this_cluster().block_rank() : 0;
     const int gt = crank * NT + tid;  // this thread's index among the scene's threads
     auto gsync = [&]() {              // a phase barrier of the scene's thread group
-        if constexpr (CL) cg::this_cluster().sync(); else __syncthreads();
+        if constexpr (CL) cluster_barrier(); else block_barrier();
     };
     const double dt = d.dt, h2 = dt * dt, inv_dt = 1.0 / dt;
     const double dhat = d.dhat;
@@ -417,11 +417,11 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         int sc;
         if constexpr (CL) {  // rank 0 takes the next scene; the cluster reads it from rank 0
             cg::cluster_group cl = cg::this_cluster();
-            cl.sync();
+            cluster_barrier();
             sc = *cl.map_shared_rank(&sc_next, 0);
-            cl.sync();  // every read of rank 0's sc_next done before any block moves on or exits
+            cluster_barrier();  // every read of rank 0's sc_next done before any block moves on or exits
         } else {
-            __syncthreads();
+            block_barrier();
             sc = sc_next;
         }
         if (sc >= d.n_scenes) break;
@@ -682,16 +682,16 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             auto cluster_offsets = [&](int mine) {
                 if constexpr (CL) {
                     if (tid == 0) s_cnt = 0;
-                    __syncthreads();
+                    block_barrier();
                     if ((tid & 31) == 0 && mine) atomicAdd(&s_cnt, mine);
                     cg::cluster_group cl = cg::this_cluster();
-                    cl.sync();
+                    cluster_barrier();
                     for (int r = 0; r < CS; ++r) {
                         const int c = *cl.map_shared_rank(&s_cnt, r);
                         if (r < crank) base_off += c;
                         n_all += c;
                     }
-                    cl.sync();
+                    cluster_barrier();
                 }
             };
             if (hashed) {
@@ -705,12 +705,12 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     return (int)(((unsigned)cx * 73856093u ^ (unsigned)cy * 19349663u) & (unsigned)(HASH_B - 1));
                 };
                 for (int h = tid; h < HASH_B; h += NT) hend[h] = 0u;
-                __syncthreads();
+                block_barrier();
                 for (int j = tid; j < nbl; j += NT) {
                     const float2 p = P32[j];
                     atomicAdd(&hend[bucket(cell_of(p.x), cell_of(p.y))], 1u);
                 }
-                __syncthreads();
+                block_barrier();
                 {  // exclusive scan of the counts: NT consecutive buckets per pass
                     unsigned carry = 0;
                     for (int base = 0; base < HASH_B; base += NT) {
@@ -723,7 +723,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                             if ((tid & 31) >= o) incl += u;
                         }
                         if ((tid & 31) == 31) s_wcnt[tid >> 5] = (int)incl;
-                        __syncthreads();
+                        block_barrier();
                         unsigned before = carry, tot = 0;
                         for (int w = 0; w < NW; ++w) {
                             if (w < (tid >> 5)) before += (unsigned)s_wcnt[w];
@@ -731,14 +731,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         }
                         if (h < HASH_B) hend[h] = before + incl - c;  // the bucket's start
                         carry += tot;
-                        __syncthreads();
+                        block_barrier();
                     }
                 }
                 for (int j = tid; j < nbl; j += NT) {  // the starts advance to the ends
                     const float2 p = P32[j];
                     hslot[atomicAdd(&hend[bucket(cell_of(p.x), cell_of(p.y))], 1u)] = j;
                 }
-                __syncthreads();
+                block_barrier();
                 // edge k's candidates: the slots in the buckets of the cells its box (grown by
                 // R) covers, each bucket once; all slots for an edge longer than that allows
                 auto walk = [&](int k, bool wr, int off) -> int {
@@ -788,7 +788,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     cluster_offsets(mine);
                 }
                 if (tid == 0) S.count = base_off;
-                __syncthreads();
+                block_barrier();
                 for (int base = e0; base < e1; base += NT) {  // pass 2: count, place, write
                     const int k = base + tid;
                     const int c = k < e1 ? walk(k, false, 0) : 0;
@@ -799,14 +799,14 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         if ((tid & 31) >= o) incl += u;
                     }
                     if ((tid & 31) == 31) s_wcnt[tid >> 5] = incl;
-                    __syncthreads();
+                    block_barrier();
                     int off = S.count + incl - c, tot = 0;
                     for (int w = 0; w < NW; ++w) {
                         if (w < (tid >> 5)) off += s_wcnt[w];
                         tot += s_wcnt[w];
                     }
                     if (c > 0) walk(k, true, off);
-                    __syncthreads();
+                    block_barrier();
                     if (tid == 0) S.count += tot;
                 }
             } else {
@@ -815,7 +815,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const long chunk = (npair + CS - 1) / CS;
                 const long q0 = CL ? (crank * chunk < npair ? crank * chunk : npair) : 0;
                 const long q1 = CL ? (q0 + chunk < npair ? q0 + chunk : npair) : npair;
-                __syncthreads();  // pos32 complete
+                block_barrier();  // pos32 complete
                 if constexpr (CL) {  // pass 1: count
                     int mine = 0;
                     for (long base = q0; base < q1; base += NT) {
@@ -827,7 +827,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     cluster_offsets((tid & 31) == 0 ? mine : 0);
                 }
                 if (tid == 0) S.count = base_off;
-                __syncthreads();
+                block_barrier();
                 for (long base = q0; base < q1; base += NT) {
                     const long q = base + tid;
                     bool keep = false;
@@ -842,18 +842,18 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     const unsigned bal = __ballot_sync(0xffffffffu, keep);
                     const int lane = tid & 31, warp = tid >> 5;
                     if (lane == 0) s_wcnt[warp] = __popc(bal);
-                    __syncthreads();
+                    block_barrier();
                     int off = S.count + __popc(bal & ((1u << lane) - 1u)), tot = 0;
                     for (int w = 0; w < NW; ++w) {
                         if (w < warp) off += s_wcnt[w];
                         tot += s_wcnt[w];
                     }
                     if (keep && off < sg.ncap) d.cand[sg.cand0 + off] = (int)(((unsigned)k << 16) | (unsigned)j);
-                    __syncthreads();
+                    block_barrier();
                     if (tid == 0) S.count += tot;
                 }
             }
-            __syncthreads();
+            block_barrier();
             double vm[1] = {(double)dmn};
             const int opm[1] = {2};
             scene_reduce<NT, CS, 1>(vm, opm, red, cres);
@@ -1031,13 +1031,13 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int cchunk = (nc + CS - 1) / CS;
                 const int c0 = min(crank * cchunk, nc), c1 = min(c0 + cchunk, nc);
                 if (tid == 0) s_nrel = 0;
-                __syncthreads();
+                block_barrier();
                 for (int base = c0; base < c1; base += NT) {
                     const int c = base + tid;
                     const bool rel = c < c1 && Ctr[sg.cand0 + c].x < m0;
                     const unsigned bal = __ballot_sync(0xffffffffu, rel);
                     if ((tid & 31) == 0) s_wmask[tid >> 5] = bal;
-                    __syncthreads();
+                    block_barrier();
                     int off = s_nrel + __popc(bal & ((1u << (tid & 31)) - 1u)), tot = 0;
                     for (int w = 0; w < NW; ++w) {
                         const int pc = __popc(s_wmask[w]);
@@ -1045,11 +1045,11 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         tot += pc;
                     }
                     if (rel && off < REL_CAP) s_rel[off] = c;
-                    __syncthreads();
+                    block_barrier();
                     if (tid == 0) s_nrel += tot;
                 }
                 cg::cluster_group cl = cg::this_cluster();
-                cl.sync();
+                cluster_barrier();
                 bool over = false;  // a list that did not fit: the full walk below, every block
                 for (int r = 0; r < CS; ++r) over |= *cl.map_shared_rank(&s_nrel, r) > REL_CAP;
                 double m = m0;
@@ -1068,7 +1068,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         }
                     }
                 }
-                cl.sync();  // every remote read done before the lists are rebuilt
+                cluster_barrier();  // every remote read done before the lists are rebuilt
                 if (!over) return m;
             }
             double m = m0, t_c = m0;
@@ -1078,7 +1078,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const bool rel = c < nc && Ctr[sg.cand0 + c].x < m0;
                 const unsigned bal = __ballot_sync(0xffffffffu, rel);
                 if ((tid & 31) == 0) s_wmask[tid >> 5] = bal;
-                __syncthreads();
+                block_barrier();
                 if (tid == 0) {
                     for (int w = 0; w < NW; ++w) {
                         unsigned msk = s_wmask[w];
@@ -1092,7 +1092,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         }
                     }
                 }
-                __syncthreads();
+                block_barrier();
             }
             return m;
         };

@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(kReadThreads) contact_force_kernel(const __gri
         const double *c = d.colliders + 8 * tid;
         cols[tid] = Col{(int)c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7]};
     }
-    __syncthreads();
+    block_barrier();
     const double2 *X = reinterpret_cast<const double2 *>(d.x);
     const double2 *Xn = reinterpret_cast<const double2 *>(d.xn);
     const double dhat = d.dhat, kappa = d.kappa, inv_dt = 1.0 / d.dt, epsv = d.epsv;

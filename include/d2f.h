@@ -235,7 +235,10 @@ int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads,
  * GPU loading the library holds until exit. A batch needing more scratch than that is
  * refused with D2F_EINVAL and a message. The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress); make that first call before any stream capture.
- * Every call shares the array: calls that overlap on the GPU race — serialise them.
+ * The address is kept for the life of the process: after cudaDeviceReset on a device, do
+ * not call this entry point again on it. Every call shares the array and keeps the last
+ * call's contents (the queue head is cleared, the candidate lists are rebuilt at each step
+ * start): calls that overlap on the GPU race — serialise them.
  * No counterpart in the reference: its solver always owns its own buffers. */
 int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream);
 
