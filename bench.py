@@ -108,6 +108,47 @@ TRAFFIC_PER_SCENE_ITER = {
 }
 
 
+# FP64 operations of the plain FP64 step kernel per PNCG iteration, counted from its source
+# (adds, subtracts, multiplies and divides; a fused multiply-add counts two; log and sqrt one
+# each; compares and min/max none):
+#   per triangle: gradient and Jacobi-diagonal pass 115, curvature and inversion-cap pass 83,
+#                 the nodes' gather of its three corner sums 12
+#   per node:     inertia 4, mask and the five Dai-Kou dot products 32, direction, p^T M p and
+#                 |p| 15, position update 4
+# The boundary nodes' collider terms add a few more per boundary node and are left out.
+FP64_OPS_PER_TRI_ITER = 115 + 83 + 12
+FP64_OPS_PER_NODE_ITER = 4 + 32 + 15 + 4
+
+
+def fp64_ops(prob, iters):
+    """Counted FP64 operations of one FP64 step at the iteration counts run."""
+    B = int(prob["B"])
+    n = np.bincount(np.asarray(prob["node2env"]), minlength=B)
+    t = np.bincount(np.asarray(prob["tri2env"]), minlength=B)
+    return float((np.asarray(iters, np.float64) * (FP64_OPS_PER_TRI_ITER * t + FP64_OPS_PER_NODE_ITER * n)).sum())
+
+
+def fp64_peak(dev, n=4096, reps=5):
+    """Measured FP64 rate of this GPU: cuBLAS DGEMM (torch.matmul on float64, n^3), best of
+    `reps`, in TFLOP/s."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize(dev)
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / best / 1e12
+
+
 # ----------------------------------------------------------------------------- CPU baseline
 def cpu_sample(prob, state_x, state_v, n_threads, per_thread, seed=1):
     """The serial FP64 oracle on a bounded sample: n_threads threads, each advancing its own
@@ -227,6 +268,109 @@ def measure_grads(args, dev):
             "loss": loss}
 
 
+def measure_single_strip(args, dev):
+    """The single-scene configuration: one 6 x 72-pixel strip (511 nodes, 864 triangles) on
+    the ground, dt 2 ms, the reference's default integrator. Scene-steps/s of the FP64 path
+    (the reference's arithmetic) and of the mixed path over `strip_steps` steps after 5
+    warm-up steps (CUDA events), and their position difference after those steps."""
+    import torch
+    from diff_2d_fem_gb300 import workloads, scene, ImplicitIntegrator
+    from diff_2d_fem_gb300.device import DeviceSolver
+    m, kw, dt = workloads.strip_on_ground()
+    prob = scene.solver_problem(m, ImplicitIntegrator(**kw), dt)
+    prob["rest"] = np.asarray(m.me.rest_pos, np.float64)
+    stream = torch.cuda.current_stream(dev)
+    out, xs = {}, {}
+    for prec in ("fp64", "mixed"):
+        s = DeviceSolver(prob, precision=prec)
+        for _ in range(5):
+            s.step()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(args.strip_steps):
+            s.step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.strip_steps
+        it, _, st = s.stats()
+        xs[prec] = s.get_x()
+        out[prec] = {"value": 1e3 / ms, "unit": "scene-steps/s", "ms_per_step": ms, "iters_last": int(it[0]),
+                     "status_ok": bool((st == 0).all())}
+        s.close()
+    out["pos_err_mixed_rel_to_coords"] = float(np.abs(xs["mixed"] - xs["fp64"]).max() / np.abs(xs["fp64"]).max())
+    out["workload"] = (f"strip_on_ground: 6x72 px (511 nodes, 864 triangles), E 0.5 MPa, nu 0.40, ground mu 0.8, "
+                       f"dt {dt}, iter_max {int(prob['iter_max'])}, steps 6..{5 + args.strip_steps}")
+    return out
+
+
+def measure_contact_batch(args, dev):
+    """The contact-heavy configuration: 512 scenes of a soft pad pushed by a kinematic jaw
+    squeezing an affine 1 GPa block against a second pad (IPC contact with per-scene
+    friction, d-hat 0.1 mm, dt 1 ms). Both precisions advance the same scenes the same
+    `contact_steps` steps from rest (the jaw's targets of each step); the mixed path is the
+    headline. Reported: scene-steps/s of each (CUDA events over the steps), the position
+    difference between them, and the difference of the step energies at the two end states
+    (every term, barriers included), evaluated by the FP64 energy read-out."""
+    import warnings
+    import torch
+    from diff_2d_fem_gb300 import workloads, scene, ImplicitIntegrator
+    from diff_2d_fem_gb300.device import DeviceSolver
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")              # mixed pixel sizes, as configured
+        m, kw, dt, ex = workloads.pads_and_block(args.contact_scenes, seed=0)
+    ex["command"](0)
+    prob = scene.solver_problem(m, ImplicitIntegrator(**kw), dt)
+    prob["rest"] = np.asarray(m.me.rest_pos, np.float64)
+    bc = np.asarray(prob["bc_idx"])
+    targets = []
+    for k in range(args.contact_steps):
+        ex["command"](k)
+        targets.append(np.asarray(m._targets, np.float64).copy())
+    stream = torch.cuda.current_stream(dev)
+    out, xs, its = {}, {}, {}
+    for prec in ("mixed", "fp64"):
+        s = DeviceSolver(prob, precision=prec)
+        ms = 0.0
+        for k in range(args.contact_steps):
+            s.set_targets(targets[k])
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.step()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms += e0.elapsed_time(e1)
+        it, ac, st = s.stats()
+        xs[prec], its[prec] = s.get_x(), it
+        out[prec] = {"value": prob["B"] * args.contact_steps / (ms / 1e3), "unit": "scene-steps/s",
+                     "ms_per_step": ms / args.contact_steps, "iters_mean_last": float(it.mean()),
+                     "converged_last": float((ac == 0).mean()), "status_ok": bool((st == 0).all())}
+        s.close()
+        torch.cuda.empty_cache()
+    x64, xmx = xs["fp64"], xs["mixed"]
+    out["pos_err_rel_to_coords"] = float(np.abs(xmx - x64).max() / np.abs(x64).max())
+    # step energy (inertia, elastic, barriers, friction, forces) with the FP64 end state as x_n
+    # and x_hat, at the FP64 and at the mixed end state: the first is the potential energy
+    # there, the difference the energy error of the mixed state
+    ev = DeviceSolver(prob, precision="fp64")
+    ev.set_targets(targets[-1])
+    ref = torch.as_tensor(x64, device=dev)
+    ev.x.copy_(ref)
+    ev.xn.copy_(ref)
+    ev.xhat.copy_(ref)
+    e64 = ev.energy()
+    ev.x.copy_(torch.as_tensor(xmx, device=dev))
+    emx = ev.energy()
+    ev.close()
+    out["energy_err_rel"] = float(np.max(np.abs(emx - e64) / np.maximum(np.abs(e64), 1e-300)))
+    out["energy_err_rel_median"] = float(np.median(np.abs(emx - e64) / np.maximum(np.abs(e64), 1e-300)))
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["workload"] = (f"pads_and_block x{prob['B']}: 40x40-px pad (E 0.3 MPa) pushed at 10 mm/s, 16x16-px affine "
+                       f"block (1 GPa), second pad; d-hat 0.1 mm, mu U[0.4, 0.8], offset U[-2, 2] mm; dt {dt}, "
+                       f"iter_max {int(prob['iter_max'])}, steps 1..{args.contact_steps} from rest")
+    return out
+
+
 def measure_large_scene(args, dev):
     """The large-scene workload: a 256 x 1024-pixel slab (0.5 mm pixels, E 1 MPa, nu 0.40) with
     200 holes and 32 affine discs dropped onto it, dt 1e-3, one scene and a batch of 8, mixed
@@ -281,6 +425,52 @@ def measure_large_scene(args, dev):
     return out
 
 
+# ----------------------------------------------------------------------------- replicas
+class Replicas:
+    """The host side of N replicas, one rank per GPU: every rank advances its own batch; the
+    ranks meet only at a barrier before and after the timed region and in the maximum over
+    ranks of the elapsed time; the job's throughput counts every rank's scenes over that
+    maximum. `sync` waits for the rank's device work; `reduce_device` holds the all-reduce's
+    tensor (a CUDA device under NCCL, the CPU under gloo)."""
+
+    def __init__(self, world, sync=None, reduce_device="cpu"):
+        self.world, self.sync, self.reduce_device = world, sync or (lambda: None), reduce_device
+
+    def barrier(self):
+        self.sync()
+        if self.world > 1:
+            import torch.distributed as tdist
+            tdist.barrier()
+
+    def maxr(self, v):
+        """The maximum of v over the ranks (every rank gets it)."""
+        if self.world <= 1:
+            return v
+        import torch
+        import torch.distributed as tdist
+        t = torch.tensor([v], dtype=torch.float64, device=self.reduce_device)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(self, step, K, W, clock):
+        """W untimed calls of step(), a barrier, K timed calls, a barrier; clock() starts a
+        timer and returns the function that stops it and gives the elapsed milliseconds.
+        Returns this rank's milliseconds (take maxr of it for the job's)."""
+        for _ in range(W):
+            step()
+        self.barrier()
+        stop = clock()
+        for _ in range(K):
+            step()
+        ms = stop()
+        self.barrier()
+        return ms
+
+    def value(self, scenes_per_rank, K, ms_max):
+        """Job throughput in scene-steps/s: every rank's scenes over the slowest rank's time."""
+        return scenes_per_rank * K * self.world / (ms_max / 1e3)
+
+
 # ----------------------------------------------------------------------------- GPU arm
 def run_ours(args, rank, world):
     import torch
@@ -317,29 +507,15 @@ def run_ours(args, rank, world):
     mixed = args.precision == "mixed"
     stream = torch.cuda.current_stream(dev)
 
-    def barrier():
-        torch.cuda.synchronize(dev)
-        if dist:
-            tdist.barrier()
-
-    def maxr(v):
-        if not dist:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        return float(t.item())
+    rep = Replicas(world, sync=lambda: torch.cuda.synchronize(dev), reduce_device=dev)
+    barrier, maxr = rep.barrier, rep.maxr
 
     def timed(solver, K, W):
-        for _ in range(W):
-            solver.step()
-        barrier()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(K):
-            solver.step()
-        ev1.record(stream)
-        barrier()
-        ms = ev0.elapsed_time(ev1)
+        def clock():
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            return lambda: (ev1.record(stream), torch.cuda.synchronize(dev), ev0.elapsed_time(ev1))[-1]
+        ms = rep.timed(solver.step, K, W, clock)
         it, ac, st = solver.stats()
         return ms, it, st
 
@@ -370,8 +546,8 @@ def run_ours(args, rank, world):
         ms, it_last, st = timed(sol, args.steps, args.warmup)
     ms = maxr(ms)
     n_sc = prob["B"]
-    value = n_sc * args.steps * world / (ms / 1e3)
-    x_head = sol.get_x()
+    value = rep.value(n_sc, args.steps, ms)
+    x_head, v_head = sol.get_x(), sol.get_v()
     bytes_last = algorithmic_bytes(prob, it_last, mixed)
 
     # per-launch time of the step kernel, on the launching stream (one launch = one step)
@@ -392,7 +568,7 @@ def run_ours(args, rank, world):
     sol2 = DeviceSolver(prob, precision=other, threads=shapes[other][0][0], blocks_per_sm=shapes[other][0][1])
     ms2, it2, st2 = timed(sol2, args.steps, args.warmup)
     ms2 = maxr(ms2)
-    value2 = n_sc * args.steps * world / (ms2 / 1e3)
+    value2 = rep.value(n_sc, args.steps, ms2)
     x2 = sol2.get_x()
     sol2.close()
     del sol2
@@ -430,16 +606,26 @@ def run_ours(args, rank, world):
 
     grads = None if args.no_grads else measure_grads(args, dev)
     large = None if args.no_large else measure_large_scene(args, dev)
+    strip = None if args.no_strip else measure_single_strip(args, dev)
+    contact = None if args.no_contact else measure_contact_batch(args, dev)
 
     if rank != 0:
         if dist:
             tdist.destroy_process_group()
         return
 
-    # ---- CPU baseline: the oracle on a bounded sample, from the benchmarked state
+    # ---- CPU baseline: the oracle on a bounded sample, from the benchmarked state (the GPU
+    # arm's state after its warm-up and timed steps; the sample times the next step)
     threads = min(os.cpu_count() or 1, 16)
-    cpu_val, cpu_desc = cpu_sample(prob, None, None, threads, 4)
-    cpu_desc += " (first step from rest)"
+    cpu_val, cpu_desc = cpu_sample(prob, x_head, v_head, threads, 4)
+    cpu_desc += f" (step {args.warmup + args.steps + 1}, from the GPU arm's state after its timed steps)"
+
+    # ---- FP64 fraction of the plain FP64 kernel: counted FP64 operations per step over its
+    # time per step, against this GPU's measured DGEMM rate
+    t64_ms = (ms2 if mixed else ms) / args.steps
+    it64 = it2 if mixed else it_last
+    fp64_rate = fp64_ops(prob, it64) / (t64_ms / 1e3) / 1e12
+    fp64_pk = fp64_peak(dev)
 
     peaks, src = _peaks()
     hbm = float(peaks.get("hbm_gbs", HBM_FALLBACK_GBS))
@@ -478,6 +664,12 @@ def run_ours(args, rank, world):
                          "sample": cpu_desc},
         "grads": grads,
         "large_scene": large,
+        "single_strip": strip,
+        "contact_batch": contact,
+        "fp64_fraction": {"achieved": fp64_rate, "peak": fp64_pk, "unit": "TFLOP/s", "frac": fp64_rate / fp64_pk,
+                          "ops_per_triangle_iter": FP64_OPS_PER_TRI_ITER, "ops_per_node_iter": FP64_OPS_PER_NODE_ITER,
+                          "peak_source": "measured: cuBLAS DGEMM (torch.matmul float64, 4096^3), best of 5",
+                          "kernel": "the plain FP64 step kernel on this batch"},
     }
     print(json.dumps(rec))
     if dist:
@@ -500,6 +692,11 @@ def main():
     ap.add_argument("--no-grads", action="store_true", help="skip the grads/s measurement")
     ap.add_argument("--no-large", action="store_true", help="skip the large-scene measurement")
     ap.add_argument("--large-steps", type=int, default=3, help="large-scene workload: timed steps")
+    ap.add_argument("--strip-steps", type=int, default=50, help="single-strip workload: timed steps")
+    ap.add_argument("--no-strip", action="store_true", help="skip the single-strip measurement")
+    ap.add_argument("--contact-scenes", type=int, default=512, help="contact-heavy workload: scenes")
+    ap.add_argument("--contact-steps", type=int, default=20, help="contact-heavy workload: steps from rest")
+    ap.add_argument("--no-contact", action="store_true", help="skip the contact-heavy measurement")
     ap.add_argument("--profile-large", type=int, default=0,
                     help="run only the large-scene step (this many slabs), for profilers")
     ap.add_argument("--profile-only", action="store_true",

@@ -1,9 +1,10 @@
 """The multi-GPU form of the step is N replicas: scenes are independent, so each rank
 advances its own batch and the ranks meet only at the barriers around the timed region and
-in the max-over-ranks of the elapsed time. This runs that host logic at world size 2 over
-gloo on the CPU, the oracle standing in for the device step: each rank builds the
-rectangles batch with its own seed, steps it, and reports its time; the job's time is the
-slowest rank's and the throughput counts every rank's scenes.
+in the max-over-ranks of the elapsed time. This runs bench.py's own replica logic
+(bench.Replicas: barriers, timed region, max over ranks, job throughput) at world size 2
+over gloo on the CPU, the oracle standing in for the device step: each rank builds the
+rectangles batch with its own seed (as bench.py does), steps it, and reports its time; the
+job's time is the slowest rank's and the throughput counts every rank's scenes.
 
 Checks: the replicas are different batches of the same size, each replica ends exactly where
 the same batch run alone ends (nothing crosses ranks), and every rank sees the same maximum."""
@@ -27,24 +28,27 @@ def _batch(seed):
 
 
 def _rank(rank, port, out):
+    import sys
     import torch
     import torch.distributed as dist
     import oracle
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=WORLD)
     try:
         prob = _batch(rank)
-        dist.barrier()
-        t0 = time.perf_counter()
-        _, xs, _ = oracle.run(prob, STEPS)
-        dist.barrier()
-        ms = (time.perf_counter() - t0) * 1e3
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        solver = oracle.OracleSolver(prob)
+        rep = bench.Replicas(WORLD, reduce_device="cpu")
+
+        def clock():
+            t0 = time.perf_counter()
+            return lambda: (time.perf_counter() - t0) * 1e3
+        ms = rep.timed(solver.step, STEPS, 1, clock)
+        ms_max = rep.maxr(ms)
         n = torch.tensor([int(prob["B"])], dtype=torch.int64)
         dist.all_reduce(n)
-        np.savez(os.path.join(out, f"rank{rank}.npz"), x=xs[-1], ms=ms, ms_max=float(t.item()),
-                 scenes=int(prob["B"]), scenes_all=int(n.item()),
-                 value=int(prob["B"]) * STEPS * WORLD / (float(t.item()) / 1e3))
+        np.savez(os.path.join(out, f"rank{rank}.npz"), x=solver.x, ms=ms, ms_max=ms_max,
+                 scenes=int(prob["B"]), scenes_all=int(n.item()), value=rep.value(int(prob["B"]), STEPS, ms_max))
     finally:
         dist.destroy_process_group()
 
@@ -66,5 +70,6 @@ def test_replicas_share_nothing_but_the_clock():
         assert int(r[k]["scenes"]) == SCENES and int(r[k]["scenes_all"]) == WORLD * SCENES
         assert float(r[k]["ms_max"]) == max(float(q["ms"]) for q in r)
         assert float(r[k]["value"]) == float(r[0]["value"])
-        _, xs, _ = oracle.run(_batch(k), STEPS)
+        _, xs, _ = oracle.run(_batch(k), STEPS + 1)       # one warm-up step and the timed ones
         assert np.array_equal(r[k]["x"], xs[-1]), k
+        assert float(r[k]["value"]) == SCENES * STEPS * WORLD / (float(r[k]["ms_max"]) / 1e3)
