@@ -212,60 +212,118 @@ def run_reference(args, rank, world):
 
 
 # ----------------------------------------------------------------------------- gradients
-def measure_grads(args, dev):
-    """grads/s of the differentiation workload: a batch of tendon-driven arms, the loss
-    sum_b |x_tip,b - target_b|^2 after `grad_steps` steps, its gradient with respect to every
-    element's modulus (per pixel: 1024 values an arm) and every step's tendon tension, by the
-    checkpointed adjoint (checkpoints every 10 steps, replay in between). One gradient = one
-    forward rollout + its backward pass, timed with CUDA events after one short warm-up
-    rollout; grads/s = arms x gradients / time. The forward steps and their replay run in
-    mixed precision, the adjoint solves in FP64 at those states."""
+def _grads_at(args, dev, arms, max_iter=None, eps=None, fd_entries=32, h=1e-3, stencil=2, warm=True):
+    """One gradient of the differentiation workload (`arms` tendon-driven arms, the loss
+    sum_b |x_tip,b - target_b|^2 after `grad_steps` steps) by the checkpointed adjoint
+    (checkpoints every 10 steps), timed with CUDA events (after a short warm-up rollout when
+    `warm`), and its accuracy at the same settings: `fd_entries` entries (3/4 pixel moduli,
+    1/4 step tensions), each in its own arm, perturbed relative by +/- h (stencil 2: central
+    differences) or also +/- 2h (stencil 4: (8 (L(h) - L(-h)) - (L(2h) - L(-2h))) / 12h, error
+    O(h^4)) in more rollouts of the whole batch (arms are independent), against the adjoint
+    gradient, relative to the entry or to 1 % of the largest checked entry for smaller ones.
+    The forward steps and their replay run in mixed precision, the adjoint solves in FP64 at
+    those states. max_iter / eps: the forward's iteration budget and energy-decrease
+    tolerance (None: the reference's CFL budget and 1e-10)."""
     import torch
     from diff_2d_fem_gb300 import workloads, ImplicitIntegrator
     from diff_2d_fem_gb300.adjoint import Rollout
     T = args.grad_steps
-    m, kw, dt, ex = workloads.tendon_arms(args.arms, seed=0, steps=T)
-    integ = ImplicitIntegrator(**kw)
+    m, kw, dt, ex = workloads.tendon_arms(arms, seed=0, steps=T)
+    integ = ImplicitIntegrator(**kw, max_iter=max_iter, eps=eps)
     s = integ.attach(m, dt)
-    B, nt = args.arms, int(s.desc.T)
+    nt = int(s.desc.T)
     x0 = s.x.detach().clone()
     tip = torch.as_tensor(ex["tip"], device=dev)
     tgt = torch.as_tensor(ex["target"], device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def grad_once(steps, ckpt):
+    def rollout(steps, ckpt, E, ten, grad):
         ro = Rollout(s, steps=steps, record=[steps], checkpoint_every=ckpt, rtol=1e-9, max_iter=20000,
                      forward_precision="mixed")
-        E = torch.ones(nt, dtype=torch.float64, device=dev, requires_grad=True)
-        ten = torch.as_tensor(ex["tension"][:steps], device=dev).clone().requires_grad_(True)
-        v0 = torch.zeros_like(x0)
+        Et = torch.as_tensor(E, device=dev).clone().requires_grad_(grad)
+        Tt = torch.as_tensor(ten, device=dev).clone().requires_grad_(grad)
         e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         e0.record(stream)
-        out = ro(E, ten, x0, v0)
+        out = ro(Et, Tt, x0, torch.zeros_like(x0))
         e1.record(stream)
-        loss = ((out[0][tip] - tgt) ** 2).sum()
-        loss.backward()
+        per_arm = ((out[0][tip] - tgt) ** 2).sum(dim=1)
+        if grad:
+            per_arm.sum().backward()
         e2.record(stream)
         torch.cuda.synchronize(dev)
         ro.close()
-        return ro, E.grad, ten.grad, e0.elapsed_time(e1), e1.elapsed_time(e2), float(loss.item())
+        return ro, Et.grad, Tt.grad, e0.elapsed_time(e1), e1.elapsed_time(e2), per_arm.detach().cpu().numpy()
 
-    grad_once(2, 1)                                           # warm-up: buffers, launch paths
-    ro, gE, gT, f_ms, b_ms, loss = grad_once(T, 10)
-    its = ro.info["adjoint_total_iters"]
-    return {"value": B / ((f_ms + b_ms) / 1e3), "unit": "grads/s",
-            "workload": f"tendon_arms x{B} (16x64 px of 0.5 mm, E log-U[0.2,1.5] MPa per pixel, "
+    ones, ten0 = np.ones(nt), np.asarray(ex["tension"][:T], np.float64)
+    if warm:
+        rollout(2, 1, ones, ten0[:2], True)                   # warm-up: buffers, launch paths
+    ro, gE, gT, f_ms, b_ms, L = rollout(T, 10, ones, ten0, True)
+    info = dict(ro.info)
+    # the checked entries, one per arm
+    rng = np.random.default_rng(7)
+    quad = np.asarray(m.me.tri_quad)
+    n_fd = min(fd_entries, arms)
+    n_pix = (3 * n_fd) // 4
+    gE_, gT_ = gE.cpu().numpy(), gT.cpu().numpy()
+    sel_e, sel_t, adj = {}, {}, []
+    for i in range(n_fd):
+        if i < n_pix:
+            el = m.body_elements(ex["handles"][i])
+            sel_e[i] = el[quad[el] == rng.choice(np.unique(quad[el]))]
+            adj.append(gE_[sel_e[i]].sum())
+        else:
+            sel_t[i] = int(rng.integers(T))
+            adj.append(gT_[sel_t[i], i] * ten0[sel_t[i], i])
+    adj = np.asarray(adj)
+
+    def perturbed_loss(c):                                   # every checked entry scaled by (1 + c)
+        E, ten = ones.copy(), ten0.copy()
+        for i, el in sel_e.items():
+            E[el] = 1.0 + c
+        for i, k in sel_t.items():
+            ten[k, i] = ten0[k, i] * (1.0 + c)
+        return rollout(T, 10, E, ten, False)[-1][:n_fd]
+
+    if stencil == 4:
+        fd = (8.0 * (perturbed_loss(h) - perturbed_loss(-h)) - (perturbed_loss(2 * h) - perturbed_loss(-2 * h))) / (12 * h)
+    else:
+        fd = (perturbed_loss(h) - perturbed_loss(-h)) / (2 * h)
+    err = np.abs(fd - adj) / np.maximum(np.abs(adj), 1e-2 * np.abs(adj).max())
+    its = info["adjoint_total_iters"]
+    unconv = int(info["forward_unconverged_steps"].sum())
+    return {"value": arms / ((f_ms + b_ms) / 1e3), "unit": "grads/s",
+            "workload": f"tendon_arms x{arms} (16x64 px of 0.5 mm, E log-U[0.2,1.5] MPa per pixel, "
                         f"tendon on node row 2, piecewise-linear tension in [0,50] N/m), {T} steps, dt {dt}",
-            "gradient": f"dL/dE per element ({nt // B} per arm) and dL/dtension per step; "
+            "forward_budget": {"iter_max": int(s.iter_max), "eps": float(integ.eps)},
+            "gradient": f"dL/dE per element ({nt // arms} per arm) and dL/dtension per step; "
                         "checkpoints every 10 steps",
             "dtype": "forward and replay mixed-f32/f64, adjoint CG f64",
             "ms_per_grad_batch": f_ms + b_ms, "forward_ms": f_ms, "backward_ms": b_ms,
             "adjoint_cg_iters_per_solve_mean": float(its.mean() / T),
-            "adjoint_worst_status": int(np.abs(ro.info["adjoint_worst_status"]).max()),
-            "forward_unconverged_scene_steps": int(ro.info["forward_unconverged_steps"].sum()),
-            "replay_mismatch": ro.info["replay_mismatch"],
-            "grad_finite": bool(torch.isfinite(gE).all().item() and torch.isfinite(gT).all().item()),
-            "loss": loss}
+            "adjoint_worst_status": int(np.abs(info["adjoint_worst_status"]).max()),
+            "forward_unconverged_scene_steps": unconv, "forward_scene_steps": int(arms * T),
+            "forward_unconverged_fraction": unconv / float(arms * T),
+            "replay_mismatch": info["replay_mismatch"],
+            "grad_err_vs_fd": {"max": float(err.max()), "median": float(np.median(err)), "entries": int(n_fd),
+                               "h_rel": h, "stencil": stencil, "pixel_moduli": int(n_pix),
+                               "step_tensions": int(n_fd - n_pix)},
+            "grad_finite": bool(np.isfinite(gE_).all() and np.isfinite(gT_).all()),
+            "loss": float(L.sum())}
+
+
+def measure_grads(args, dev):
+    """grads/s of the differentiation workload with the accuracy of its gradient stated at
+    the same settings. The headline runs every forward step to convergence (iteration budget
+    --grad-iters, energy-decrease tolerance 1e-13): the adjoint differentiates the converged
+    step (the implicit-function argument), so its gradient is the forward map's. The checked
+    entries use a 4-point stencil at h = 1e-2: the mixed forward repeats itself only to FP32
+    rounding of its atomic sums (~3e-9 of the positions), which central differences at
+    h = 1e-3 amplify past 1e-4 on the smallest entries. `at_reference_budget`: the same at
+    the reference's CFL iteration budget, where the forward steps stop at the cap before
+    converging and the gradient is not the truncated forward map's."""
+    out = _grads_at(args, dev, args.arms, max_iter=args.grad_iters, eps=1e-13, h=1e-2, stencil=4)
+    out["at_reference_budget"] = _grads_at(args, dev, args.arms, warm=False)
+    return out
 
 
 def measure_single_strip(args, dev):
@@ -689,6 +747,8 @@ def main():
     ap.add_argument("--tune-sample", type=int, default=1024)
     ap.add_argument("--arms", type=int, default=256, help="differentiation workload: arms per batch")
     ap.add_argument("--grad-steps", type=int, default=100, help="differentiation workload: steps")
+    ap.add_argument("--grad-iters", type=int, default=3000,
+                    help="differentiation workload: forward iteration budget (steps stop on the energy test)")
     ap.add_argument("--no-grads", action="store_true", help="skip the grads/s measurement")
     ap.add_argument("--no-large", action="store_true", help="skip the large-scene measurement")
     ap.add_argument("--large-steps", type=int, default=3, help="large-scene workload: timed steps")

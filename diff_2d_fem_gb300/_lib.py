@@ -13,7 +13,7 @@ _I = C.c_int32
 _D = C.c_double
 _P = C.c_void_p
 
-D2F_ABI_VERSION = 6
+D2F_ABI_VERSION = 7
 D2F_FP64, D2F_MIXED = 0, 1
 ERRORS = {0: "ok", -1: "D2F_EINVAL", -2: "D2F_ECUDA", -3: "D2F_ECAP", -4: "D2F_ENAN"}
 
@@ -54,7 +54,7 @@ class SceneDesc(C.Structure):
 
 EXPORTS = ("d2f_abi_version", "d2f_create", "d2f_step", "d2f_set_dt", "d2f_stats", "d2f_destroy",
            "d2f_last_error", "d2f_kernels_per_step", "d2f_step_noalloc", "d2f_mixed_scratch_bytes",
-           "d2f_adjoint_solve", "d2f_adjoint_vjp", "d2f_launch_shape",
+           "d2f_adjoint_solve", "d2f_adjoint_vjp", "d2f_adjoint_work_doubles", "d2f_launch_shape",
            "d2f_element_fields", "d2f_adjoint_vjp_pressure", "d2f_contact_force", "d2f_energy")
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
@@ -106,6 +106,8 @@ def load(build_if_missing: bool = True):
     L.d2f_adjoint_solve.restype = _I
     L.d2f_adjoint_vjp.argtypes = [_P, _P, _P, _P, _P, _P]
     L.d2f_adjoint_vjp.restype = _I
+    L.d2f_adjoint_work_doubles.argtypes = [_P]
+    L.d2f_adjoint_work_doubles.restype = C.c_int64
     if L.d2f_abi_version() != D2F_ABI_VERSION:
         raise RuntimeError("libd2f.so ABI version mismatch; rebuild it")
     _LIB = L

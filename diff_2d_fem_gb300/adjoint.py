@@ -24,10 +24,13 @@ Two layers:
 
   which follows from the predictor xhat_{k+1} = x_k + h drag v_k, v_k = (x_k - x_{k-1}) / h.
 
-The operator H_k = M + h^2 (K_elastic + K_collider + K_tendon) has the collider contact gate
-frozen at x_k, as the reference's; like the reference it leaves out friction, and it refuses
-IPC contact between bodies and affine bodies (no tangent for them, implicit/adjoint.py:376-385).
-The tendon tangent (tension-controlled cables) is beyond the reference, which refuses tendons.
+The operator H_k = M + h^2 (K_elastic + K_collider + K_tendon + K_spring + K_pressure + K_ipc)
+has the collider contact gate frozen at x_k, as the reference's; like the reference it leaves
+out friction. Beyond the reference, which refuses them (implicit/adjoint.py:372-385): the
+tangent of IPC contact between bodies (the barrier terms active at x_k, frozen, each
+distance's exact Hessian), affine bodies in their reduced coordinates (x = J q on a body's
+nodes, the body's exact elastic block; the solution on its nodes is J lam_q), and tendons
+(tension-controlled cables).
 """
 from __future__ import annotations
 
@@ -49,12 +52,6 @@ def _solver_of(obj):
         raise RuntimeError("the model has no solver yet: run simulate() once first")
     if s.mixed:
         raise ValueError("the adjoint needs an FP64 solver (ImplicitIntegrator(precision='fp64'))")
-    if s.desc.Ne > 0:
-        raise NotImplementedError(
-            "the adjoint operator has no tangent for IPC contact between bodies: use "
-            "ImplicitIntegrator(self_collision=False)")
-    if s.desc.n_aff > 0:
-        raise NotImplementedError("the adjoint operator has no tangent for affine bodies")
     _refuse_actuators(False, False, bool(s.prob.get("active_regions", 0)))
     return s
 
@@ -89,7 +86,7 @@ class AdjointPNCG2D:
         fm = s.tensor("free_mask").to(torch.int32)
         self.free = torch.stack([(fm & 1) > 0, (fm & 2) > 0], 1).to(torch.float64)
         self.mass = s.tensor("mass")
-        self._work = torch.empty(10 * self.N, dtype=torch.float64, device=self.dev)
+        self._work = torch.empty(int(s.L.d2f_adjoint_work_doubles(s.h)), dtype=torch.float64, device=self.dev)
         self.iters = torch.zeros(self.B, dtype=torch.int32, device=self.dev)
         self.status = torch.zeros(self.B, dtype=torch.int32, device=self.dev)
         self.worst_status = torch.zeros(self.B, dtype=torch.int32, device=self.dev)

@@ -17,6 +17,7 @@
 
 #include "d2f_math.cuh"
 #include "d2f_solver.h"
+#include "pncg_kernel.cuh"
 
 namespace d2f {
 namespace adj {
@@ -76,6 +77,156 @@ __device__ __forceinline__ void collider_hessian(const double *cd, int kind, dou
     h11 = kappa * (bpp * ny * ny + bp * H11);
 }
 
+// ---- contact between bodies (IPC), frictionless, active set frozen at x (ipc_pair_kernel
+// terms, implicit/ipc_contact.py:174-296; the reference's adjoint refuses IPC)
+// Index of (i, j), i <= j, in the upper triangle of a symmetric 6x6 stored row by row.
+__device__ __forceinline__ int ut6(int i, int j) { return 6 * i - (i * (i - 1)) / 2 + (j - i); }
+
+// The directional second derivative of the point-line distance |cross(ab, w)| / |ab| along
+// v = (v_p, v_a, v_b): the same quadratic form in v as the step's curvature pass uses.
+__device__ __forceinline__ double line_ddd(double abx, double aby, double wx, double wy, double Ll, double c0,
+                                           const double *v) {
+    const double dex = v[4] - v[2], dey = v[5] - v[3], dwx = v[0] - v[2], dwy = v[1] - v[3];
+    const double c1 = (dex * wy - dey * wx) + (abx * dwy - aby * dwx);
+    const double c2 = 2.0 * (dex * dwy - dey * dwx);
+    const double L1 = (abx * dex + aby * dey) / Ll;
+    const double Lq = ((dex * dex + dey * dey) - L1 * L1) / Ll;
+    const double s0 = c0 / Ll, s1 = (c1 - s0 * L1) / Ll;
+    const double ddd = (c2 - 2.0 * s1 * L1 - s0 * Lq) / Ll;
+    return c0 < 0.0 ? -ddd : ddd;
+}
+
+// kappa (b''(d) g g^T + b'(d) grad^2 d) of one point-point term (the distance between the
+// point and node `o` = 1 (a) or 2 (b)), times coef, added to the pair's block H.
+__device__ __forceinline__ void point_block(double coef, double wx, double wy, double dist, double dhat, double kappa,
+                                            int o, double *H) {
+    const double nx = wx / dist, ny = wy / dist;
+    const double bp = barrier_bp<double>(dist, dhat), bpp = barrier_bpp<double>(dist, dhat);
+    const double K[2][2] = {{(1.0 - nx * nx) / dist, -nx * ny / dist}, {-nx * ny / dist, (1.0 - ny * ny) / dist}};
+    const double n[2] = {nx, ny};
+    const int dof[4] = {0, 1, 2 * o, 2 * o + 1};
+    for (int r = 0; r < 4; ++r)
+        for (int c = r; c < 4; ++c) {
+            const double sr = r < 2 ? 1.0 : -1.0, sc = c < 2 ? 1.0 : -1.0;
+            const double gg = sr * n[r & 1] * sc * n[c & 1];
+            const double hd = sr * sc * K[r & 1][c & 1];
+            H[ut6(dof[r], dof[c])] += coef * kappa * (bpp * gg + bp * hd);
+        }
+}
+
+// Every barrier term of the node-edge pair (p, edge ge = (a, b)) at x, frozen: the edge
+// interior with weights (1 - t, t), and each end with its vertex-correction coefficient, as
+// the step evaluates them; the exact Hessian of each distance (the interior's by
+// polarisation of its directional second derivative). H: the 6x6 over (p, a, b), upper
+// triangle, kappa-scaled (no h^2). False when no term is active.
+__device__ __noinline__ bool pair_block(const d2f_scene_desc &d, int ge, double2 xp, double2 xa, double2 xb, double *H) {
+    const double dhat = d.ipc_dhat, kappa = d.ipc_kappa, dlo = 1.0e-9 * dhat;
+    const double abx = xb.x - xa.x, aby = xb.y - xa.y;
+    const double L2 = dmax(abx * abx + aby * aby, 1.0e-30), Ll = sqrt(L2);
+    const double wx = xp.x - xa.x, wy = xp.y - xa.y;
+    const double tt = (wx * abx + wy * aby) / L2;
+    double dvx = wx - tt * abx, dvy = wy - tt * aby;
+    if (tt <= 0.0) { dvx = wx; dvy = wy; }
+    else if (tt >= 1.0) { dvx = xp.x - xb.x; dvy = xp.y - xb.y; }
+    const double dd0 = sqrt(dvx * dvx + dvy * dvy);
+    if (!(dd0 < d.reach)) return false;
+    for (int q = 0; q < 21; ++q) H[q] = 0.0;
+    bool any = false;
+    if (tt > 0.0 && tt < 1.0 && dd0 < dhat) {
+        const double dd = dmax(dd0, dlo), nx = dvx / dd, ny = dvy / dd;
+        const double g[6] = {nx, ny, -(1.0 - tt) * nx, -(1.0 - tt) * ny, -tt * nx, -tt * ny};
+        const double c0 = abx * wy - aby * wx;
+        const double bp = barrier_bp<double>(dd, dhat), bpp = barrier_bpp<double>(dd, dhat);
+        double q[6], v[6];
+        for (int i = 0; i < 6; ++i) {
+            for (int k = 0; k < 6; ++k) v[k] = k == i ? 1.0 : 0.0;
+            q[i] = line_ddd(abx, aby, wx, wy, Ll, c0, v);
+        }
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j) {
+                double hd = q[i];
+                if (j != i) {
+                    for (int k = 0; k < 6; ++k) v[k] = (k == i || k == j) ? 1.0 : 0.0;
+                    hd = 0.5 * (line_ddd(abx, aby, wx, wy, Ll, c0, v) - q[i] - q[j]);
+                }
+                H[ut6(i, j)] += kappa * (bpp * g[i] * g[j] + bp * hd);
+            }
+        any = true;
+    }
+    double coef_a = -d.ca[ge];
+    if (tt <= 0.0) coef_a += 1.0;
+    const double d_a = sqrt(wx * wx + wy * wy);
+    if (coef_a != 0.0 && d_a < dhat) {
+        point_block(coef_a, wx, wy, dmax(d_a, dlo), dhat, kappa, 1, H);
+        any = true;
+    }
+    double coef_b = -d.cb[ge];
+    if (tt >= 1.0) coef_b += 1.0;
+    const double wbx = xp.x - xb.x, wby = xp.y - xb.y, d_b = sqrt(wbx * wbx + wby * wby);
+    if (coef_b != 0.0 && d_b < dhat) {
+        point_block(coef_b, wbx, wby, dmax(d_b, dlo), dhat, kappa, 2, H);
+        any = true;
+    }
+    return any;
+}
+
+// ---- affine bodies (AffineBodies, implicit/affine.py:60-101, 156-269; the reference's
+// adjoint refuses them): the system in the reduced coordinates, S^T H S + h^2 K_A with
+// x = J q on a body's nodes (J = [w^T 0; 0 w^T], q = (t_x, A11, A12, t_y, A21, A22)) and K_A
+// the body's exact elastic block at its A. Per body, QW doubles of the work buffer:
+constexpr int QW = 112;
+constexpr int Q_R = 0, Q_Z = 6, Q_P = 12, Q_AP = 18, Q_L = 24, Q_W = 30, Q_K = 36, Q_PI = 72;
+// R, Z, P, AP, lam (6 each) of the CG; W = sum w w^T (00 01 02 11 12 22); K = h^2 K_A (6x6);
+// PI = the inverse of the body's block preconditioner sum J^T diag(D) J + h^2 K_A (6x6).
+
+// 3x3 symmetric solve by the adjugate (W from the node weights of one body: well conditioned)
+__device__ __forceinline__ void sym3_solve(const double *W, const double *b, double *x) {
+    const double a00 = W[0], a01 = W[1], a02 = W[2], a11 = W[3], a12 = W[4], a22 = W[5];
+    const double c00 = a11 * a22 - a12 * a12, c01 = a02 * a12 - a01 * a22, c02 = a01 * a12 - a02 * a11;
+    const double c11 = a00 * a22 - a02 * a02, c12 = a01 * a02 - a00 * a12, c22 = a00 * a11 - a01 * a01;
+    const double det = a00 * c00 + a01 * c01 + a02 * c02, r = det != 0.0 ? 1.0 / det : 0.0;
+    x[0] = (c00 * b[0] + c01 * b[1] + c02 * b[2]) * r;
+    x[1] = (c01 * b[0] + c11 * b[1] + c12 * b[2]) * r;
+    x[2] = (c02 * b[0] + c12 * b[1] + c22 * b[2]) * r;
+}
+
+// One body's setup from its node sums v (24: W = sum w w^T, sum D_x w w^T, sum D_y w w^T
+// (6 each, 00 01 02 11 12 22), sum w x, sum w y (3 each)) and, warm, lw = sum w lam (6):
+// W, h^2 K_A at the body's A, the inverse of its block preconditioner, lam_q and p_q. Out of
+// line: its local 6x6 arrays would otherwise sit in every thread's frame of the CG kernel.
+__device__ __noinline__ void affine_setup(double *qb, const double *v, const double *lw, int warm, double Mu,
+                                          double La, double h2) {
+    for (int q = 0; q < 6; ++q) qb[Q_W + q] = v[q];
+    double qx[3], qy[3];
+    sym3_solve(v, v + 18, qx);
+    sym3_solve(v, v + 21, qy);
+    const M2 A{qx[1], qx[2], qy[1], qy[2]};
+    for (int q = 0; q < 36; ++q) qb[Q_K + q] = 0.0;
+    const int idx[4] = {1, 2, 4, 5};
+    for (int k = 0; k < 4; ++k) {
+        const M2 E{k == 0 ? 1.0 : 0.0, k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0, k == 3 ? 1.0 : 0.0};
+        const M2 col = nh_d2(A, E, Mu, La);
+        const double cv[4] = {col.a, col.b, col.c, col.d};
+        for (int r = 0; r < 4; ++r) qb[Q_K + 6 * idx[r] + idx[k]] = h2 * cv[r];
+    }
+    // the block preconditioner: Cholesky of the projected reduced Hessian, its inverse
+    double H6[6][6], L6[6][6];
+    reduced_hessian(A, Mu, La, h2, v + 6, H6);
+    chol6(H6, L6);
+    for (int c = 0; c < 6; ++c) {
+        double e[6], xcol[6];
+        for (int q = 0; q < 6; ++q) e[q] = q == c ? 1.0 : 0.0;
+        chol6_solve(L6, e, xcol);
+        for (int r = 0; r < 6; ++r) qb[Q_PI + 6 * r + c] = xcol[r];
+    }
+    double lx[3] = {0.0, 0.0, 0.0}, ly[3] = {0.0, 0.0, 0.0};
+    if (warm) { sym3_solve(v, lw, lx); sym3_solve(v, lw + 3, ly); }
+    for (int q = 0; q < 3; ++q) {
+        qb[Q_L + q] = lx[q]; qb[Q_L + 3 + q] = ly[q];
+        qb[Q_P + q] = lx[q]; qb[Q_P + 3 + q] = ly[q];
+    }
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_scene_desc d, const double *__restrict__ xl,
                                                  const double *__restrict__ rhs, double *__restrict__ lam,
@@ -85,9 +236,9 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
     constexpr int NW = NT / 32;
     __shared__ double red[NW * 4 + 4];
     __shared__ double s_col[MAXC][8];
-    __shared__ int sc_next, s_stop, s_status;
+    __shared__ int sc_next, s_stop, s_status, s_npair;
     __shared__ double s_alpha, s_beta, s_rz;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const double h2 = d.dt * d.dt;
     const int N = d.N;
     const double2 *__restrict__ XL = reinterpret_cast<const double2 *>(xl);
@@ -98,6 +249,9 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
     double2 *__restrict__ P = R + 2 * N;
     double2 *__restrict__ AP = R + 3 * N;
     double2 *__restrict__ DI = R + 4 * N;
+    double2 *__restrict__ EX = R + 5 * N;                       // P with the affine nodes' J p_q
+    double *__restrict__ PB = work + 12 * (size_t)N;            // IPC pair blocks, 24 a candidate slot
+    double *__restrict__ QB = PB + 24 * (size_t)d.cand_total;   // affine bodies, QW each
     const double4_32a *__restrict__ Bm = reinterpret_cast<const double4_32a *>(d.Bm);
     const double *__restrict__ Ar = reinterpret_cast<const double *>(d.area);
     const double *__restrict__ Mu = reinterpret_cast<const double *>(d.mu);
@@ -115,8 +269,18 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
         if (sc >= d.n_scenes) break;
         const d2f_seg sg = d.segs[sc];
         const int n0 = sg.node0, n1 = sg.node0 + sg.nn, t0 = sg.tri0, t1 = sg.tri0 + sg.nt;
+        const bool has_aff = sg.naff > 0, has_ipc = d.Ne > 0 && sg.ne > 0;
+        // a DOF of the CG on the nodes: free and not slaved to an affine body
+        auto plain = [&](int i, uint8_t fm, int c) -> bool { return (fm & (1 << c)) && d.node_aff[i] < 0; };
+        auto J_of = [&](int i, double &w0, double &w1, double &w2) -> double * {
+            const int ka = d.node_aff[i];
+            const double *w = d.a_w + 3 * ka;
+            w0 = w[0]; w1 = w[1]; w2 = w[2];
+            return QB + (size_t)QW * d.a_grp[ka];
+        };
 
-        // AP = (M + h^2 (K_elastic + K_collider + K_tendon)) V for this scene, all DOFs
+        // AP = (M + h^2 (K_elastic + K_collider + K_tendon + K_spring + K_pressure + K_ipc)) V
+        // for this scene, all DOFs
         auto hvp = [&](const double2 *__restrict__ V) {
             // element pass: corner shares of h^2 K_elastic V (hvp_elastic_kernel, implicit/adjoint.py:69-84)
             for (int t = t0 + tid; t < t1; t += NT) {
@@ -218,6 +382,57 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                 }
                 block_barrier();
             }
+            if (has_ipc) {  // the frozen pair blocks, h^2 H_pair V
+                const int np = s_npair < sg.ncap ? s_npair : sg.ncap;
+                for (int c = tid; c < np; c += NT) {
+                    const double *pb = PB + 24 * (size_t)(sg.cand0 + c);
+                    const int ids[3] = {(int)pb[21], (int)pb[22], (int)pb[23]};
+                    double v[6], o[6];
+                    for (int q = 0; q < 3; ++q) { v[2 * q] = V[ids[q]].x; v[2 * q + 1] = V[ids[q]].y; }
+                    for (int r = 0; r < 6; ++r) {
+                        double acc = 0.0;
+                        for (int q = 0; q < 6; ++q) acc += pb[r <= q ? ut6(r, q) : ut6(q, r)] * v[q];
+                        o[r] = h2 * acc;
+                    }
+                    for (int q = 0; q < 3; ++q) { atomicAdd(&AP[ids[q]].x, o[2 * q]); atomicAdd(&AP[ids[q]].y, o[2 * q + 1]); }
+                }
+                block_barrier();
+            }
+        };
+        // the affine bodies' share of a product: AP_q = sum J^T AP (a warp per body, fixed
+        // shuffle tree) + h^2 K_A p_q
+        auto gather_q = [&]() {
+            for (int b = sg.aff0 + warp; b < sg.aff0 + sg.naff; b += NW) {
+                double *qb = QB + (size_t)QW * b;
+                double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+                for (int k = d.a_ptr[b] + lane; k < d.a_ptr[b + 1]; k += 32) {
+                    const int i = d.a_node[k];
+                    const double *w = d.a_w + 3 * k;
+                    const double2 a = AP[i];
+                    v[0] += w[0] * a.x; v[1] += w[1] * a.x; v[2] += w[2] * a.x;
+                    v[3] += w[0] * a.y; v[4] += w[1] * a.y; v[5] += w[2] * a.y;
+                }
+                for (int q = 0; q < 6; ++q) v[q] = wsum(v[q]);
+                if (lane < 6) {
+                    double kp = 0.0;
+                    for (int q = 0; q < 6; ++q) kp += qb[Q_K + 6 * lane + q] * qb[Q_P + q];
+                    double vv = v[0];
+                    for (int q = 1; q < 6; ++q) if (lane == q) vv = v[q];
+                    qb[Q_AP + lane] = vv + kp;
+                }
+            }
+            block_barrier();
+        };
+        // EX = P on the plain nodes, J p_q on the affine ones
+        auto expand = [&](const double2 *__restrict__ V, int qoff) {
+            for (int i = n0 + tid; i < n1; i += NT) {
+                if (d.node_aff[i] < 0) { EX[i] = V[i]; continue; }
+                double w0, w1, w2;
+                const double *qb = J_of(i, w0, w1, w2);
+                const double *q = qb + qoff;
+                EX[i] = make_double2(w0 * q[0] + w1 * q[1] + w2 * q[2], w0 * q[3] + w1 * q[4] + w2 * q[5]);
+            }
+            block_barrier();
         };
 
         // ---- tangent at x_lin: F^-T and (la log J - mu) per triangle, the Jacobi diagonal per corner
@@ -242,8 +457,28 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                 Esc[3 * t + c] = make_double4_32a(0.0, 0.0, hA * dmax(bb + kk * gx * gx, 0.0), hA * dmax(bb + kk * gy * gy, 0.0));
             }
         }
-        if (tid == 0) { s_stop = 0; s_status = 0; }
+        if (tid == 0) { s_stop = 0; s_status = 0; s_npair = 0; }
         block_barrier();
+        // ---- the frozen IPC pair blocks at x_lin: every node-edge pair of the scene tested
+        if (has_ipc) {
+            const int nbs = sg.nb;
+            const long npairs = (long)sg.ne * nbs;
+            for (long c = tid; c < npairs; c += NT) {
+                const int k = (int)(c / nbs), j = (int)(c % nbs);
+                const int ge = sg.edge0 + k, a = d.ea[ge], b = d.eb[ge], pn = d.bnd[sg.bnd0 + j];
+                if (pn == a || pn == b) continue;
+                if (excluded(d, sg.bnd0 + j, d.ela[ge]) || excluded(d, sg.bnd0 + j, d.elb[ge])) continue;
+                double H[21];
+                if (!pair_block(d, ge, XL[pn], XL[a], XL[b], H)) continue;
+                const int slot = atomicAdd(&s_npair, 1);
+                if (slot >= sg.ncap) continue;
+                double *pb = PB + 24 * (size_t)(sg.cand0 + slot);
+                for (int q = 0; q < 21; ++q) pb[q] = H[q];
+                pb[21] = pn; pb[22] = a; pb[23] = b;
+            }
+            block_barrier();
+            if (tid == 0 && s_npair > sg.ncap) { s_stop = 1; s_status = D2F_ECAP; }
+        }
         // ---- the Jacobi preconditioner; the initial guess (0, or lam as given with warm)
         for (int i = n0 + tid; i < n1; i += NT) {
             const double m = d.mass[i];
@@ -272,35 +507,113 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
             atomicAdd(&DI[a].x, hx); atomicAdd(&DI[a].y, hy);
             if (b >= 0) { atomicAdd(&DI[b].x, hx); atomicAdd(&DI[b].y, hy); }
         }
+        if (has_ipc) {  // the pair blocks' diagonals, clamped
+            const int np = s_npair < sg.ncap ? s_npair : sg.ncap;
+            for (int c = tid; c < np; c += NT) {
+                const double *pb = PB + 24 * (size_t)(sg.cand0 + c);
+                for (int q = 0; q < 3; ++q) {
+                    const int n = (int)pb[21 + q];
+                    atomicAdd(&DI[n].x, h2 * dmax(pb[ut6(2 * q, 2 * q)], 0.0));
+                    atomicAdd(&DI[n].y, h2 * dmax(pb[ut6(2 * q + 1, 2 * q + 1)], 0.0));
+                }
+            }
+        }
         block_barrier();
+        if (has_aff) {
+            // per body: its A from x_lin (least squares over its nodes: x = J q holds there), the
+            // exact block h^2 K_A, and the inverse of the block preconditioner sum J^T D J +
+            // h^2 K_A (the forward's reduced Hessian, projected SPD, by Cholesky); the initial
+            // lam_q from lam on its nodes (warm) or 0
+            for (int b = sg.aff0 + warp; b < sg.aff0 + sg.naff; b += NW) {
+                double v[24];
+                for (int q = 0; q < 24; ++q) v[q] = 0.0;
+                for (int k = d.a_ptr[b] + lane; k < d.a_ptr[b + 1]; k += 32) {
+                    const int i = d.a_node[k];
+                    const double *w = d.a_w + 3 * k;
+                    const double2 x = XL[i], dg = DI[i];
+                    const double o[6] = {w[0] * w[0], w[0] * w[1], w[0] * w[2], w[1] * w[1], w[1] * w[2], w[2] * w[2]};
+                    for (int q = 0; q < 6; ++q) { v[q] += o[q]; v[6 + q] += dg.x * o[q]; v[12 + q] += dg.y * o[q]; }
+                    for (int q = 0; q < 3; ++q) { v[18 + q] += w[q] * x.x; v[21 + q] += w[q] * x.y; }
+                }
+                for (int q = 0; q < 24; ++q) v[q] = wsum(v[q]);
+                double lw[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+                if (warm) {
+                    for (int k = d.a_ptr[b] + lane; k < d.a_ptr[b + 1]; k += 32) {
+                        const double *w = d.a_w + 3 * k;
+                        const double2 l = LAM[d.a_node[k]];
+                        for (int q = 0; q < 3; ++q) { lw[q] += w[q] * l.x; lw[3 + q] += w[q] * l.y; }
+                    }
+                    for (int q = 0; q < 6; ++q) lw[q] = wsum(lw[q]);
+                }
+                if (lane == 0) affine_setup(QB + (size_t)QW * b, v, lw, warm, d.a_Mu[b], d.a_La[b], h2);
+                __syncwarp();
+            }
+            block_barrier();
+        }
         for (int i = n0 + tid; i < n1; i += NT) {
             const uint8_t fm = d.free_mask[i];
             const double2 dd = DI[i];
-            DI[i] = make_double2((fm & 1) ? 1.0 / dd.x : 0.0, (fm & 2) ? 1.0 / dd.y : 0.0);
+            DI[i] = make_double2(plain(i, fm, 0) ? 1.0 / dd.x : 0.0, plain(i, fm, 1) ? 1.0 / dd.y : 0.0);
             double2 l0 = make_double2(0.0, 0.0);
             if (warm) {
                 const double2 l = LAM[i];
-                l0 = make_double2((fm & 1) ? l.x : 0.0, (fm & 2) ? l.y : 0.0);
+                l0 = make_double2(plain(i, fm, 0) ? l.x : 0.0, plain(i, fm, 1) ? l.y : 0.0);
             }
             LAM[i] = l0;
             P[i] = l0;
         }
         block_barrier();
-        if (warm) hvp(P);  // A lam0
-        // r = b - A lam0 on the free DOFs, z = D^-1 r, p = z
+        if (warm) {  // A lam0
+            if (has_aff) expand(P, Q_P);
+            hvp(has_aff ? EX : P);
+            if (has_aff) gather_q();
+        }
+        // r = b - A lam0 on the plain DOFs and the bodies' coordinates, z = D^-1 r, p = z
         double acc[3] = {0.0, 0.0, 0.0};
         for (int i = n0 + tid; i < n1; i += NT) {
             const uint8_t fm = d.free_mask[i];
             const double2 b = B2[i], di = DI[i];
             const double2 a = warm ? AP[i] : make_double2(0.0, 0.0);
-            const double rx = (fm & 1) ? b.x - a.x : 0.0, ry = (fm & 2) ? b.y - a.y : 0.0;
+            const double rx = plain(i, fm, 0) ? b.x - a.x : 0.0, ry = plain(i, fm, 1) ? b.y - a.y : 0.0;
             R[i] = make_double2(rx, ry);
             const double zx = di.x * rx, zy = di.y * ry;
             Z[i] = make_double2(zx, zy);
             P[i] = make_double2(zx, zy);
             acc[0] += rx * zx + ry * zy;
             acc[1] += rx * rx + ry * ry;
-            acc[2] += ((fm & 1) ? b.x * b.x : 0.0) + ((fm & 2) ? b.y * b.y : 0.0);
+            acc[2] += (plain(i, fm, 0) ? b.x * b.x : 0.0) + (plain(i, fm, 1) ? b.y * b.y : 0.0);
+        }
+        if (has_aff) {
+            // b_q = sum J^T b (a warp per body), r_q = b_q - A_q lam0, then z_q = PI r_q, p_q = z_q
+            for (int b = sg.aff0 + warp; b < sg.aff0 + sg.naff; b += NW) {
+                double *qb = QB + (size_t)QW * b;
+                double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+                for (int k = d.a_ptr[b] + lane; k < d.a_ptr[b + 1]; k += 32) {
+                    const double *w = d.a_w + 3 * k;
+                    const double2 bb = B2[d.a_node[k]];
+                    v[0] += w[0] * bb.x; v[1] += w[1] * bb.x; v[2] += w[2] * bb.x;
+                    v[3] += w[0] * bb.y; v[4] += w[1] * bb.y; v[5] += w[2] * bb.y;
+                }
+                for (int q = 0; q < 6; ++q) v[q] = wsum(v[q]);
+                if (lane == 0)
+                    for (int q = 0; q < 6; ++q) {
+                        qb[Q_R + q] = v[q] - (warm ? qb[Q_AP + q] : 0.0);
+                        acc[2] += v[q] * v[q];
+                    }
+            }
+            block_barrier();
+            for (int b = sg.aff0 + warp; b < sg.aff0 + sg.naff; b += NW) {
+                double *qb = QB + (size_t)QW * b;
+                if (lane < 6) {
+                    double z = 0.0;
+                    for (int q = 0; q < 6; ++q) z += qb[Q_PI + 6 * lane + q] * qb[Q_R + q];
+                    qb[Q_Z + lane] = z;
+                    qb[Q_P + lane] = z;
+                }
+                __syncwarp();
+                if (lane == 0)
+                    for (int q = 0; q < 6; ++q) { acc[0] += qb[Q_R + q] * qb[Q_Z + q]; acc[1] += qb[Q_R + q] * qb[Q_R + q]; }
+            }
         }
         bsum<NT, 3>(acc, red);
         const double bb = acc[2];
@@ -310,14 +623,21 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
         double rr = acc[1];
         for (; it < max_iter; ++it) {
             if (!(rr > rtol * rtol * bb) || s_stop) break;
-            hvp(P);
+            if (has_aff) expand(P, Q_P);
+            hvp(has_aff ? EX : P);
+            if (has_aff) gather_q();
             // ---- alpha = rz / p.Ap
             double pa[1] = {0.0};
             for (int i = n0 + tid; i < n1; i += NT) {
                 const uint8_t fm = d.free_mask[i];
                 const double2 pi = P[i], ai = AP[i];
-                pa[0] += ((fm & 1) ? pi.x * ai.x : 0.0) + ((fm & 2) ? pi.y * ai.y : 0.0);
+                pa[0] += (plain(i, fm, 0) ? pi.x * ai.x : 0.0) + (plain(i, fm, 1) ? pi.y * ai.y : 0.0);
             }
+            for (int b = sg.aff0 + warp; has_aff && b < sg.aff0 + sg.naff; b += NW)
+                if (lane == 0) {
+                    const double *qb = QB + (size_t)QW * b;
+                    for (int q = 0; q < 6; ++q) pa[0] += qb[Q_P + q] * qb[Q_AP + q];
+                }
             bsum<NT, 1>(pa, red);
             if (tid == 0) {
                 if (!(pa[0] > 0.0)) { s_stop = 1; s_status = D2F_ENAN; }  // not positive definite along p
@@ -331,12 +651,30 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                 const uint8_t fm = d.free_mask[i];
                 const double2 pi = P[i], ai = AP[i], li = LAM[i], ri = R[i], di = DI[i];
                 LAM[i] = make_double2(li.x + al * pi.x, li.y + al * pi.y);
-                const double rx = (fm & 1) ? ri.x - al * ai.x : 0.0, ry = (fm & 2) ? ri.y - al * ai.y : 0.0;
+                const double rx = plain(i, fm, 0) ? ri.x - al * ai.x : 0.0, ry = plain(i, fm, 1) ? ri.y - al * ai.y : 0.0;
                 R[i] = make_double2(rx, ry);
                 const double zx = di.x * rx, zy = di.y * ry;
                 Z[i] = make_double2(zx, zy);
                 nr[0] += rx * zx + ry * zy;
                 nr[1] += rx * rx + ry * ry;
+            }
+            if (has_aff) {
+                for (int b = sg.aff0 + warp; b < sg.aff0 + sg.naff; b += NW) {
+                    double *qb = QB + (size_t)QW * b;
+                    if (lane < 6) {
+                        qb[Q_L + lane] += al * qb[Q_P + lane];
+                        qb[Q_R + lane] -= al * qb[Q_AP + lane];
+                    }
+                    __syncwarp();
+                    if (lane < 6) {
+                        double z = 0.0;
+                        for (int q = 0; q < 6; ++q) z += qb[Q_PI + 6 * lane + q] * qb[Q_R + q];
+                        qb[Q_Z + lane] = z;
+                    }
+                    __syncwarp();
+                    if (lane == 0)
+                        for (int q = 0; q < 6; ++q) { nr[0] += qb[Q_R + q] * qb[Q_Z + q]; nr[1] += qb[Q_R + q] * qb[Q_R + q]; }
+                }
             }
             bsum<NT, 2>(nr, red);
             rr = nr[1];
@@ -347,6 +685,16 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                 const double2 zi = Z[i], pi = P[i];
                 P[i] = make_double2(zi.x + be * pi.x, zi.y + be * pi.y);
             }
+            for (int b = sg.aff0 + warp; has_aff && b < sg.aff0 + sg.naff; b += NW) {
+                double *qb = QB + (size_t)QW * b;
+                if (lane < 6) qb[Q_P + lane] = qb[Q_Z + lane] + be * qb[Q_P + lane];
+            }
+            block_barrier();
+        }
+        if (has_aff) {  // lam on the bodies' nodes: J lam_q
+            expand(LAM, Q_L);
+            for (int i = n0 + tid; i < n1; i += NT)
+                if (d.node_aff[i] >= 0) LAM[i] = EX[i];
             block_barrier();
         }
         if (tid == 0) {
@@ -438,6 +786,12 @@ __global__ void vjp_tension_kernel(const __grid_constant__ d2f_scene_desc d, con
 
 extern "C" {
 
+int64_t d2f_adjoint_work_doubles(const d2f_solver *s) {
+    if (!s) return 0;
+    return 12 * (int64_t)s->d.N + (s->d.Ne > 0 ? 24 * (int64_t)s->d.cand_total : 0) +
+           (int64_t)d2f::adj::QW * s->d.n_aff;
+}
+
 int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs, double *lam, double *work,
                           const double *tension, double rtol, int32_t max_iter, int32_t warm_start, int32_t *iters,
                           int32_t *status, void *stream) {
@@ -445,8 +799,6 @@ int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs,
     if (!s || !x_lin || !rhs || !lam || !work || !iters || !status)
         return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: null argument");
     if (s->d.precision != D2F_FP64) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: needs an FP64 solver");
-    if (s->d.Ne > 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: IPC contact between bodies has no adjoint tangent");
-    if (s->d.n_aff > 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: affine bodies have no adjoint tangent");
     if (!(rtol > 0.0) || max_iter <= 0) return d2f_fail(D2F_EINVAL, "d2f_adjoint_solve: rtol > 0 and max_iter > 0");
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(s->d.work, 0, 4 * sizeof(int32_t), st) != cudaSuccess)

@@ -90,9 +90,7 @@ static int validate(const d2f_scene_desc &d, bool scratch) {
     if (nt != 32 && nt != 64 && nt != 128 && nt != 256) return fail(D2F_EINVAL, "d2f: threads must be 32, 64, 128 or 256");
     if (!d.inc8) return fail(D2F_EINVAL, "d2f: inc8 (padded node-corner table) is null");
     if (d.line_search) {
-        if (d.precision != D2F_FP64) return fail(D2F_EINVAL, "d2f: the line search runs in FP64 only");
-        if (d.n_aff > 0) return fail(D2F_EINVAL, "d2f: the line search with affine bodies is not in this build");
-        if (!d.xu) return fail(D2F_EINVAL, "d2f: the line search needs xu (N x 2 doubles)");
+        if (!d.xu) return fail(D2F_EINVAL, "d2f: the line search needs xu (2 N + 6 n_aff doubles)");
         if (d.n_backtrack < 0 || !(d.ls_tol >= 0.0)) return fail(D2F_EINVAL, "d2f: n_backtrack >= 0, ls_tol >= 0");
     }
     if (d.n_sp < 0 || (d.n_sp > 0 && (!d.sp_a || !d.sp_b || !d.sp_k || !d.sp_L0 || !d.sp_anchor)))

@@ -135,6 +135,114 @@ __device__ __forceinline__ bool excluded(const d2f_scene_desc &d, int slot, int 
     return false;
 }
 
+// ---------------------------------------------------------------------- the step energy
+// One thread's share of a scene's step energy (energy_into, solver.py:453-498) in FP64, its
+// terms in a fixed order: inertia and external force (kernels.py:445-468, actuation.py:43-50),
+// elastic (kernels.py:445-468), collider barriers and lagged friction (core/sdf.py:174-181,
+// 274-294; kernels.py:483-513), affine bodies (affine.py:237-246), contact between bodies
+// (`ipc`, the caller's pair pass, ipc_contact.py:414-429), springs (actuation.py:447-456),
+// pressure (actuation.py:121-130) and tendons (actuation.py:259-268). The thread takes items
+// me, me + stride, ... of each list; pos(n) and hat(n) are node n's position and inertial
+// target x-hat in FP64. Both kernels call it: the FP64 kernel on its positions, the mixed
+// kernel on x_b + r.
+template <class Pos, class Hat, class Rm, class B4, class Ipc>
+__device__ __forceinline__ double energy_partial(const d2f_scene_desc &d, const d2f_seg &sg, int me, int stride,
+                                                 Pos pos, Hat hat, const B4 *Bm, const Rm *Ar, const Rm *Mu,
+                                                 const Rm *La, const Col *cols, const double *colmu, Ipc ipc) {
+    const double h2 = d.dt * d.dt, inv_dt = 1.0 / d.dt, dhat = d.dhat, kappa = d.kappa, epsv = d.epsv;
+    const int n_col = d.n_col;
+    const double2 *Xn = reinterpret_cast<const double2 *>(d.xn);
+    const double2 *Fx = reinterpret_cast<const double2 *>(d.fext);
+    double e = 0.0;
+    for (int i = sg.node0 + me; i < sg.node0 + sg.nn; i += stride) {
+        const double2 xi = pos(i), xh = hat(i);
+        const double ux = xi.x - xh.x, uy = xi.y - xh.y;
+        e += 0.5 * d.mass[i] * (ux * ux + uy * uy);
+        if (d.fext) {
+            const double2 f = Fx[i], xn = Xn[i];
+            e += -h2 * (f.x * (xi.x - xn.x) + f.y * (xi.y - xn.y));
+        }
+    }
+    for (int t = sg.tri0 + me; t < sg.tri0 + sg.nt; t += stride) {
+        const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
+        const double2 x0 = pos(i0), x1 = pos(i1), x2 = pos(i2);
+        const B4 B = Bm[t];
+        const double e1x = x1.x - x0.x, e1y = x1.y - x0.y, e2x = x2.x - x0.x, e2y = x2.y - x0.y;
+        const double F00 = e1x * B.x + e2x * B.z, F01 = e1x * B.y + e2x * B.w;
+        const double F10 = e1y * B.x + e2y * B.z, F11 = e1y * B.y + e2y * B.w;
+        const double J = F00 * F11 - F10 * F01, logJ = log(dmax(J, 1.0e-6));
+        const double I2 = F00 * F00 + F01 * F01 + F10 * F10 + F11 * F11;
+        const double mu = (double)Mu[t], la = (double)La[t];
+        e += h2 * (double)Ar[t] * (0.5 * mu * (I2 - 2.0) - mu * logJ + 0.5 * la * logJ * logJ);
+    }
+    for (int j = me; j < sg.nb; j += stride) {
+        const int n = d.bnd[sg.bnd0 + j];
+        const double2 xi = pos(n);
+        const uint8_t fm = d.free_mask[n];
+        for (int k = 0; k < n_col; ++k) {
+            const Col c = cols[k];
+            double dd, nx, ny, gn = 1.0;
+            if (c.kind == 0) {
+                const double ex = xi.x - c.cx, ey = xi.y - c.cy, dc = sqrt(ex * ex + ey * ey);
+                dd = dc - c.r; nx = ex / dc; ny = ey / dc;
+            } else {
+                const SdfHit hh = sdf_eval(c.kind, c.cx, c.cy, c.rx, c.ry, c.rref, xi.x, xi.y);
+                dd = hh.d;
+                gn = sqrt(hh.gx * hh.gx + hh.gy * hh.gy);
+                nx = hh.gx / dmax(gn, 1.0e-30); ny = hh.gy / dmax(gn, 1.0e-30);
+            }
+            if (dd <= 0.0 || dd >= dhat) continue;
+            e += h2 * kappa * barrier_b<double>(dd, dhat);
+            if (d.friction && (fm & 3)) {
+                const double2 xni = Xn[n];
+                const double f_n = kappa * dabs(barrier_bp<double>(dd, dhat)) * gn;
+                const double vx = (xi.x - xni.x) * inv_dt, vy = (xi.y - xni.y) * inv_dt;
+                const double vn = vx * nx + vy * ny;
+                const double vtx = vx - vn * nx, vty = vy - vn * ny;
+                const double ut = sqrt(vtx * vtx + vty * vty) / inv_dt, a = epsv / inv_dt;
+                const double f0 = ut < a ? ut * ut / (2.0 * a) : ut - a * 0.5;
+                e += h2 * colmu[k] * f_n * f0;
+            }
+        }
+    }
+    for (int b = sg.aff0 + me; b < sg.aff0 + sg.naff; b += stride) {
+        const double *q = d.a_q + 6 * b;
+        const M2 A{q[1], q[2], q[4], q[5]};
+        const double logJ = log(dmax(det2(A), 1.0e-6));
+        e += h2 * (0.5 * d.a_Mu[b] * (ddot2(A, A) - 2.0) - d.a_Mu[b] * logJ + 0.5 * d.a_La[b] * logJ * logJ);
+    }
+    ipc(e);
+    for (int k = sg.sp0 + me; k < sg.sp0 + sg.nsp; k += stride) {  // Springs.energy, actuation.py:447-456
+        const int b = d.sp_b[k];
+        const SpringAt sa = spring_at(pos(d.sp_a[k]), b >= 0 ? pos(b) : spring_anchor(d, k), d.sp_k[k], d.sp_L0[k]);
+        const double ext = sa.len - d.sp_L0[k];
+        e += 0.5 * h2 * d.sp_k[k] * ext * ext;
+    }
+    for (int q = sg.pe0 + me; q < sg.pe0 + sg.npe; q += stride) {  // Pressure.energy, actuation.py:121-130
+        const int c = d.pe_ch[q];
+        const double2 xa = pos(d.pe_a[q]), xb = pos(d.pe_b[q]);
+        const double rax = xa.x - d.ch_ref[2 * c], ray = xa.y - d.ch_ref[2 * c + 1];
+        const double rbx = xb.x - d.ch_ref[2 * c], rby = xb.y - d.ch_ref[2 * c + 1];
+        e += -h2 * d.ch_p[c] * 0.5 * (rax * rby - ray * rbx);
+    }
+    for (int k = sg.ten0 + me; k < sg.ten0 + sg.nten; k += stride) {
+        double L = 0.0;
+        for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
+            if (d.t_tid[j] != k || d.t_nxt[j] < 0) continue;
+            const double2 xa = pos(d.t_node[j]), xb = pos(d.t_node[d.t_nxt[j]]);
+            const double ex = xb.x - xa.x, ey = xb.y - xa.y;
+            L += sqrt(ex * ex + ey * ey);
+        }
+        if (d.t_stiff[k] > 0.0) {
+            const double ext = L - d.t_L0[k];
+            if (ext > 0.0) e += 0.5 * h2 * d.t_stiff[k] * ext * ext;
+        } else {
+            e += h2 * dmax(d.t_Tcmd[k], 0.0) * L;
+        }
+    }
+    return e;
+}
+
 // ---------------------------------------------------------------------- the kernel
 template <class R, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_constant__ d2f_scene_desc d) {
@@ -512,93 +620,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
         // (actuation.py:43-50), affine bodies (affine.py:237-246), IPC (ipc_contact.py:414-429)
         // and tendons (actuation.py:259-268). Every thread calls; every thread gets the sum.
         auto scene_energy = [&]() -> double {
-            double e = 0.0;
-            for (int i = n0 + tid; i < n1; i += NT) {
-                const double2 xi = X[i], xh = Xh[i];
-                const double ux = xi.x - xh.x, uy = xi.y - xh.y;
-                e += 0.5 * d.mass[i] * (ux * ux + uy * uy);
-                if (d.fext) {
-                    const double2 f = Fx[i], xn = Xn[i];
-                    e += -h2 * (f.x * (xi.x - xn.x) + f.y * (xi.y - xn.y));
-                }
-            }
-            for (int t = t0 + tid; t < t1; t += NT) {
-                const int i0 = d.tri[3 * t], i1 = d.tri[3 * t + 1], i2 = d.tri[3 * t + 2];
-                const double2 x0 = X[i0], x1 = X[i1], x2 = X[i2];
-                const R4 B = Bm[t];
-                const double e1x = x1.x - x0.x, e1y = x1.y - x0.y, e2x = x2.x - x0.x, e2y = x2.y - x0.y;
-                const double F00 = e1x * B.x + e2x * B.z, F01 = e1x * B.y + e2x * B.w;
-                const double F10 = e1y * B.x + e2y * B.z, F11 = e1y * B.y + e2y * B.w;
-                const double J = F00 * F11 - F10 * F01, logJ = log(dmax(J, 1.0e-6));
-                const double I2 = F00 * F00 + F01 * F01 + F10 * F10 + F11 * F11;
-                const double mu = Mu[t], la = La[t];
-                e += h2 * double(Ar[t]) * (0.5 * mu * (I2 - 2.0) - mu * logJ + 0.5 * la * logJ * logJ);
-            }
-            for (int j = tid; j < nbl; j += NT) {
-                const int n = d.bnd[sg.bnd0 + j];
-                const double2 xi = X[n];
-                const uint8_t fm = d.free_mask[n];
-                for (int k = 0; k < n_col; ++k) {
-                    const Col c = cols[k];
-                    double dd, nx, ny, gn = 1.0;
-                    if (c.kind == 0) {
-                        const double ex = xi.x - c.cx, ey = xi.y - c.cy, dc = sqrt(ex * ex + ey * ey);
-                        dd = dc - c.r; nx = ex / dc; ny = ey / dc;
-                    } else {
-                        const SdfHit hh = sdf_eval(c.kind, c.cx, c.cy, c.rx, c.ry, c.rref, xi.x, xi.y);
-                        dd = hh.d;
-                        gn = sqrt(hh.gx * hh.gx + hh.gy * hh.gy);
-                        nx = hh.gx / dmax(gn, 1.0e-30); ny = hh.gy / dmax(gn, 1.0e-30);
-                    }
-                    if (dd <= 0.0 || dd >= dhat) continue;
-                    e += h2 * kappa * barrier_b<double>(dd, dhat);
-                    if (d.friction && (fm & 3)) {
-                        const double2 xni = Xn[n];
-                        const double f_n = kappa * dabs(barrier_bp<double>(dd, dhat)) * gn;
-                        const double vx = (xi.x - xni.x) * inv_dt, vy = (xi.y - xni.y) * inv_dt;
-                        const double vn = vx * nx + vy * ny;
-                        const double vtx = vx - vn * nx, vty = vy - vn * ny;
-                        const double ut = sqrt(vtx * vtx + vty * vty) / inv_dt, a = epsv / inv_dt;
-                        const double f0 = ut < a ? ut * ut / (2.0 * a) : ut - a * 0.5;
-                        e += h2 * colmu[k] * f_n * f0;
-                    }
-                }
-            }
-            for (int b = sg.aff0 + tid; b < sg.aff0 + sg.naff; b += NT) {
-                const double *q = d.a_q + 6 * b;
-                const M2 A{q[1], q[2], q[4], q[5]};
-                const double logJ = log(dmax(det2(A), 1.0e-6));
-                e += h2 * (0.5 * d.a_Mu[b] * (ddot2(A, A) - 2.0) - d.a_Mu[b] * logJ + 0.5 * d.a_La[b] * logJ * logJ);
-            }
-            if (scene_ipc) ipc_pairs(2, e, 0.0);
-            for (int k = sg.sp0 + tid; k < sg.sp0 + sg.nsp; k += NT) {  // Springs.energy, actuation.py:447-456
-                const int b = d.sp_b[k];
-                const SpringAt sa = spring_at(X[d.sp_a[k]], b >= 0 ? X[b] : spring_anchor(d, k), d.sp_k[k], d.sp_L0[k]);
-                const double ext = sa.len - d.sp_L0[k];
-                e += 0.5 * h2 * d.sp_k[k] * ext * ext;
-            }
-            for (int q = sg.pe0 + tid; q < sg.pe0 + sg.npe; q += NT) {  // Pressure.energy, actuation.py:121-130
-                const int c = d.pe_ch[q];
-                const double2 xa = X[d.pe_a[q]], xb = X[d.pe_b[q]];
-                const double rax = xa.x - d.ch_ref[2 * c], ray = xa.y - d.ch_ref[2 * c + 1];
-                const double rbx = xb.x - d.ch_ref[2 * c], rby = xb.y - d.ch_ref[2 * c + 1];
-                e += -h2 * d.ch_p[c] * 0.5 * (rax * rby - ray * rbx);
-            }
-            for (int k = sg.ten0 + tid; k < sg.ten0 + sg.nten; k += NT) {
-                double L = 0.0;
-                for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
-                    if (d.t_tid[j] != k || d.t_nxt[j] < 0) continue;
-                    const double2 xa = X[d.t_node[j]], xb = X[d.t_node[d.t_nxt[j]]];
-                    const double ex = xb.x - xa.x, ey = xb.y - xa.y;
-                    L += sqrt(ex * ex + ey * ey);
-                }
-                if (d.t_stiff[k] > 0.0) {
-                    const double ext = L - d.t_L0[k];
-                    if (ext > 0.0) e += 0.5 * h2 * d.t_stiff[k] * ext * ext;
-                } else {
-                    e += h2 * dmax(d.t_Tcmd[k], 0.0) * L;
-                }
-            }
+            double e = energy_partial(d, sg, tid, NT, [&](int n) { return X[n]; }, [&](int n) { return Xh[n]; }, Bm, Ar,
+                                      Mu, La, cols, colmu, [&](double &acc) { if (scene_ipc) ipc_pairs(2, acc, 0.0); });
             double v[1] = {e};
             const int ops[1] = {0};
             block_reduce<NT, 1>(v, ops, red);
@@ -1279,8 +1302,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                             }
                         }
                     }
-                    // affine_advance_kernel (affine.py:249-257)
-                    if (S.active)
+                    // affine_advance_kernel (affine.py:249-257); with the line search the
+                    // trial points move q instead (affine_trial_kernel)
+                    if (S.active && !d.line_search)
                         for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b)
                             for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
                 }
@@ -1292,17 +1316,31 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
             if (d.line_search) {
                 // E0 at x, then n_backtrack trial points x0 + alpha p, alpha halved while the
                 // energy exceeds E0 + ls_tol (|E0| + 1) (ls_halve_kernel, solver.py:63-73)
+                // affine bodies: q0 saved after the nodes (AffineBodies.save), the trial
+                // q = q0 + alpha p_q and its nodes J q (affine_trial_kernel, affine.py:260-269)
                 double2 *__restrict__ X0 = reinterpret_cast<double2 *>(d.xu);
+                double *__restrict__ Q0 = d.xu + 2 * (size_t)d.N;
                 const double E0 = scene_energy();
                 for (int i = n0 + tid; i < n1; i += NT) X0[i] = X[i];
+                for (int k = sg.aff0 * 6 + tid; k < (sg.aff0 + sg.naff) * 6; k += NT) Q0[k] = d.a_q[k];
                 block_barrier();
                 auto trial = [&]() {  // set_x_from_x0_kernel, solver.py:52-60
                     if (S.active) {
                         const double al = S.alpha;
+                        for (int k = sg.aff0 * 6 + tid; k < (sg.aff0 + sg.naff) * 6; k += NT)
+                            d.a_q[k] = Q0[k] + al * d.a_pq[k];
+                        if (sg.naff > 0) block_barrier();
                         for (int i = n0 + tid; i < n1; i += NT) {
-                            const R2 pp = P[i];
-                            const double2 x0 = X0[i];
-                            X[i] = make_double2(x0.x + al * double(pp.x), x0.y + al * double(pp.y));
+                            const int ka = d.node_aff[i];
+                            if (ka >= 0) {
+                                const double *w = d.a_w + 3 * ka, *q = d.a_q + 6 * d.a_grp[ka];
+                                X[i] = make_double2(w[0] * q[0] + w[1] * q[1] + w[2] * q[2],
+                                                    w[0] * q[3] + w[1] * q[4] + w[2] * q[5]);
+                            } else {
+                                const R2 pp = P[i];
+                                const double2 x0 = X0[i];
+                                X[i] = make_double2(x0.x + al * double(pp.x), x0.y + al * double(pp.y));
+                            }
                         }
                     }
                     block_barrier();

@@ -22,9 +22,12 @@
 //   * friction: slip velocity dx / dt;
 //   * rigid modes: arms a = (x_n - c_n) + dx - (c - c_n).
 //   * dot products: each thread accumulates its FP32 products with compensated (TwoSum)
-//     FP32 pairs, warps merge the pairs, and the per-warp partials are summed in FP64. The
-//     Dai-Kou beta, the step length, the convergence ratio and the energy model stay FP64.
-//   * step caps (inversion, CCD, |p|, clearance) are FP32 minima/maxima.
+//     FP32 pairs, warps and then the per-warp partials merge the pairs, and each sum is
+//     converted to FP64 once. The Dai-Kou beta, the step length and the energy-decrease test
+//     stay FP64 (divisions through an FP32 reciprocal and one FP64 Newton step);
+//   * step caps (inversion, CCD, |p|, clearance), the gradient-norm test and the rigid-mode
+//     preconditioner's 3x3 solve are FP32;
+//   * the line search (when on): every energy term in FP64 at x_b + r.
 // At the end of the step x = x_b + r and v = (x - x_n)/dt in FP64.
 #pragma once
 #include <cooperative_groups.h>
@@ -85,13 +88,16 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
         for (int k = 0; k < NM; ++k) w[2 * NS + k] = m[k];
     }
     block_barrier();
-    // the per-warp partials: sum k by thread k (FP64), extremum k by thread NS + k
+    // the per-warp partials: sum k by thread k (merged as compensated pairs, then one
+    // conversion to FP64: dependent FP64 operations are slow on this part), extremum k by
+    // thread NS + k
     {
         const int k = threadIdx.x;
         if (k < NS) {
-            double acc = 0.0;
-            for (int q = 0; q < NW; ++q) acc += (double)fred[q * (2 * NS + NM) + 2 * k] + (double)fred[q * (2 * NS + NM) + 2 * k + 1];
-            dres[k] = acc;
+            FF acc{fred[2 * k], fred[2 * k + 1]};
+            for (int q = 1; q < NW; ++q)
+                acc = ff_merge(acc, FF{fred[q * (2 * NS + NM) + 2 * k], fred[q * (2 * NS + NM) + 2 * k + 1]});
+            dres[k] = (double)acc.hi + (double)acc.lo;
         } else if (k < NS + NM) {
             const int j = k - NS;
             float a = fred[2 * NS + j];
@@ -326,6 +332,55 @@ inline MixedPtrs mixed_ptrs(const d2f_scene_desc &d) {
     return p;
 }
 
+// The mixed kernel's per-scene FP32 scalars: FP32 copies of the step length and Dai-Kou
+// coefficient for the node passes, the rigid-mode preconditioner's terms, the caps and the
+// gradient-norm test. A chain of dependent FP64 operations on one thread costs ~100 cycles an
+// operation on this part, and these run once per iteration while the scene's other threads
+// wait at the next barrier; the CG coefficients themselves and the energy-decrease test stay
+// FP64 (SceneSh).
+struct SceneF {
+    float alpha, beta, pinf, gn0, gn2;
+    float gPg, g_Py, y_Py;      // the rigid pieces' Dai-Kou terms
+    float csx, csy, mpx, mpy;   // single rigid piece: centroid shift (copy of SceneSh's), sum m p / M
+    float inv_m;                // single rigid piece: 1 / M
+};
+
+// 1 / v in FP64 from the FP32 reciprocal and one Newton step (relative error ~1e-14): four
+// FP64 operations where a division takes several times that, on a thread the scene's other
+// warps wait for. Outside FP32's range, the division.
+__device__ __forceinline__ double rcp64(double v) {
+    const float f = (float)v;
+    if (!(fabsf(f) > 1.0e-36f && fabsf(f) < 1.0e36f)) return 1.0 / v;
+    const double r = (double)(1.0f / f);
+    return r * fma(-v, r, 2.0);
+}
+
+// One rigid piece's preconditioner solve (RigidModes reduce, rigid_reduce_kernel,
+// affine.py:456-473) in FP32: v = B^T g (3), B^T g_prev (3) and the symmetric 3x3 B^T D' B as
+// a00, a02, a11, a12, a22 (a01 = 0); z = A^-1 B^T g and zy = A^-1 B^T (g - g_prev) through the
+// adjugate (A^-1 = 0 for a singular A, as the FP64 kernel); the piece's Dai-Kou terms g.z,
+// g.zy, y.zy added to F; z to zq (FP64) or zf.
+__device__ __forceinline__ void rigid_precondition(const float *v, SceneF &F, double *zq, float *zf) {
+    const float A = v[6], B = v[7], C = v[8], D = v[9], E = v[10];
+    const float c00 = C * E - D * D, c01 = B * D, c02 = -B * C;
+    const float c11 = A * E - B * B, c12 = -A * D, c22 = A * C;
+    const float det = A * c00 + B * c02;
+    const float r = det != 0.f ? 1.f / det : 0.f;
+    const float g0 = v[0], g1 = v[1], g2 = v[2];
+    const float y0 = g0 - v[3], y1 = g1 - v[4], y2 = g2 - v[5];
+    const float z0 = (c00 * g0 + c01 * g1 + c02 * g2) * r;
+    const float z1 = (c01 * g0 + c11 * g1 + c12 * g2) * r;
+    const float z2 = (c02 * g0 + c12 * g1 + c22 * g2) * r;
+    const float w0 = (c00 * y0 + c01 * y1 + c02 * y2) * r;
+    const float w1 = (c01 * y0 + c11 * y1 + c12 * y2) * r;
+    const float w2 = (c02 * y0 + c12 * y1 + c22 * y2) * r;
+    if (zq) { zq[0] = z0; zq[1] = z1; zq[2] = z2; }
+    if (zf) { zf[0] = z0; zf[1] = z1; zf[2] = z2; }
+    F.gPg += g0 * z0 + g1 * z1 + g2 * z2;
+    F.g_Py += g0 * w0 + g1 * w1 + g2 * w2;
+    F.y_Py += y0 * w0 + y1 * w1 + y2 * w2;
+}
+
 // CS: blocks per scene. 1: a block per scene (batches). > 1: a cluster of CS blocks works on
 // one scene (large scenes): the scene's loops are spread over the cluster's threads, phases are
 // separated by cluster barriers, reductions combine the blocks' results through distributed
@@ -338,6 +393,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     constexpr bool CL = CS > 1;
     constexpr int GS = CS * NT;  // threads working on one scene
     __shared__ SceneSh S;
+    __shared__ SceneF F;
     __shared__ Col cols[MAX_COL];
     __shared__ double red[NW * 20 + 20];
     __shared__ float fred[NW * 40];
@@ -369,6 +425,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 finv_dt = (float)inv_dt, feta = (float)d.ccd_eta;
     const bool has_ipc = d.Ne > 0;
     const int n_col = d.n_col;
+    // the stop tests' and caps' constants in FP32
+    const bool use_gtol = d.gtol > 0.0, use_tolx = d.tol_x > 0.0, use_guard = d.cg_guard > 0.0;
+    const float fgtol2 = (float)(d.gtol * d.gtol), ftol_x = (float)d.tol_x;
+    const float falpha_max = (float)d.alpha_max, fnear = (float)(d.near_factor * dhat), freach45 = (float)(0.45 * d.reach);
 
     double2 *__restrict__ X = reinterpret_cast<double2 *>(d.x);
     double2 *__restrict__ Xn = reinterpret_cast<double2 *>(d.xn);
@@ -432,7 +492,6 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         const bool scene_rig = sg.nrig > 0;
         const bool scene_rare = scene_ipc || sg.naff > 0 || sg.nten > 0 || sg.nsp > 0 || sg.npe > 0;  // terms with FP64 contributions
         const int nbl = sg.nb;
-        const double near = d.near_factor * dhat;
         if (tid < n_col && tid < MAX_COL) {
             colmu[tid] = d.col_mu_env ? d.col_mu_env[sc * n_col + tid] : cols[tid].mu;
             colmuf[tid] = (float)colmu[tid];
@@ -587,6 +646,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             S.alpha = d.alpha_max; S.pHp = 0.0; S.q_inf = 0.0; S.alpha_s = 1.0;
             S.ncand = 0; S.rebuild = 1; S.gn0 = 0.0; S.beta = 0.0;
             S.motion = 0.0; S.csx = 0.0; S.csy = 0.0;
+            F.alpha = falpha_max; F.beta = 0.f; F.pinf = 0.f; F.gn0 = 0.f; F.gn2 = 0.f;
+            F.gPg = 0.f; F.g_Py = 0.f; F.y_Py = 0.f; F.csx = 0.f; F.csy = 0.f; F.mpx = 0.f; F.mpy = 0.f; F.inv_m = 0.f;
         }
         gsync();
         for (int j = gt; j < nbl; j += GS) {  // half-space distances at x_n
@@ -624,6 +685,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 RARM[i] = make_float2((float)(xi.x - cx), (float)(xi.y - cy));
             }
             if (tid == 0 && crank == 0) { d.r_acc[3 * b] = cx; d.r_acc[3 * b + 1] = cy; d.r_acc[3 * b + 2] = c[2]; }
+            if (tid == 0 && sg.nrig == 1) F.inv_m = (float)(1.0 / c[2]);
         }
         gsync();
 
@@ -954,6 +1016,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                             atomicAdd(dp_, (float)(ch[q] * hx));
                             atomicAdd(dp_ + 1, (float)(ch[q] * hy));
                         }
+                    } else if (mode == 2) {  // energy: barrier + lagged friction (ipc_contact.py:414-429)
+                        const double asl = d.epsv / inv_dt, au = dabs(ut);
+                        const double f0 = au < asl ? au * au / (2.0 * asl) : au - 0.5 * asl;
+                        acc_pHp += coef * h2 * (ikappa * barrier_b<double>(dist, idhat) + mu_p * f_n * f0);
                     } else {
                         const double bpp = barrier_bpp<double>(dist, idhat);
                         const float2 u0 = P[ip], u1 = P[ia], u2 = P[ib];
@@ -1129,6 +1195,23 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             gsync();
         };
 
+        // the scene's step energy at x_b + r in FP64 (PNCG2DSolver._energy_into,
+        // solver.py:453-498), for the line search; a kinematic node's x-hat is its position
+        // (inertia 0), as the FP64 step sets it (apply_bc_kernel, IPCContact.advance_bc)
+        auto energy_mx = [&]() -> double {
+            double v[1] = {energy_partial(
+                d, sg, gt, GS, xpos,
+                [&](int n) -> double2 {
+                    if (d.node_bc[n] >= 0) return xpos(n);
+                    const double2 xn = Xn[n], vn = Vv[n];
+                    return make_double2(xn.x + dt * d.drag * vn.x, xn.y + dt * d.drag * vn.y);
+                },
+                Bm, Ar, Mu, La, cols, colmu, [&](double &acc) { if (scene_ipc) ipc_pairs(2, acc, 0.0); })};
+            const int ops[1] = {0};
+            scene_reduce<NT, CS, 1>(v, ops, red, cres);
+            return v[0];
+        };
+
         if (scene_ipc && sg.nbc > 0) {
             sweep();
             if (tid == 0) S.pending = !(S.alpha_s >= 1.0);
@@ -1296,16 +1379,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 gsync();
             }
             if (sg.nten > 0) {
-                for (int k = sg.ten0 + gt; k < sg.ten0 + sg.nten; k += GS) {
-                    double L = 0.0;
-                    for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
-                        if (d.t_tid[j] != k) continue;
-                        const int m = d.t_nxt[j];
-                        if (m < 0) continue;
-                        const double2 xa = xpos(d.t_node[j]), xb = xpos(d.t_node[m]);
-                        const double ex = xb.x - xa.x, ey = xb.y - xa.y;
-                        L += sqrt(ex * ex + ey * ey);
-                    }
+                // tension and stiffness of each tendon at x (Tendon.grad_diag, actuation.py:169-228)
+                auto tendon_state = [&](int k, double L) {
                     double tau, keff;
                     if (d.t_stiff[k] > 0.0) {
                         const double ext = L - d.t_L0[k];
@@ -1316,6 +1391,34 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     }
                     double *ts = d.t_state + 4 * k;
                     ts[0] = L; ts[2] = tau; ts[3] = keff;
+                };
+                if (sg.nten == 1) {
+                    // one tendon (the common case): its length as a scene reduction over the
+                    // segments, a thread per segment, instead of one thread walking them all
+                    double L[1] = {0.0};
+                    for (int j = sg.tent0 + gt; j < sg.tent0 + sg.ntent; j += GS) {
+                        const int m = d.t_nxt[j];
+                        if (m < 0) continue;
+                        const double2 xa = xpos(d.t_node[j]), xb = xpos(d.t_node[m]);
+                        const double ex = xb.x - xa.x, ey = xb.y - xa.y;
+                        L[0] += sqrt(ex * ex + ey * ey);
+                    }
+                    const int ops1[1] = {0};
+                    scene_reduce<NT, CS, 1>(L, ops1, red, cres);
+                    if (gt == 0) tendon_state(sg.ten0, L[0]);
+                } else {
+                    for (int k = sg.ten0 + gt; k < sg.ten0 + sg.nten; k += GS) {
+                        double L = 0.0;
+                        for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
+                            if (d.t_tid[j] != k) continue;
+                            const int m = d.t_nxt[j];
+                            if (m < 0) continue;
+                            const double2 xa = xpos(d.t_node[j]), xb = xpos(d.t_node[m]);
+                            const double ex = xb.x - xa.x, ey = xb.y - xa.y;
+                            L += sqrt(ex * ex + ey * ey);
+                        }
+                        tendon_state(k, L);
+                    }
                 }
                 gsync();
                 for (int j = sg.tent0 + gt; j < sg.tent0 + sg.ntent; j += GS) {
@@ -1422,7 +1525,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 gsync();
                 for (int k = sg.affn0 + gt; k < sg.affn0 + sg.naffn; k += GS) G[d.a_node[k]] = make_float2(0.f, 0.f);
             }
-            if (tid == 0) { S.gPg = 0.0; S.g_Py = 0.0; S.y_Py = 0.0; }
+            if (tid == 0) { F.gPg = 0.f; F.g_Py = 0.f; F.y_Py = 0.f; }
             // one rigid piece (a free soft body): its gather is folded into the Dai-Kou pass below;
             // several pieces: one reduction each here
             const bool rig1 = sg.nrig == 1;
@@ -1443,8 +1546,8 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 double so[2];
                 float mo_[1];
                 scene_reduce_mx<NT, CS, 2, 1>(cs2, nm, nmo, so, mo_, fred, dres, mres, cres, cmres);
-                const double Mtot = d.r_acc[3 * b + 2];
-                const float csx = (float)(so[0] / Mtot), csy = (float)(so[1] / Mtot);
+                const float Mtot = (float)d.r_acc[3 * b + 2];
+                const float csx = (float)so[0] / Mtot, csy = (float)so[1] / Mtot;
                 FF v[11];
 #pragma unroll
                 for (int q = 0; q < 11; ++q) v[q] = FF{0.f, 0.f};
@@ -1464,33 +1567,11 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 double vs[11];
                 scene_reduce_mx<NT, CS, 11, 1>(v, nm, nmo, vs, mo_, fred, dres, mres, cres, cmres);
                 if (tid == 0) {
-                    const double a[9] = {vs[6], 0.0, vs[7], 0.0, vs[8], vs[9], vs[7], vs[9], vs[10]};
-                    const double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[6] * a[5]) +
-                                       a[2] * (a[3] * a[7] - a[6] * a[4]);
-                    double Hi[9] = {0};
-                    if (det != 0.0) {
-                        const double r = 1.0 / det;
-                        Hi[0] = (a[4] * a[8] - a[5] * a[7]) * r; Hi[1] = (a[2] * a[7] - a[1] * a[8]) * r;
-                        Hi[2] = (a[1] * a[5] - a[2] * a[4]) * r; Hi[3] = (a[5] * a[6] - a[3] * a[8]) * r;
-                        Hi[4] = (a[0] * a[8] - a[2] * a[6]) * r; Hi[5] = (a[2] * a[3] - a[0] * a[5]) * r;
-                        Hi[6] = (a[3] * a[7] - a[4] * a[6]) * r; Hi[7] = (a[1] * a[6] - a[0] * a[7]) * r;
-                        Hi[8] = (a[0] * a[4] - a[1] * a[3]) * r;
-                    }
-                    const double g[3] = {vs[0], vs[1], vs[2]}, y[3] = {vs[0] - vs[3], vs[1] - vs[4], vs[2] - vs[5]};
-                    double z[3], zy[3];
-                    for (int r = 0; r < 3; ++r) {
-                        z[r] = Hi[3 * r] * g[0] + Hi[3 * r + 1] * g[1] + Hi[3 * r + 2] * g[2];
-                        zy[r] = Hi[3 * r] * y[0] + Hi[3 * r + 1] * y[1] + Hi[3 * r + 2] * y[2];
-                    }
-                    for (int r = 0; r < 3; ++r) d.r_zq[3 * b + r] = z[r];
+                    float v32[11];
+                    for (int q = 0; q < 11; ++q) v32[q] = (float)vs[q];
+                    rigid_precondition(v32, F, lb < 8 ? nullptr : d.r_zq + 3 * b, lb < 8 ? s_zf[lb] : nullptr);
                     RCS[b] = make_float2(csx, csy);
-                    if (lb < 8) {
-                        s_zf[lb][0] = (float)z[0]; s_zf[lb][1] = (float)z[1]; s_zf[lb][2] = (float)z[2];
-                        s_cs[lb][0] = csx; s_cs[lb][1] = csy;
-                    }
-                    S.gPg += g[0] * z[0] + g[1] * z[1] + g[2] * z[2];
-                    S.g_Py += g[0] * zy[0] + g[1] * zy[1] + g[2] * zy[2];
-                    S.y_Py += y[0] * zy[0] + y[1] * zy[1] + y[2] * zy[2];
+                    if (lb < 8) { s_cs[lb][0] = csx; s_cs[lb][1] = csy; }
                 }
                 gsync();
             }
@@ -1529,21 +1610,28 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         for (int r = 0; r < 6; ++r) { d.a_gq[6 * b + r] = g[r]; d.a_zq[6 * b + r] = z[r]; }
                     }
                 }
-                if (tid == 0) {  // B2: per-scene scalars, FP64 (every block of a cluster alike)
-                    const double gPg = vs[0] + S.gPg + ab[0], g_p = vs[1] + ab[1], g_Py = vs[2] + S.g_Py + ab[2];
-                    const double y_p = vs[3] + ab[3], y_Py = vs[4] + S.y_Py + ab[4];
+                if (tid == 0) {  // B2: Dai-Kou beta (every block of a cluster alike)
+                    // the dot products and the coefficients formed from them in FP64 (the
+                    // rigid pieces' terms come from the FP32 preconditioner solve); divisions by
+                    // rcp64, in an order with no product of two dot products
+                    double gPg = vs[0] + (double)F.gPg, g_p = vs[1], g_Py = vs[2] + (double)F.g_Py;
+                    double y_p = vs[3], y_Py = vs[4] + (double)F.y_Py;
+                    if (sg.naff > 0) { gPg += ab[0]; g_p += ab[1]; g_Py += ab[2]; y_p += ab[3]; y_Py += ab[4]; }
                     double bta = 0.0;  // finalize_beta_kernel, kernels.py:195-217
-                    if (it > 0 && dabs(y_p) > 1.0e-30) bta = g_Py / y_p - y_Py * g_p / (y_p * y_p);
+                    if (it > 0 && dabs(y_p) > 1.0e-30) {
+                        const double r = rcp64(y_p);
+                        bta = (g_Py - y_Py * (g_p * r)) * r;
+                    }
                     double gtp = -gPg + bta * g_p;
                     if (gtp >= 0.0) { bta = 0.0; gtp = -gPg; }
-                    if (d.cg_guard > 0.0 && it > 0) {  // cg_guard_kernel, solver.py:76-94
-                        const double hold = (scene_ipc && S.pending) ? S.q_inf : 0.0;
-                        if (hold <= 0.0 && y_p < d.cg_guard * S.alpha * S.pHp) { bta = 0.0; gtp = -gPg; }
+                    if (use_guard && it > 0) {  // cg_guard_kernel, solver.py:76-94
+                        const bool hold = scene_ipc && S.pending && S.q_inf > 0.0;
+                        if (!hold && y_p < d.cg_guard * S.alpha * S.pHp) { bta = 0.0; gtp = -gPg; }
                     }
-                    S.beta = bta; S.gTp = gtp; S.gn2 = vs[5];
+                    S.beta = bta; S.gTp = gtp; F.beta = (float)bta; F.gn2 = (float)vs[5];
                 }
                 gsync();
-                if (sg.naff > 0) {  // the bodies' directions, read by B3
+                if (sg.naff > 0) {  // the bodies' directions, read by B3 (FP64 beta: the stiff bodies need it)
                     const double bta = S.beta;
                     for (int b = sg.aff0 + gt; b < sg.aff0 + sg.naff; b += GS)
                         for (int r = 0; r < 6; ++r) d.a_pq[6 * b + r] = -d.a_zq[6 * b + r] + bta * d.a_pq[6 * b + r];
@@ -1562,7 +1650,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 int rops[NM];
 #pragma unroll
                 for (int q = 0; q < NM; ++q) { r[q] = 0.f; rops[q] = q == 0 ? 1 : 0; }
-                const float csx = (float)S.csx, csy = (float)S.csy;
+                const float csx = F.csx, csy = F.csy;
                 for (int i = n0 + gt; i < n1; i += GS) {
                     const int inf = NINFO[i].x, fm = inf & 3;
                     float2 g = G[i];
@@ -1597,34 +1685,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 float mo_[NM];
                 scene_reduce_mx<NT, CS, NS, NM>(v, r, rops, vs, mo_, fred, dres, mres, cres, cmres);
                 if constexpr (RIG) {
-                    if (tid == 0) {  // rigid_reduce_kernel, affine.py:456-473 (FP64)
-                        const int b = sg.rig0;
-                        double rv[17];
-                        for (int q = 6; q < 17; ++q) rv[q] = (double)mo_[q - 5];
-                        const double a[9] = {rv[12], 0.0, rv[13], 0.0, rv[14], rv[15], rv[13], rv[15], rv[16]};
-                        const double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[1] * (a[3] * a[8] - a[6] * a[5]) +
-                                           a[2] * (a[3] * a[7] - a[6] * a[4]);
-                        double Hi[9] = {0};
-                        if (det != 0.0) {
-                            const double r = 1.0 / det;
-                            Hi[0] = (a[4] * a[8] - a[5] * a[7]) * r; Hi[1] = (a[2] * a[7] - a[1] * a[8]) * r;
-                            Hi[2] = (a[1] * a[5] - a[2] * a[4]) * r; Hi[3] = (a[5] * a[6] - a[3] * a[8]) * r;
-                            Hi[4] = (a[0] * a[8] - a[2] * a[6]) * r; Hi[5] = (a[2] * a[3] - a[0] * a[5]) * r;
-                            Hi[6] = (a[3] * a[7] - a[4] * a[6]) * r; Hi[7] = (a[1] * a[6] - a[0] * a[7]) * r;
-                            Hi[8] = (a[0] * a[4] - a[1] * a[3]) * r;
-                        }
-                        const double g[3] = {rv[6], rv[7], rv[8]}, y[3] = {rv[6] - rv[9], rv[7] - rv[10], rv[8] - rv[11]};
-                        double z[3], zy[3];
-                        for (int r = 0; r < 3; ++r) {
-                            z[r] = Hi[3 * r] * g[0] + Hi[3 * r + 1] * g[1] + Hi[3 * r + 2] * g[2];
-                            zy[r] = Hi[3 * r] * y[0] + Hi[3 * r + 1] * y[1] + Hi[3 * r + 2] * y[2];
-                        }
-                        for (int r = 0; r < 3; ++r) d.r_zq[3 * b + r] = z[r];
-                        s_zf[0][0] = (float)z[0]; s_zf[0][1] = (float)z[1]; s_zf[0][2] = (float)z[2];
+                    if (tid == 0) {  // rigid_reduce_kernel, affine.py:456-473
+                        rigid_precondition(mo_ + 1, F, nullptr, s_zf[0]);
                         s_cs[0][0] = csx; s_cs[0][1] = csy;
-                        S.gPg += g[0] * z[0] + g[1] * z[1] + g[2] * z[2];
-                        S.g_Py += g[0] * zy[0] + g[1] * zy[1] + g[2] * zy[2];
-                        S.y_Py += y[0] * zy[0] + y[1] * zy[1] + y[2] * zy[2];
                     }
                 }
                 b2(vs);
@@ -1634,9 +1697,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             // ---------------------------------------------- B3: direction + node curvature and caps
             FF acc_pHp{0.f, 0.f}, acc_mpx{0.f, 0.f}, acc_mpy{0.f, 0.f};  // p^T H p; single rigid piece: sum m p
             double acc_rare = 0.0;
-            float acc_pinf = 0.f, acc_clr = 1.0e30f, acc_alpha = (float)d.alpha_max;
+            float acc_pinf = 0.f, acc_clr = 1.0e30f, acc_alpha = falpha_max;
             {
-                const float bta = (float)S.beta;
+                const float bta = F.beta;
                 for (int i = n0 + gt; i < n1; i += GS) {
                     const int2 inf = NINFO[i];
                     const int fm = inf.x & 3;
@@ -1828,7 +1891,25 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         const float2 pa = P[d.pe_a[e]], pb = P[d.pe_b[e]];
                         acc_rare += -h2 * d.ch_p[d.pe_ch[e]] * ((double)pa.x * (double)pb.y - (double)pa.y * (double)pb.x);
                     }
-                    for (int k = sg.ten0 + gt; k < sg.ten0 + sg.nten; k += GS) {  // Tendon.pHp
+                    const bool ten_par = sg.nten == 1 && d.t_state[4 * sg.ten0 + 3] == 0.0;
+                    if (ten_par) {
+                        // one tendon without length stiffness at x (Tendon.pHp): a thread per
+                        // segment, tau / len (|dp|^2 - (dp.s)^2) each
+                        const double tau = d.t_state[4 * sg.ten0 + 2];
+                        for (int j = sg.tent0 + gt; j < sg.tent0 + sg.ntent; j += GS) {
+                            const int m = d.t_nxt[j];
+                            if (m < 0) continue;
+                            const int na = d.t_node[j], nb_ = d.t_node[m];
+                            const double2 xa = xpos(na), xb = xpos(nb_);
+                            const double tx = xb.x - xa.x, ty = xb.y - xa.y, ln = dmax(sqrt(tx * tx + ty * ty), 1.0e-12);
+                            const double sx = tx / ln, sy = ty / ln;
+                            const float2 pa = P[na], pb = P[nb_];
+                            const double dpx = (double)pb.x - (double)pa.x, dpy = (double)pb.y - (double)pa.y;
+                            const double along = dpx * sx + dpy * sy;
+                            acc_rare += h2 * tau * ((dpx * dpx + dpy * dpy) - along * along) * (1.0 / ln);
+                        }
+                    }
+                    for (int k = sg.ten0 + gt; !ten_par && k < sg.ten0 + sg.nten; k += GS) {  // Tendon.pHp, a thread per tendon
                         const double tau = d.t_state[4 * k + 2], keff = d.t_state[4 * k + 3];
                         double dL = 0.0;
                         for (int j = sg.tent0; j < sg.tent0 + sg.ntent; ++j) {
@@ -1861,32 +1942,38 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 float mo[3];
                 scene_reduce_mx<NT, CS, 3, 3>(sv, mv, mops, so, mo, fred, dres, mres, cres, cmres);
                 const double a_ccd = scene_ipc ? tc_scan(d.alpha_max) : 0.0;
-                // ---------------------------------------------- B5: step length and convergence (FP64)
+                // ---------------------------------------------- B5: step length and convergence
+                // (alpha_finalize_kernel, kernels.py:374-423): the step length and the
+                // energy-decrease test in FP64 from the FP64 dot products, the caps and the
+                // gradient-norm test in FP32
                 if (tid == 0) {
-                    const double ph = so[0], pinf = mo[0], clr = mo[1];
-                    double a = mo[2];
+                    const double ph = so[0];
+                    const float pinf = mo[0], clr = mo[1];
+                    float af = mo[2];
                     if (scene_ipc) {
-                        a = dmin(a, a_ccd);
-                        if (pinf > 0.0) a = dmin(a, 0.45 * d.reach / pinf);
+                        af = fminf(af, __double2float_rd(a_ccd));
+                        if (pinf > 0.f) af = fminf(af, freach45 / pinf);
                     }
-                    S.pHp = ph; S.p_inf = pinf; S.clr_min = clr;
+                    F.pinf = pinf;
+                    S.pHp = ph;
+                    double a = af;
                     S.alpha = a;
                     if (S.active) {
                         bool done = false;
-                        if (d.gtol > 0.0) {
-                            if (it == 0) S.gn0 = S.gn2;
-                            else if (S.gn2 <= d.gtol * d.gtol * S.gn0) { S.active = 0; done = true; }
+                        if (use_gtol) {
+                            if (it == 0) F.gn0 = F.gn2;
+                            else if (F.gn2 <= fgtol2 * F.gn0) { S.active = 0; done = true; }
                         }
                         if (!done) {
-                            if (ph > 0.0) a = dmin(a, -S.gTp / ph);
-                            if (clr < near && pinf > 0.0) a = dmin(a, 0.5 * dhat / pinf);
+                            if (ph > 0.0) a = dmin(a, -S.gTp * rcp64(ph));
+                            if (clr < fnear && pinf > 0.f) a = dmin(a, (double)(0.5f * fdhat / pinf));
                             if (!(a == a)) { S.status = D2F_ENAN; S.active = 0; S.alpha = 0.0; }
                             else if (a <= 0.0) { S.active = 0; S.alpha = 0.0; }
                             else {
                                 S.alpha = a;
-                                if (d.tol_x > 0.0 && a * pinf < d.tol_x) { S.active = 0; S.iters += 1; }
+                                if (use_tolx && (float)a * pinf < ftol_x) { S.active = 0; S.iters += 1; }
                                 else {
-                                    const double dm = -a * S.gTp - 0.5 * a * a * ph;
+                                    const double dm = a * (-S.gTp - 0.5 * a * ph);
                                     if (it == 0) S.dE0 = dmax(dm, 1.0e-300);
                                     else if (dm < d.eps * S.dE0) S.active = 0;
                                     S.iters += 1;
@@ -1894,27 +1981,98 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                             }
                         }
                     }
+                    F.alpha = (float)S.alpha;
                     if (S.active) {
-                        S.motion += S.alpha * pinf;              // bound on any node's move
+                        if (scene_ipc) S.motion += S.alpha * (double)pinf;  // bound on any node's move
                         if (rig1) {                              // centroid shift, sum m dx / M
-                            const double Mt = d.r_acc[3 * sg.rig0 + 2];
-                            S.csx += S.alpha * so[1] / Mt;
-                            S.csy += S.alpha * so[2] / Mt;
+                            const float mx = (float)so[1] * F.inv_m, my = (float)so[2] * F.inv_m;
+                            if (d.line_search) {                 // added with the accepted step
+                                F.mpx = mx;
+                                F.mpy = my;
+                            } else {
+                                S.csx += S.alpha * (double)mx;
+                                S.csy += S.alpha * (double)my;
+                                F.csx = (float)S.csx;
+                                F.csy = (float)S.csy;
+                            }
                         }
                     }
                 }
                 gsync();
-                if (sg.naff > 0 && S.active) {  // AffineBodies.advance, affine.py:249-257: q += alpha p_q
+                if (sg.naff > 0 && S.active && !d.line_search) {  // AffineBodies.advance, affine.py:249-257: q += alpha p_q
                     for (int b = sg.aff0 + gt; b < sg.aff0 + sg.naff; b += GS)
                         for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
                     gsync();
                 }
             }
 
-            // ---------------------------------------------- D1: r += alpha p, dx = (x_b - x_n) + r (slaved nodes: J q)
-            {
+            // ---------------------------------------------- D1: r += alpha p, dx = (x_b - x_n) + r (slaved nodes: J q),
+            // or the backtracking line search (solver.py:397-425): the energy E0 at x in FP64,
+            // then n_backtrack trial points x_b + (r0 + alpha p) (affine bodies q0 + alpha p_q,
+            // affine.py:383-389), alpha halved while E exceeds E0 + ls_tol (|E0| + 1)
+            // (ls_halve_kernel, solver.py:63-73). The trial points lie within alpha |p|_inf of x,
+            // which S.motion already counts, so one candidate-list check before the first trial
+            // covers them all (a rebuild there is at x; the far cap keeps alpha |p|_inf within
+            // 0.45 reach < skin / 2 of it).
+            if (d.line_search) {
+                float2 *__restrict__ R0 = reinterpret_cast<float2 *>(d.xu);
+                double *__restrict__ Q0 = d.xu + 2 * (size_t)d.N;
+                const double E0 = energy_mx();
+                for (int i = n0 + gt; i < n1; i += GS) R0[i] = XR[i];
+                for (int k = sg.aff0 * 6 + gt; k < (sg.aff0 + sg.naff) * 6; k += GS) Q0[k] = d.a_q[k];
+                if (scene_ipc) {
+                    const bool rebuild = S.rebuild || 2.0 * S.motion >= d.skin;
+                    ipc_refresh();
+                    if (rebuild) {  // rebuilt at x: the trial points are within alpha |p|_inf of it
+                        if (tid == 0) S.motion = S.alpha * (double)F.pinf;
+                        gsync();
+                    }
+                    ipc_far = S.dmin_c - 2.0 * S.motion >= d.reach;
+                }
+                gsync();
+                auto trial = [&]() {  // set_x_from_x0_kernel (solver.py:52-60) + affine_trial_kernel
+                    if (S.active) {
+                        const double al = S.alpha;
+                        const float alf = F.alpha;
+                        for (int k = sg.aff0 * 6 + gt; k < (sg.aff0 + sg.naff) * 6; k += GS)
+                            d.a_q[k] = Q0[k] + al * d.a_pq[k];
+                        if (sg.naff > 0) gsync();
+                        for (int i = n0 + gt; i < n1; i += GS) {
+                            if (NINFO[i].x & NI_AFF) {
+                                const int ka = d.node_aff[i];
+                                const double *w = d.a_w + 3 * ka, *q = d.a_q + 6 * d.a_grp[ka];
+                                const double2 xn = Xn[i], xb = XBd[i];
+                                const double jx = w[0] * q[0] + w[1] * q[1] + w[2] * q[2];
+                                const double jy = w[0] * q[3] + w[1] * q[4] + w[2] * q[5];
+                                XD[i] = make_float2((float)(jx - xn.x), (float)(jy - xn.y));
+                                XR[i] = make_float2((float)(jx - xb.x), (float)(jy - xb.y));
+                            } else {
+                                const float2 pp = P[i], r = R0[i], db = DB[i];
+                                const float2 rn = make_float2(r.x + alf * pp.x, r.y + alf * pp.y);
+                                XR[i] = rn;
+                                XD[i] = make_float2(db.x + rn.x, db.y + rn.y);
+                            }
+                        }
+                    }
+                    gsync();
+                };
+                for (int bt = 0; bt < d.n_backtrack; ++bt) {
+                    trial();
+                    const double E = energy_mx();
+                    if (tid == 0 && S.active && E > E0 + d.ls_tol * (dabs(E0) + 1.0)) { S.alpha *= 0.5; F.alpha *= 0.5f; }
+                    gsync();
+                }
+                trial();
+                if (tid == 0 && S.active && sg.nrig == 1) {
+                    S.csx += S.alpha * (double)F.mpx;
+                    S.csy += S.alpha * (double)F.mpy;
+                    F.csx = (float)S.csx;
+                    F.csy = (float)S.csy;
+                }
+                gsync();
+            } else {
                 const bool act = S.active != 0;
-                const float al = (float)S.alpha;
+                const float al = F.alpha;
                 for (int i = n0 + gt; i < n1; i += GS) {
                     if (NINFO[i].x & NI_AFF) {
                         const int ka = d.node_aff[i];

@@ -331,11 +331,9 @@ class DeviceSolver:
         d.blocks_per_sm = int(blocks_per_sm or 0)
         d.blocks_per_scene = int(blocks_per_scene or 0)
         if int(sc.get("line_search", 0)):
-            if self.mixed:
-                raise NotImplementedError("the energy line search runs in FP64 only (precision='fp64')")
-            if n_aff:
-                raise NotImplementedError("the energy line search with affine bodies is not in this build")
-            self._t["xu"] = torch.zeros((N, 2), dtype=torch.float64, device=self.dev)
+            # saved positions (FP64 pairs; the mixed kernel keeps its FP32 offsets there), then
+            # the affine bodies' coordinates
+            self._t["xu"] = torch.zeros(2 * N + 6 * n_aff, dtype=torch.float64, device=self.dev)
             d.xu = self._t["xu"].data_ptr()
             d.line_search, d.n_backtrack, d.ls_tol = 1, int(sc.get("n_bt", 4)), float(sc.get("ls_tol", 1e-7))
         h = C.c_void_p()

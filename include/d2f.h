@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define D2F_ABI_VERSION 6
+#define D2F_ABI_VERSION 7
 
 /* status codes */
 #define D2F_OK 0
@@ -69,7 +69,8 @@ typedef struct d2f_scene_desc {
     const d2f_seg *segs;         /* n_scenes */
     /* node state */
     double *x, *v, *xn, *xhat;   /* N x 2 */
-    double *xu;                  /* N x 2: the line search's saved positions (NULL without it) */
+    double *xu;                  /* 2 N + 6 n_aff doubles: the line search's saved state (positions,
+                                    then affine coordinates; NULL without it) */
     const double *xrest;         /* N x 2: rest positions (mixed precision; else NULL) */
     void *grad, *grad_prev, *p, *diagH, *diag_el; /* N x 2 real */
     const double *mass;          /* N */
@@ -131,8 +132,9 @@ typedef struct d2f_scene_desc {
                                     scenes per SM, else 128) */
     int32_t blocks_per_sm;       /* resident scene blocks per SM the register budget targets
                                     (0: the library's default for that width) */
-    /* backtracking energy line search (PNCG2DSolver line_search, solver.py:397-425): FP64
-       solvers without affine bodies; needs xu */
+    /* backtracking energy line search (PNCG2DSolver line_search, solver.py:397-425; with
+       affine bodies AffineBodies.save/trial, affine.py:383-389): both precisions, the energy
+       summed in FP64 per scene; needs xu */
     double ls_tol;               /* accept while E <= E0 + ls_tol (|E0| + 1) */
     int32_t line_search;         /* 0 off, 1 on */
     int32_t n_backtrack;         /* halvings tried per iteration */
@@ -246,22 +248,29 @@ int32_t d2f_step_noalloc(const d2f_scene_desc *desc, void *stream);
  *
  * Solve, per scene, the transposed linearised step system at the converged positions x_lin
  * (N x 2, device):
- *     (M + h^2 (K_elastic + K_collider + K_tendon)) lam = rhs      on the free DOFs,
- * with the collider contact gate frozen at x_lin and friction left out, by Jacobi-
- * preconditioned CG run on the device, one thread block per scene. `rhs` (N x 2) is read on
- * the free DOFs only; `lam` (N x 2) gets the solution, zero on the kinematic DOFs; with
- * warm_start != 0 the CG starts from the `lam` passed in (e.g. the next step's adjoint,
- * which a step's adjoint is close to), else from zero. `work`
- * is 10 N doubles of scratch. `tension` (n_ten, device, or NULL = desc->t_Tcmd) is the
- * tension of each tension-controlled tendon at this step. A scene stops when
- * |r| <= rtol |rhs| or after max_iter iterations; per scene, `iters` (device, n_scenes)
- * gets the iterations and `status` (device, n_scenes) 0 (converged), 1 (max_iter reached)
- * or D2F_ENAN (the operator was not positive along a search direction). The handle's
- * per-triangle scratch (escr, ecache) is overwritten: call between steps, not during one.
- * Refused (D2F_EINVAL) for mixed-precision solvers, IPC contact between bodies and affine
- * bodies, which the operator has no tangent for.
+ *     (M + h^2 (K_elastic + K_collider + K_tendon + K_spring + K_pressure + K_ipc)) lam = rhs
+ * on the free DOFs, with the collider contact gate and the set of active IPC barrier terms
+ * frozen at x_lin and friction left out, by preconditioned CG run on the device, one thread
+ * block per scene. Affine bodies enter in their reduced coordinates: the system is
+ * S^T H S + h^2 K_A with x = J q on a body's nodes and K_A its exact elastic block at its A
+ * (recovered from x_lin), preconditioned per body by the inverse of its 6x6 block; lam is
+ * J lam_q on the body's nodes. `rhs` (N x 2) is read on the free DOFs only; `lam` (N x 2)
+ * gets the solution, zero on the kinematic DOFs; with warm_start != 0 the CG starts from the
+ * `lam` passed in (e.g. the next step's adjoint, which a step's adjoint is close to), else
+ * from zero. `work` is d2f_adjoint_work_doubles(s) doubles of scratch. `tension` (n_ten,
+ * device, or NULL = desc->t_Tcmd) is the tension of each tension-controlled tendon at this
+ * step. A scene stops when |r| <= rtol |rhs| or after max_iter iterations; per scene,
+ * `iters` (device, n_scenes) gets the iterations and `status` (device, n_scenes) 0
+ * (converged), 1 (max_iter reached), D2F_ENAN (the operator was not positive along a search
+ * direction) or D2F_ECAP (more active IPC pairs than the scene's candidate capacity). The
+ * handle's per-triangle scratch (escr, ecache) is overwritten: call between steps, not
+ * during one. Refused (D2F_EINVAL) for mixed-precision solvers.
  * Replaces AdjointPNCG2D.adjoint_solve (implicit/adjoint.py:339-369), whose MINRES runs on
- * the host and crosses to the device twice per matrix-vector product. */
+ * the host and crosses to the device twice per matrix-vector product; the reference refuses
+ * IPC contact and affine bodies (:372-385). */
+/* Doubles of scratch d2f_adjoint_solve needs for this solver: 12 N, plus 24 per IPC
+ * candidate slot, plus 112 per affine body. */
+int64_t d2f_adjoint_work_doubles(const d2f_solver *s);
 int32_t d2f_adjoint_solve(d2f_solver *s, const double *x_lin, const double *rhs, double *lam, double *work,
                           const double *tension, double rtol, int32_t max_iter, int32_t warm_start, int32_t *iters,
                           int32_t *status, void *stream);
