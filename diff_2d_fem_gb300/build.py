@@ -2,8 +2,8 @@
 
     python -m diff_2d_fem_gb300.build
 
-Six translation units (FP64 step kernels, mixed step kernels, mixed cluster kernels, C ABI, adjoint kernels,
-read-out kernels) compiled in parallel, one
+Seven translation units (FP64 step kernels, mixed step kernels with every term, mixed step kernels with
+reduced feature sets, mixed cluster kernels, C ABI, adjoint kernels, read-out kernels) compiled in parallel, one
 -gencode (sm_103a), no CMake. The library lands in
 diff_2d_fem_gb300/_build/libd2f.so and is rebuilt when a source is newer than it.
 """
@@ -18,8 +18,8 @@ ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libd2f.so")
 CSRC = os.path.join(HERE, "csrc")
-SOURCES = [os.path.join(CSRC, f) for f in ("pncg_fp64.cu", "pncg_mixed.cu", "pncg_mixed_cluster.cu", "d2f_capi.cu", "adjoint.cu",
-                                               "readouts.cu")]
+SOURCES = [os.path.join(CSRC, f) for f in ("pncg_fp64.cu", "pncg_mixed.cu", "pncg_mixed_feat.cu", "pncg_mixed_cluster.cu",
+                                               "d2f_capi.cu", "adjoint.cu", "readouts.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("pncg_kernel.cuh", "pncg_mixed_kernel.cuh", "d2f_math.cuh", "d2f_solver.h")] + [
                   os.path.join(ROOT, "include", "d2f.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -30,6 +30,13 @@ __device__ __forceinline__ double wsum(double v) {
     return v;
 }
 
+// the warp's sum in every lane (butterfly)
+__device__ __forceinline__ double wsum_all(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // deterministic block sum of NV values (fixed tree), result to every thread
 template <int NT, int NV>
 __device__ __forceinline__ void bsum(double (&v)[NV], double *red) {
@@ -251,7 +258,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
     double2 *__restrict__ DI = R + 4 * N;
     double2 *__restrict__ EX = R + 5 * N;                       // P with the affine nodes' J p_q
     double *__restrict__ PB = work + 12 * (size_t)N;            // IPC pair blocks, 24 a candidate slot
-    double *__restrict__ QB = PB + 24 * (size_t)d.cand_total;   // affine bodies, QW each
+    double *__restrict__ QB = PB + (d.Ne > 0 ? 24 * (size_t)d.cand_total : 0);   // affine bodies, QW each
     const double4_32a *__restrict__ Bm = reinterpret_cast<const double4_32a *>(d.Bm);
     const double *__restrict__ Ar = reinterpret_cast<const double *>(d.area);
     const double *__restrict__ Mu = reinterpret_cast<const double *>(d.mu);
@@ -412,7 +419,7 @@ __global__ void __launch_bounds__(NT) pcg_kernel(const __grid_constant__ d2f_sce
                     v[0] += w[0] * a.x; v[1] += w[1] * a.x; v[2] += w[2] * a.x;
                     v[3] += w[0] * a.y; v[4] += w[1] * a.y; v[5] += w[2] * a.y;
                 }
-                for (int q = 0; q < 6; ++q) v[q] = wsum(v[q]);
+                for (int q = 0; q < 6; ++q) v[q] = wsum_all(v[q]);  // lanes 0-5 each write one
                 if (lane < 6) {
                     double kp = 0.0;
                     for (int q = 0; q < 6; ++q) kp += qb[Q_K + 6 * lane + q] * qb[Q_P + q];

@@ -42,7 +42,7 @@ int d2f_default_threads(const d2f_scene_desc &d) {
 }
 
 static int occupancy(const d2f_scene_desc &d, int smem, int vnt, int vminb) {
-    return d.precision == D2F_MIXED ? d2f::occupancy_mixed(vnt, vminb, smem) : d2f::occupancy_fp64(vnt, vminb, smem);
+    return d.precision == D2F_MIXED ? d2f::occupancy_mixed(vnt, vminb, smem, d2f::mixed_features(d)) : d2f::occupancy_fp64(vnt, vminb, smem);
 }
 
 extern "C" {

@@ -1402,7 +1402,21 @@ namespace d2f {
 cudaError_t launch_fp64(int nt, int minb, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st);
 cudaError_t launch_mixed(int nt, int minb, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st);
 int occupancy_fp64(int nt, int minb, int smem);
-int occupancy_mixed(int nt, int minb, int smem);
+int occupancy_mixed(int nt, int minb, int smem, int feat);
+// The mixed batch kernel's feature sets. Bit 0: contact between bodies (IPC); bit 1: affine
+// bodies, tendons, springs, pressure and the line search. A batch runs the smallest set that
+// covers it: code for terms a batch does not have still costs registers, and the batch kernel
+// runs at 80-128 registers a thread, where the live values the rare paths add spill in the
+// hot loop (measured at 256 threads: a 736-byte stack frame with every term, 240 without
+// bit 1, 32 with neither). Instantiated in pncg_mixed.cu (all) and pncg_mixed_feat.cu.
+enum : int { FEAT_IPC = 1, FEAT_RARE = 2, FEAT_ALL = 3 };
+inline int mixed_features(const d2f_scene_desc &d) {
+    int f = d.Ne > 0 ? FEAT_IPC : 0;
+    if (d.n_aff > 0 || d.n_ten > 0 || d.n_sp > 0 || d.n_pe > 0 || d.line_search) f = FEAT_ALL;
+    return f;
+}
+cudaError_t launch_mixed_feat(int feat, int nt, int minb, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st);
+int occupancy_mixed_feat(int feat, int nt, int minb, int smem);
 // threads per block of the cluster path (a block per SM: 16 warps to hide the latency of a
 // large scene's passes, 128 registers a thread)
 constexpr int kClusterThreads = 512;

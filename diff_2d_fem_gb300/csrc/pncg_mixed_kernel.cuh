@@ -88,18 +88,23 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
         for (int k = 0; k < NM; ++k) w[2 * NS + k] = m[k];
     }
     block_barrier();
-    // the per-warp partials: sum k by thread k (merged as compensated pairs, then one
-    // conversion to FP64: dependent FP64 operations are slow on this part), extremum k by
-    // thread NS + k
+    // the per-warp partials. Sum k: its NW pairs converted to FP64 (exactly) by NW adjacent
+    // lanes, q = lane within the group, and added in a fixed shuffle tree, so the FP64 sum
+    // costs one conversion and log2(NW) dependent additions (dependent FP64 operations are
+    // slow on this part); extremum j by thread SOFF + j (small blocks: thread j, after its sum).
     {
-        const int k = threadIdx.x;
-        if (k < NS) {
-            FF acc{fred[2 * k], fred[2 * k + 1]};
-            for (int q = 1; q < NW; ++q)
-                acc = ff_merge(acc, FF{fred[q * (2 * NS + NM) + 2 * k], fred[q * (2 * NS + NM) + 2 * k + 1]});
-            dres[k] = (double)acc.hi + (double)acc.lo;
-        } else if (k < NS + NM) {
-            const int j = k - NS;
+        constexpr int SOFF = ((NS * NW + 31) / 32) * 32;
+        const int t = threadIdx.x;
+        if (t < SOFF) {
+            const int k = t / NW, q = t % NW;
+            double v = 0.0;
+            if (t < NS * NW) v = (double)fred[q * (2 * NS + NM) + 2 * k] + (double)fred[q * (2 * NS + NM) + 2 * k + 1];
+#pragma unroll
+            for (int o = NW / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (q == 0 && t < NS * NW) dres[k] = v;
+        }
+        const int j = SOFF + NM <= NT ? t - SOFF : t;
+        if (j >= 0 && j < NM) {
             float a = fred[2 * NS + j];
             for (int q = 1; q < NW; ++q) {
                 const float b = fred[q * (2 * NS + NM) + 2 * NS + j];
@@ -385,7 +390,8 @@ __device__ __forceinline__ void rigid_precondition(const float *v, SceneF &F, do
 // one scene (large scenes): the scene's loops are spread over the cluster's threads, phases are
 // separated by cluster barriers, reductions combine the blocks' results through distributed
 // shared memory, and the per-scene scalars are kept, identically, by every block.
-template <int NT, int MINB, int CS = 1>
+// FEAT: the terms the kernel is compiled with (FEAT_IPC, FEAT_RARE; mixed_features).
+template <int NT, int MINB, int CS = 1, int FEAT = FEAT_ALL>
 __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_constant__ d2f_scene_desc d,
                                                               const __grid_constant__ MixedPtrs mp) {
     namespace cg = cooperative_groups;
@@ -423,7 +429,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     const double dhat = d.dhat;
     const float fh2 = (float)h2, fkappa = (float)d.kappa, fdhat = (float)dhat, fepsv = (float)d.epsv,
                 finv_dt = (float)inv_dt, feta = (float)d.ccd_eta;
-    const bool has_ipc = d.Ne > 0;
+    constexpr bool F_IPC = (FEAT & FEAT_IPC) != 0, F_RARE = (FEAT & FEAT_RARE) != 0;
+    const bool has_ipc = F_IPC && d.Ne > 0;
+    const bool line_search = F_RARE && d.line_search;
     const int n_col = d.n_col;
     // the stop tests' and caps' constants in FP32
     const bool use_gtol = d.gtol > 0.0, use_tolx = d.tol_x > 0.0, use_guard = d.cg_guard > 0.0;
@@ -485,7 +493,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             sc = sc_next;
         }
         if (sc >= d.n_scenes) break;
-        const d2f_seg sg = d.segs[sc];
+        d2f_seg sg = d.segs[sc];
+        if constexpr (!F_RARE) { sg.naff = 0; sg.naffn = 0; sg.nten = 0; sg.ntent = 0; sg.nsp = 0; sg.npe = 0; }
+        if constexpr (!F_IPC) sg.ne = 0;
         const int n0 = sg.node0, n1 = sg.node0 + sg.nn;
         const int t0 = sg.tri0, t1 = sg.tri0 + sg.nt;
         const bool scene_ipc = has_ipc && sg.ne > 0;
@@ -1986,7 +1996,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         if (scene_ipc) S.motion += S.alpha * (double)pinf;  // bound on any node's move
                         if (rig1) {                              // centroid shift, sum m dx / M
                             const float mx = (float)so[1] * F.inv_m, my = (float)so[2] * F.inv_m;
-                            if (d.line_search) {                 // added with the accepted step
+                            if (line_search) {                   // added with the accepted step
                                 F.mpx = mx;
                                 F.mpy = my;
                             } else {
@@ -1999,7 +2009,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     }
                 }
                 gsync();
-                if (sg.naff > 0 && S.active && !d.line_search) {  // AffineBodies.advance, affine.py:249-257: q += alpha p_q
+                if (sg.naff > 0 && S.active && !line_search) {  // AffineBodies.advance, affine.py:249-257: q += alpha p_q
                     for (int b = sg.aff0 + gt; b < sg.aff0 + sg.naff; b += GS)
                         for (int r = 0; r < 6; ++r) d.a_q[6 * b + r] += S.alpha * d.a_pq[6 * b + r];
                     gsync();
@@ -2014,7 +2024,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             // which S.motion already counts, so one candidate-list check before the first trial
             // covers them all (a rebuild there is at x; the far cap keeps alpha |p|_inf within
             // 0.45 reach < skin / 2 of it).
-            if (d.line_search) {
+            if (line_search) {
                 float2 *__restrict__ R0 = reinterpret_cast<float2 *>(d.xu);
                 double *__restrict__ Q0 = d.xu + 2 * (size_t)d.N;
                 const double E0 = energy_mx();
