@@ -218,6 +218,39 @@ static __device__ __noinline__ double accd_profile(double px, double py, double 
     return t;
 }
 
+// The same profile in FP32, on the pair's geometry taken relative to one of its nodes (so
+// the magnitudes are the pair's own, which FP32 resolves to ~1e-7 of them): the mixed step's
+// step cap between bodies. The search ends 10 % short of each measured distance and stops at
+// the margin g, which is far above that rounding. T = 3e38 when no contact within t_c0.
+__device__ __forceinline__ float seg_dist_f(float px, float py, float ax, float ay, float bx, float by) {
+    const float abx = bx - ax, aby = by - ay;
+    float t = ((px - ax) * abx + (py - ay) * aby) / fmaxf(abx * abx + aby * aby, 1.0e-30f);
+    t = fminf(fmaxf(t, 0.f), 1.f);
+    const float dx = (px - ax) - t * abx, dy = (py - ay) - t * aby;
+    return sqrtf(dx * dx + dy * dy);
+}
+static __device__ __noinline__ float accd_profile_f(float px, float py, float ax, float ay, float bx, float by,
+                                                    float dpx, float dpy, float dax, float day, float dbx, float dby,
+                                                    float g, float t_c0, float &T) {
+    const float mx = (dpx + dax + dbx) / 3.f, my = (dpy + day + dby) / 3.f;
+    dpx -= mx; dpy -= my; dax -= mx; day -= my; dbx -= mx; dby -= my;
+    const float lp = sqrtf(dpx * dpx + dpy * dpy) + fmaxf(sqrtf(dax * dax + day * day), sqrtf(dbx * dbx + dby * dby));
+    T = 3.0e38f;
+    if (lp <= 1.0e-30f) return t_c0;
+    float d = seg_dist_f(px, py, ax, ay, bx, by);
+    float t = 0.f, tl = (d - g) / lp;
+    for (int k = 0; k < 32; ++k) {
+        const float tn = t + tl;
+        if (tn >= t_c0) return t_c0;
+        d = seg_dist_f(px + tn * dpx, py + tn * dpy, ax + tn * dax, ay + tn * day, bx + tn * dbx, by + tn * dby);
+        if (k > 0 && d < g) { T = tn; return t; }
+        t = tn;
+        tl = 0.9f * d / lp;
+    }
+    T = t;
+    return t;
+}
+
 // ---- Neo-Hookean on a 2x2 (FP64), core/math.py:75-93: used by the affine blocks
 struct M2 { double a, b, c, d; };
 __device__ __forceinline__ double det2(M2 A) { return A.a * A.d - A.c * A.b; }

@@ -18,7 +18,11 @@
 //   * inertia: x - x_hat = dx - dt e^(-dt c) v with dx = (x_b - x_n) + r in FP32;
 //   * half-space colliders: phi = phi0 + n.dx with phi0 = n.(x_n - c) in FP64 per step,
 //     so the barrier distance keeps FP64 accuracy near contact; other collider shapes,
-//     IPC pairs, tendons and affine bodies evaluate in FP64 from x_b + r;
+//     tendons and affine bodies evaluate in FP64 from x_b + r;
+//   * contact between bodies: each candidate pair's geometry relative to one of its nodes
+//     (FP64 differences of the base positions, rounded once, plus the FP32 offsets), its
+//     barrier, friction and ACCD profile in FP32; a pair with a term closer than 1e-3 d-hat
+//     (the barrier near its singularity) in FP64;
 //   * friction: slip velocity dx / dt;
 //   * rigid modes: arms a = (x_n - c_n) + dx - (c - c_n).
 //   * dot products: each thread accumulates its FP32 products with compensated (TwoSum)
@@ -947,148 +951,280 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             const double2 t = Tgt[b], x = xpos(n);
             return make_double2(t.x - x.x, t.y - x.y);
         };
-        // IPC pairs (ipc_pair_kernel + _pair, ipc_contact.py:130-296) in FP64 at x_n + dx
-        auto ipc_pairs = [&](int mode, double &acc_pHp, double t_c) {
-            if (ipc_far) return;  // every pair out of reach: no term, no cap
+        // One candidate pair in FP64 at x_b + r (ipc_pair_kernel + _pair, ipc_contact.py:130-296);
+        // mode 0: gradient and diagonal, 1: curvature along p and the ACCD profile, 2: energy,
+        // 3: the kinematic sweep's ACCD profile
+        auto pair64 = [&](int c, int mode, double &acc_pHp, double t_c) {
             const double idhat = d.ipc_dhat, ikappa = d.ipc_kappa, reach = d.reach, gap = d.gap;
             const double dlo = 1.0e-9 * idhat, onset = 0.02 * idhat;
             const double mu_s = d.friction ? d.ipc_mu : 0.0;
             const int per_body = d.friction ? d.per_body : 0;
             const double floor_ = d.bc_floor * idhat;
+            const unsigned packed = (unsigned)d.cand[sg.cand0 + c];
+            const int k = (int)(packed >> 16), j = (int)(packed & 0xffffu);
+            const int ge = sg.edge0 + k;
+            const int a = d.ea[ge], b = d.eb[ge], pn = d.bnd[sg.bnd0 + j];
+            const double2 xa = xpos(a), xb = xpos(b), xp = xpos(pn);
+            const double abx = xb.x - xa.x, aby = xb.y - xa.y;
+            const double L2 = dmax(abx * abx + aby * aby, 1.0e-30), Ll = sqrt(L2);
+            const double wx = xp.x - xa.x, wy = xp.y - xa.y;
+            const double tt = (wx * abx + wy * aby) / L2;
+            double dvx = wx - tt * abx, dvy = wy - tt * aby;
+            if (tt <= 0.0) { dvx = wx; dvy = wy; }
+            else if (tt >= 1.0) { dvx = xp.x - xb.x; dvy = xp.y - xb.y; }
+            const double dd = sqrt(dvx * dvx + dvy * dvy);
+            if (!(dd < reach)) {
+                if (mode == 1 || mode == 3) Ctr[sg.cand0 + c] = make_double2(1.0e300, 1.0e300);
+                return;
+            }
+            if (mode == 1 || mode == 3) {
+                double keep = dmax(gap * dd, idhat - onset);
+                if (dd < idhat) keep = dd - dmin(2.0 * (idhat - dd) + onset, 0.5 * dd);
+                if (mode == 3) keep = dmin(dd, dmax(gap * dd, floor_));
+                double2 qp, qa, qb;
+                if (mode == 3) { qp = kin_dir(pn); qa = kin_dir(a); qb = kin_dir(b); }
+                else {
+                    const float2 u0 = P[pn], u1 = P[a], u2 = P[b];
+                    qp = make_double2(u0.x, u0.y); qa = make_double2(u1.x, u1.y); qb = make_double2(u2.x, u2.y);
+                }
+                double T;
+                const double Rv = accd_profile(xp.x, xp.y, xa.x, xa.y, xb.x, xb.y, qp.x, qp.y, qa.x, qa.y,
+                                               qb.x, qb.y, keep, t_c, T);
+                Ctr[sg.cand0 + c] = make_double2(T, Rv);
+            }
+            if (mode == 3) return;
+            double mu_p = mu_s;
+            if (per_body) {
+                const double mi = d.mu_node[pn], mj = d.mu_node[a], sm = mi + mj;
+                mu_p = sm > 0.0 ? 2.0 * mi * mj / sm : 0.0;
+            }
+            auto term = [&](double coef, int ip, int ia, int ib, double wa, double wb, double dist, double nx,
+                            double ny, double ddd) {
+                const double bp = barrier_bp<double>(dist, idhat);
+                const double f_n = -ikappa * bp;
+                const double tnx = -ny, tny = nx;
+                const float2 di = XD[ip], da = XD[ia], db = XD[ib];  // slip since the step began
+                const double ux = (double)di.x - wa * (double)da.x - wb * (double)db.x;
+                const double uy = (double)di.y - wa * (double)da.y - wb * (double)db.y;
+                const double ut = ux * tnx + uy * tny;
+                const double vt = dabs(ut) * inv_dt;
+                const double kt = mu_p * f_n * inv_dt / dmax(vt, d.epsv);
+                if (mode == 0) {
+                    const double bpp = barrier_bpp<double>(dist, idhat);
+                    const double s = mu_p * f_n * (ut * inv_dt / dmax(vt, d.epsv));
+                    const double gx = h2 * (-f_n * nx + s * tnx), gy = h2 * (-f_n * ny + s * tny);
+                    const double hx = h2 * (ikappa * bpp * nx * nx + kt * tnx * tnx);
+                    const double hy = h2 * (ikappa * bpp * ny * ny + kt * tny * tny);
+                    const int ids[3] = {ip, ia, ib};
+                    const double cg[3] = {coef, -coef * wa, -coef * wb};
+                    const double ch[3] = {coef, coef * wa * wa, coef * wb * wb};
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        const int n = ids[q];
+                        const uint8_t fm = d.free_mask[n];
+                        float *gp_ = reinterpret_cast<float *>(G + n);
+                        float *dp_ = reinterpret_cast<float *>(D + n);
+                        if (fm & 1) atomicAdd(gp_, (float)(cg[q] * gx));
+                        if (fm & 2) atomicAdd(gp_ + 1, (float)(cg[q] * gy));
+                        atomicAdd(dp_, (float)(ch[q] * hx));
+                        atomicAdd(dp_ + 1, (float)(ch[q] * hy));
+                    }
+                } else if (mode == 2) {  // energy: barrier + lagged friction (ipc_contact.py:414-429)
+                    const double asl = d.epsv / inv_dt, au = dabs(ut);
+                    const double f0 = au < asl ? au * au / (2.0 * asl) : au - 0.5 * asl;
+                    acc_pHp += coef * h2 * (ikappa * barrier_b<double>(dist, idhat) + mu_p * f_n * f0);
+                } else {
+                    const double bpp = barrier_bpp<double>(dist, idhat);
+                    const float2 u0 = P[ip], u1 = P[ia], u2 = P[ib];
+                    const double qx = (double)u0.x - wa * (double)u1.x - wb * (double)u2.x;
+                    const double qy = (double)u0.y - wa * (double)u1.y - wb * (double)u2.y;
+                    const double dn = qx * nx + qy * ny, dt_ = qx * tnx + qy * tny;
+                    const double val = dmax(ikappa * (bpp * dn * dn + bp * ddd), 0.0);
+                    acc_pHp += coef * h2 * (val + kt * dt_ * dt_);
+                }
+            };
+            if (tt > 0.0 && tt < 1.0 && dd < idhat) {
+                const double dist = dmax(dd, dlo);
+                double ddd = 0.0;
+                if (mode == 1) {
+                    const float2 pb_ = P[b], pa_ = P[a], pp_ = P[pn];
+                    const double dex = (double)pb_.x - (double)pa_.x, dey = (double)pb_.y - (double)pa_.y;
+                    const double dwx = (double)pp_.x - (double)pa_.x, dwy = (double)pp_.y - (double)pa_.y;
+                    const double c0 = abx * wy - aby * wx;
+                    const double c1 = (dex * wy - dey * wx) + (abx * dwy - aby * dwx);
+                    const double c2 = 2.0 * (dex * dwy - dey * dwx);
+                    const double L1 = (abx * dex + aby * dey) / Ll;
+                    const double Lq = ((dex * dex + dey * dey) - L1 * L1) / Ll;
+                    const double s0 = c0 / Ll;
+                    const double s1 = (c1 - s0 * L1) / Ll;
+                    ddd = (c2 - 2.0 * s1 * L1 - s0 * Lq) / Ll;
+                    if (c0 < 0.0) ddd = -ddd;
+                }
+                term(1.0, pn, a, b, 1.0 - tt, tt, dist, dvx / dist, dvy / dist, ddd);
+            }
+            double coef_a = -d.ca[ge];
+            if (tt <= 0.0) coef_a += 1.0;
+            double d_a = sqrt(wx * wx + wy * wy);
+            if (coef_a != 0.0 && d_a < idhat) {
+                d_a = dmax(d_a, dlo);
+                const double nx = wx / d_a, ny = wy / d_a;
+                double ddd = 0.0;
+                if (mode == 1) {
+                    const float2 pp_ = P[pn], pa_ = P[a];
+                    const double dwx = (double)pp_.x - (double)pa_.x, dwy = (double)pp_.y - (double)pa_.y;
+                    const double dn = dwx * nx + dwy * ny;
+                    ddd = ((dwx * dwx + dwy * dwy) - dn * dn) / d_a;
+                }
+                term(coef_a, pn, a, b, 1.0, 0.0, d_a, nx, ny, ddd);
+            }
+            double coef_b = -d.cb[ge];
+            if (tt >= 1.0) coef_b += 1.0;
+            const double wbx = xp.x - xb.x, wby = xp.y - xb.y;
+            double d_b = sqrt(wbx * wbx + wby * wby);
+            if (coef_b != 0.0 && d_b < idhat) {
+                d_b = dmax(d_b, dlo);
+                const double nx = wbx / d_b, ny = wby / d_b;
+                double ddd = 0.0;
+                if (mode == 1) {
+                    const float2 pp_ = P[pn], pb_ = P[b];
+                    const double dwx = (double)pp_.x - (double)pb_.x, dwy = (double)pp_.y - (double)pb_.y;
+                    const double dn = dwx * nx + dwy * ny;
+                    ddd = ((dwx * dwx + dwy * dwy) - dn * dn) / d_b;
+                }
+                term(coef_b, pn, a, b, 0.0, 1.0, d_b, nx, ny, ddd);
+            }
+        };
+        auto ipc_pairs = [&](int mode, double &acc_pHp, double t_c) {
+            if (ipc_far) return;  // every pair out of reach: no term, no cap
+            const int nc = S.ncand;
+            for (int c = gt; c < nc; c += GS) pair64(c, mode, acc_pHp, t_c);
+        };
+        // Modes 0 and 1 of the pair pass in FP32: the barrier and friction arithmetic and the
+        // ACCD profile on the pair's geometry taken relative to node a — the FP64 differences of
+        // the base positions, rounded once, plus the FP32 offsets — which resolves the pair's own
+        // magnitudes (~d-hat) to ~1e-7 of them. A pair with a term closer than 1e-3 d-hat, where
+        // the barrier nears its singularity, takes the FP64 pass (pair64). Mode 1's curvature
+        // goes to the compensated pair accf, the FP64 fallback's to acc64.
+        auto ipc_pairs32 = [&](int mode, FF &accf, double &acc64, float t_c) {
+            if (ipc_far) return;  // every pair out of reach: no term, no cap
+            const float idhat = (float)d.ipc_dhat, ikappa = (float)d.ipc_kappa, reach = (float)d.reach;
+            const float gap = (float)d.gap, dlo = 1.0e-9f * idhat, onset = 0.02f * idhat, dnear = 1.0e-3f * idhat;
+            const float mu_s = d.friction ? (float)d.ipc_mu : 0.f;
+            const int per_body = d.friction ? d.per_body : 0;
             const int nc = S.ncand;
             for (int c = gt; c < nc; c += GS) {
                 const unsigned packed = (unsigned)d.cand[sg.cand0 + c];
                 const int k = (int)(packed >> 16), j = (int)(packed & 0xffffu);
                 const int ge = sg.edge0 + k;
                 const int a = d.ea[ge], b = d.eb[ge], pn = d.bnd[sg.bnd0 + j];
-                const double2 xa = xpos(a), xb = xpos(b), xp = xpos(pn);
-                const double abx = xb.x - xa.x, aby = xb.y - xa.y;
-                const double L2 = dmax(abx * abx + aby * aby, 1.0e-30), Ll = sqrt(L2);
-                const double wx = xp.x - xa.x, wy = xp.y - xa.y;
-                const double tt = (wx * abx + wy * aby) / L2;
-                double dvx = wx - tt * abx, dvy = wy - tt * aby;
-                if (tt <= 0.0) { dvx = wx; dvy = wy; }
-                else if (tt >= 1.0) { dvx = xp.x - xb.x; dvy = xp.y - xb.y; }
-                const double dd = sqrt(dvx * dvx + dvy * dvy);
+                const double2 ba = XBd[a], bb = XBd[b], bp = XBd[pn];
+                const float2 ra = XR[a], rb = XR[b], rp = XR[pn];
+                const float abx = (float)(bb.x - ba.x) + (rb.x - ra.x), aby = (float)(bb.y - ba.y) + (rb.y - ra.y);
+                const float wx = (float)(bp.x - ba.x) + (rp.x - ra.x), wy = (float)(bp.y - ba.y) + (rp.y - ra.y);
+                const float L2 = fmaxf(abx * abx + aby * aby, 1.0e-30f), Ll = sqrtf(L2);
+                const float tt = (wx * abx + wy * aby) / L2;
+                float dvx = wx - tt * abx, dvy = wy - tt * aby;
+                const float wbx = wx - abx, wby = wy - aby;
+                if (tt <= 0.f) { dvx = wx; dvy = wy; }
+                else if (tt >= 1.f) { dvx = wbx; dvy = wby; }
+                const float dd = sqrtf(dvx * dvx + dvy * dvy);
                 if (!(dd < reach)) {
-                    if (mode == 1 || mode == 3) Ctr[sg.cand0 + c] = make_double2(1.0e300, 1.0e300);
+                    if (mode == 1) Ctr[sg.cand0 + c] = make_double2(1.0e300, 1.0e300);
                     continue;
                 }
-                if (mode == 1 || mode == 3) {
-                    double keep = dmax(gap * dd, idhat - onset);
-                    if (dd < idhat) keep = dd - dmin(2.0 * (idhat - dd) + onset, 0.5 * dd);
-                    if (mode == 3) keep = dmin(dd, dmax(gap * dd, floor_));
-                    double2 qp, qa, qb;
-                    if (mode == 3) { qp = kin_dir(pn); qa = kin_dir(a); qb = kin_dir(b); }
-                    else {
-                        const float2 u0 = P[pn], u1 = P[a], u2 = P[b];
-                        qp = make_double2(u0.x, u0.y); qa = make_double2(u1.x, u1.y); qb = make_double2(u2.x, u2.y);
-                    }
-                    double T;
-                    const double Rv = accd_profile(xp.x, xp.y, xa.x, xa.y, xb.x, xb.y, qp.x, qp.y, qa.x, qa.y,
-                                                   qb.x, qb.y, keep, t_c, T);
-                    Ctr[sg.cand0 + c] = make_double2(T, Rv);
+                const float d_a = sqrtf(wx * wx + wy * wy), d_b = sqrtf(wbx * wbx + wby * wby);
+                if (fminf(dd, fminf(d_a, d_b)) < dnear) {  // near the barrier's singularity: FP64
+                    pair64(c, mode, acc64, (double)t_c);
+                    continue;
                 }
-                if (mode == 3) continue;
-                double mu_p = mu_s;
+                const float2 pp_ = P[pn], pa_ = P[a], pb_ = P[b];
+                if (mode == 1) {  // ACCD profile (ipc_contact.py:94-127), the FP64 pass's margins
+                    float keep = fmaxf(gap * dd, idhat - onset);
+                    if (dd < idhat) keep = dd - fminf(2.f * (idhat - dd) + onset, 0.5f * dd);
+                    float T;
+                    const float Rv = accd_profile_f(wx, wy, 0.f, 0.f, abx, aby, pp_.x, pp_.y, pa_.x, pa_.y, pb_.x, pb_.y,
+                                                    keep, t_c, T);
+                    Ctr[sg.cand0 + c] = make_double2(T >= 3.0e38f ? 1.0e300 : (double)T, (double)Rv);
+                }
+                float mu_p = mu_s;
                 if (per_body) {
-                    const double mi = d.mu_node[pn], mj = d.mu_node[a], sm = mi + mj;
-                    mu_p = sm > 0.0 ? 2.0 * mi * mj / sm : 0.0;
+                    const float mi = (float)d.mu_node[pn], mj = (float)d.mu_node[a], sm = mi + mj;
+                    mu_p = sm > 0.f ? 2.f * mi * mj / sm : 0.f;
                 }
-                auto term = [&](double coef, int ip, int ia, int ib, double wa, double wb, double dist, double nx,
-                                double ny, double ddd) {
-                    const double bp = barrier_bp<double>(dist, idhat);
-                    const double f_n = -ikappa * bp;
-                    const double tnx = -ny, tny = nx;
-                    const float2 di = XD[ip], da = XD[ia], db = XD[ib];  // slip since the step began
-                    const double ux = (double)di.x - wa * (double)da.x - wb * (double)db.x;
-                    const double uy = (double)di.y - wa * (double)da.y - wb * (double)db.y;
-                    const double ut = ux * tnx + uy * tny;
-                    const double vt = dabs(ut) * inv_dt;
-                    const double kt = mu_p * f_n * inv_dt / dmax(vt, d.epsv);
+                auto term = [&](float coef, int ia, int ib, float wa, float wb, float dist, float nx, float ny, float ddd) {
+                    const float bp1 = barrier_bp<float>(dist, idhat), bpp = barrier_bpp<float>(dist, idhat);
+                    const float f_n = -ikappa * bp1;
+                    const float tnx = -ny, tny = nx;
+                    const float2 di = XD[pn], da = XD[ia], db = XD[ib];  // slip since the step began
+                    const float ux = di.x - wa * da.x - wb * db.x, uy = di.y - wa * da.y - wb * db.y;
+                    const float ut = ux * tnx + uy * tny;
+                    const float vt = fabsf(ut) * finv_dt;
+                    const float kt = mu_p * f_n * finv_dt / fmaxf(vt, fepsv);
                     if (mode == 0) {
-                        const double bpp = barrier_bpp<double>(dist, idhat);
-                        const double s = mu_p * f_n * (ut * inv_dt / dmax(vt, d.epsv));
-                        const double gx = h2 * (-f_n * nx + s * tnx), gy = h2 * (-f_n * ny + s * tny);
-                        const double hx = h2 * (ikappa * bpp * nx * nx + kt * tnx * tnx);
-                        const double hy = h2 * (ikappa * bpp * ny * ny + kt * tny * tny);
-                        const int ids[3] = {ip, ia, ib};
-                        const double cg[3] = {coef, -coef * wa, -coef * wb};
-                        const double ch[3] = {coef, coef * wa * wa, coef * wb * wb};
+                        const float sf = mu_p * f_n * (ut * finv_dt / fmaxf(vt, fepsv));
+                        const float gx = fh2 * (-f_n * nx + sf * tnx), gy = fh2 * (-f_n * ny + sf * tny);
+                        const float hx = fh2 * (ikappa * bpp * nx * nx + kt * tnx * tnx);
+                        const float hy = fh2 * (ikappa * bpp * ny * ny + kt * tny * tny);
+                        const int ids[3] = {pn, ia, ib};
+                        const float cg[3] = {coef, -coef * wa, -coef * wb};
+                        const float ch[3] = {coef, coef * wa * wa, coef * wb * wb};
 #pragma unroll
                         for (int q = 0; q < 3; ++q) {
                             const int n = ids[q];
                             const uint8_t fm = d.free_mask[n];
                             float *gp_ = reinterpret_cast<float *>(G + n);
                             float *dp_ = reinterpret_cast<float *>(D + n);
-                            if (fm & 1) atomicAdd(gp_, (float)(cg[q] * gx));
-                            if (fm & 2) atomicAdd(gp_ + 1, (float)(cg[q] * gy));
-                            atomicAdd(dp_, (float)(ch[q] * hx));
-                            atomicAdd(dp_ + 1, (float)(ch[q] * hy));
+                            if (fm & 1) atomicAdd(gp_, cg[q] * gx);
+                            if (fm & 2) atomicAdd(gp_ + 1, cg[q] * gy);
+                            atomicAdd(dp_, ch[q] * hx);
+                            atomicAdd(dp_ + 1, ch[q] * hy);
                         }
-                    } else if (mode == 2) {  // energy: barrier + lagged friction (ipc_contact.py:414-429)
-                        const double asl = d.epsv / inv_dt, au = dabs(ut);
-                        const double f0 = au < asl ? au * au / (2.0 * asl) : au - 0.5 * asl;
-                        acc_pHp += coef * h2 * (ikappa * barrier_b<double>(dist, idhat) + mu_p * f_n * f0);
                     } else {
-                        const double bpp = barrier_bpp<double>(dist, idhat);
-                        const float2 u0 = P[ip], u1 = P[ia], u2 = P[ib];
-                        const double qx = (double)u0.x - wa * (double)u1.x - wb * (double)u2.x;
-                        const double qy = (double)u0.y - wa * (double)u1.y - wb * (double)u2.y;
-                        const double dn = qx * nx + qy * ny, dt_ = qx * tnx + qy * tny;
-                        const double val = dmax(ikappa * (bpp * dn * dn + bp * ddd), 0.0);
-                        acc_pHp += coef * h2 * (val + kt * dt_ * dt_);
+                        const float2 u1 = P[ia], u2 = P[ib];
+                        const float qx = pp_.x - wa * u1.x - wb * u2.x, qy = pp_.y - wa * u1.y - wb * u2.y;
+                        const float dn = qx * nx + qy * ny, dt_ = qx * tnx + qy * tny;
+                        const float val = fmaxf(ikappa * (bpp * dn * dn + bp1 * ddd), 0.f);
+                        ff_add(accf, coef * fh2 * (val + kt * dt_ * dt_));
                     }
                 };
-                if (tt > 0.0 && tt < 1.0 && dd < idhat) {
-                    const double dist = dmax(dd, dlo);
-                    double ddd = 0.0;
+                if (tt > 0.f && tt < 1.f && dd < idhat) {
+                    const float dist = fmaxf(dd, dlo);
+                    float ddd = 0.f;
                     if (mode == 1) {
-                        const float2 pb_ = P[b], pa_ = P[a], pp_ = P[pn];
-                        const double dex = (double)pb_.x - (double)pa_.x, dey = (double)pb_.y - (double)pa_.y;
-                        const double dwx = (double)pp_.x - (double)pa_.x, dwy = (double)pp_.y - (double)pa_.y;
-                        const double c0 = abx * wy - aby * wx;
-                        const double c1 = (dex * wy - dey * wx) + (abx * dwy - aby * dwx);
-                        const double c2 = 2.0 * (dex * dwy - dey * dwx);
-                        const double L1 = (abx * dex + aby * dey) / Ll;
-                        const double Lq = ((dex * dex + dey * dey) - L1 * L1) / Ll;
-                        const double s0 = c0 / Ll;
-                        const double s1 = (c1 - s0 * L1) / Ll;
-                        ddd = (c2 - 2.0 * s1 * L1 - s0 * Lq) / Ll;
-                        if (c0 < 0.0) ddd = -ddd;
+                        const float dex = pb_.x - pa_.x, dey = pb_.y - pa_.y;
+                        const float dwx = pp_.x - pa_.x, dwy = pp_.y - pa_.y;
+                        const float c0 = abx * wy - aby * wx;
+                        const float c1 = (dex * wy - dey * wx) + (abx * dwy - aby * dwx);
+                        const float c2 = 2.f * (dex * dwy - dey * dwx);
+                        const float L1 = (abx * dex + aby * dey) / Ll;
+                        const float Lq = ((dex * dex + dey * dey) - L1 * L1) / Ll;
+                        const float s0 = c0 / Ll, s1 = (c1 - s0 * L1) / Ll;
+                        ddd = (c2 - 2.f * s1 * L1 - s0 * Lq) / Ll;
+                        if (c0 < 0.f) ddd = -ddd;
                     }
-                    term(1.0, pn, a, b, 1.0 - tt, tt, dist, dvx / dist, dvy / dist, ddd);
+                    term(1.f, a, b, 1.f - tt, tt, dist, dvx / dist, dvy / dist, ddd);
                 }
-                double coef_a = -d.ca[ge];
-                if (tt <= 0.0) coef_a += 1.0;
-                double d_a = sqrt(wx * wx + wy * wy);
-                if (coef_a != 0.0 && d_a < idhat) {
-                    d_a = dmax(d_a, dlo);
-                    const double nx = wx / d_a, ny = wy / d_a;
-                    double ddd = 0.0;
+                float coef_a = -(float)d.ca[ge];
+                if (tt <= 0.f) coef_a += 1.f;
+                if (coef_a != 0.f && d_a < idhat) {
+                    const float dist = fmaxf(d_a, dlo), nx = wx / dist, ny = wy / dist;
+                    float ddd = 0.f;
                     if (mode == 1) {
-                        const float2 pp_ = P[pn], pa_ = P[a];
-                        const double dwx = (double)pp_.x - (double)pa_.x, dwy = (double)pp_.y - (double)pa_.y;
-                        const double dn = dwx * nx + dwy * ny;
-                        ddd = ((dwx * dwx + dwy * dwy) - dn * dn) / d_a;
+                        const float dwx = pp_.x - pa_.x, dwy = pp_.y - pa_.y, dn = dwx * nx + dwy * ny;
+                        ddd = ((dwx * dwx + dwy * dwy) - dn * dn) / dist;
                     }
-                    term(coef_a, pn, a, b, 1.0, 0.0, d_a, nx, ny, ddd);
+                    term(coef_a, a, b, 1.f, 0.f, dist, nx, ny, ddd);
                 }
-                double coef_b = -d.cb[ge];
-                if (tt >= 1.0) coef_b += 1.0;
-                const double wbx = xp.x - xb.x, wby = xp.y - xb.y;
-                double d_b = sqrt(wbx * wbx + wby * wby);
-                if (coef_b != 0.0 && d_b < idhat) {
-                    d_b = dmax(d_b, dlo);
-                    const double nx = wbx / d_b, ny = wby / d_b;
-                    double ddd = 0.0;
+                float coef_b = -(float)d.cb[ge];
+                if (tt >= 1.f) coef_b += 1.f;
+                if (coef_b != 0.f && d_b < idhat) {
+                    const float dist = fmaxf(d_b, dlo), nx = wbx / dist, ny = wby / dist;
+                    float ddd = 0.f;
                     if (mode == 1) {
-                        const float2 pp_ = P[pn], pb_ = P[b];
-                        const double dwx = (double)pp_.x - (double)pb_.x, dwy = (double)pp_.y - (double)pb_.y;
-                        const double dn = dwx * nx + dwy * ny;
-                        ddd = ((dwx * dwx + dwy * dwy) - dn * dn) / d_b;
+                        const float dwx = pp_.x - pb_.x, dwy = pp_.y - pb_.y, dn = dwx * nx + dwy * ny;
+                        ddd = ((dwx * dwx + dwy * dwy) - dn * dn) / dist;
                     }
-                    term(coef_b, pn, a, b, 0.0, 1.0, d_b, nx, ny, ddd);
+                    term(coef_b, a, b, 0.f, 1.f, dist, nx, ny, ddd);
                 }
             }
         };
@@ -1384,8 +1520,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             // ---------------------------------------------- A3: contact between bodies, tendons (FP64)
             if (scene_ipc) {
                 ipc_refresh();
+                FF zf{0.f, 0.f};
                 double z0 = 0.0;
-                ipc_pairs(0, z0, 0.0);
+                ipc_pairs32(0, zf, z0, 0.f);
                 gsync();
             }
             if (sg.nten > 0) {
@@ -1888,7 +2025,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         const M2 dA{pq[1], pq[2], pq[4], pq[5]}, A{q[1], q[2], q[4], q[5]};
                         acc_rare += h2 * dmax(ddot2(dA, nh_d2(A, dA, d.a_Mu[b], d.a_La[b])), 0.0);
                     }
-                    if (scene_ipc) ipc_pairs(1, acc_rare, d.alpha_max);
+                    if (scene_ipc) ipc_pairs32(1, acc_pHp, acc_rare, falpha_max);
                     for (int k = sg.sp0 + gt; k < sg.sp0 + sg.nsp; k += GS) {  // Springs.pHp, actuation.py:427-444
                         const int a = d.sp_a[k], b = d.sp_b[k];
                         const SpringAt sa = spring_at(xpos(a), b >= 0 ? xpos(b) : spring_anchor(d, k), d.sp_k[k], d.sp_L0[k]);
