@@ -1119,15 +1119,25 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int a = d.ea[ge], b = d.eb[ge], pn = d.bnd[sg.bnd0 + j];
                 const double2 ba = XBd[a], bb = XBd[b], bp = XBd[pn];
                 const float2 ra = XR[a], rb = XR[b], rp = XR[pn];
-                const float abx = (float)(bb.x - ba.x) + (rb.x - ra.x), aby = (float)(bb.y - ba.y) + (rb.y - ra.y);
-                const float wx = (float)(bp.x - ba.x) + (rp.x - ra.x), wy = (float)(bp.y - ba.y) + (rp.y - ra.y);
+                // base differences in FP64, rounded once; offsets since the base in FP32
+                const double abxb = bb.x - ba.x, abyb = bb.y - ba.y, wxb = bp.x - ba.x, wyb = bp.y - ba.y;
+                const float fabx = (float)abxb, faby = (float)abyb, fwx = (float)wxb, fwy = (float)wyb;
+                const float dabx = rb.x - ra.x, daby = rb.y - ra.y, dwx0 = rp.x - ra.x, dwy0 = rp.y - ra.y;
+                const float abx = fabx + dabx, aby = faby + daby;
+                const float wx = fwx + dwx0, wy = fwy + dwy0;
+                const float wbx = (float)(bp.x - bb.x) + (rp.x - rb.x), wby = (float)(bp.y - bb.y) + (rp.y - rb.y);
+                // cross(ab, w) = |ab| x the signed distance of p from the edge's line: the base
+                // product in FP64 and the increment in FP32, so the distance of a close pair keeps
+                // FP32's relative accuracy (w - t ab in FP32 would lose it to cancellation, by the
+                // ratio of the edge length to the distance)
+                const float cr = (float)(abxb * wyb - abyb * wxb) +
+                                 (((fabx * dwy0 - faby * dwx0) + (dabx * fwy - daby * fwx)) + (dabx * dwy0 - daby * dwx0));
                 const float L2 = fmaxf(abx * abx + aby * aby, 1.0e-30f), Ll = sqrtf(L2);
                 const float tt = (wx * abx + wy * aby) / L2;
-                float dvx = wx - tt * abx, dvy = wy - tt * aby;
-                const float wbx = wx - abx, wby = wy - aby;
-                if (tt <= 0.f) { dvx = wx; dvy = wy; }
-                else if (tt >= 1.f) { dvx = wbx; dvy = wby; }
-                const float dd = sqrtf(dvx * dvx + dvy * dvy);
+                float dd;
+                if (tt <= 0.f) dd = sqrtf(wx * wx + wy * wy);
+                else if (tt >= 1.f) dd = sqrtf(wbx * wbx + wby * wby);
+                else dd = fabsf(cr) / Ll;
                 if (!(dd < reach)) {
                     if (mode == 1) Ctr[sg.cand0 + c] = make_double2(1.0e300, 1.0e300);
                     continue;
@@ -1193,7 +1203,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     if (mode == 1) {
                         const float dex = pb_.x - pa_.x, dey = pb_.y - pa_.y;
                         const float dwx = pp_.x - pa_.x, dwy = pp_.y - pa_.y;
-                        const float c0 = abx * wy - aby * wx;
+                        const float c0 = cr;
                         const float c1 = (dex * wy - dey * wx) + (abx * dwy - aby * dwx);
                         const float c2 = 2.f * (dex * dwy - dey * dwx);
                         const float L1 = (abx * dex + aby * dey) / Ll;
@@ -1202,7 +1212,9 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         ddd = (c2 - 2.f * s1 * L1 - s0 * Lq) / Ll;
                         if (c0 < 0.f) ddd = -ddd;
                     }
-                    term(1.f, a, b, 1.f - tt, tt, dist, dvx / dist, dvy / dist, ddd);
+                    // the normal from the edge to the point: the edge's perpendicular on the point's side
+                    const float sgn = cr >= 0.f ? 1.f / Ll : -1.f / Ll;
+                    term(1.f, a, b, 1.f - tt, tt, dist, -aby * sgn, abx * sgn, ddd);
                 }
                 float coef_a = -(float)d.ca[ge];
                 if (tt <= 0.f) coef_a += 1.f;
