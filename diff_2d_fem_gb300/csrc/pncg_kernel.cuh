@@ -953,8 +953,10 @@ __global__ void __launch_bounds__(NT, MINB) pncg_step_kernel(const __grid_consta
                 }
             }
             if (sg.naff > 0) {
+                // written by the body entries' threads, read by the nodes' own threads in B1
                 block_barrier();
                 for (int k = sg.affn0 + tid; k < sg.affn0 + sg.naffn; k += NT) G[d.a_node[k]] = mk2<R>(R(0), R(0));
+                block_barrier();
             }
             // RigidModes.gather (affine.py:404-453): centroid, B^T g, B^T g_prev, B^T D' B
             if (tid == 0) { S.gPg = 0.0; S.g_Py = 0.0; S.y_Py = 0.0; }  // (only thread 0 uses these)

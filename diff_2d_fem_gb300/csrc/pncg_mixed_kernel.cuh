@@ -1681,8 +1681,12 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 }
             }
             if (sg.naff > 0) {
+                // the bodies' nodes take their direction from J p_q: their g leaves the node dots.
+                // The zeros are written by the body entries' threads (any block of a cluster) and
+                // read by the nodes' own threads in the next pass, hence the second barrier
                 gsync();
                 for (int k = sg.affn0 + gt; k < sg.affn0 + sg.naffn; k += GS) G[d.a_node[k]] = make_float2(0.f, 0.f);
+                gsync();
             }
             if (tid == 0) { F.gPg = 0.f; F.g_Py = 0.f; F.y_Py = 0.f; }
             // one rigid piece (a free soft body): its gather is folded into the Dai-Kou pass below;

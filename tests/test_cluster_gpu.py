@@ -4,7 +4,7 @@ the contact list compacted across the blocks in pair order, affine bodies spread
 cluster's warps and threads.
 
 Checked like the block-per-scene mixed path: on converged steps against FP64 (1e-6 relative
-to the coordinates on the reference fixtures; 1e-8 and the IPC energy to 1e-6 on the
+to the coordinates on the reference fixtures; 1e-8 and the IPC energy to 5e-6 on the
 contact-heavy state), and the library's default choice of clusters for a large scene.
 """
 import warnings
@@ -60,7 +60,8 @@ def test_cluster_matches_fp64_when_converged(name, cs):
 def test_cluster_contact_converged_matches_fp64():
     """The contact-heavy state (a block gripped between two pads: IPC pairs between bodies
     with friction, an affine body): one step run to convergence with a 16-block cluster,
-    within 1e-8 of FP64 and the IPC energy within 1e-6 relative. 40000 iterations: the mixed
+    within 1e-8 of FP64 and the IPC energy within 5e-6 relative (FP32 barrier forces between
+    bodies, as test_contact_batch explains). 40000 iterations: the mixed
     path's FP32 atomic sums make its approach to the answer vary from run to run on this
     ill-conditioned step (1.4e-8 to 4.6e-7 from FP64 seen after 20000 iterations, 2e-11 to
     3e-10 after 40000)."""
@@ -82,7 +83,7 @@ def test_cluster_contact_converged_matches_fp64():
     e64 = o.ipc_energy(xs["fp64"], x0)[0]
     emx = o.ipc_energy(xs["mixed"], x0)[0]
     assert e64 > 0.0
-    assert abs(emx - e64) / e64 < 1e-6
+    assert abs(emx - e64) / e64 < 5e-6
 
 
 def test_large_scenes_default_to_clusters():
