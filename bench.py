@@ -99,12 +99,13 @@ def algorithmic_bytes(prob, iters, mixed):
 
 # DRAM traffic of the step kernel per scene-iteration: dram__bytes_read.sum +
 # dram__bytes_write.sum of one ncu capture of one step of 608 scenes of this workload (after
-# one warm-up step), divided by that step's scene-iterations. keyed by precision:
-# (bytes per scene-iteration, launch shape captured). A launch's traffic is this times its
-# scene-iterations (traffic grows with the iterations each scene runs).
+# one warm-up step), divided by that step's scene-iterations, keyed by (precision, launch
+# shape): the resident scenes' working set, and so the L2 hit rate, depends on the blocks per
+# SM. A launch's traffic is this times its scene-iterations (traffic grows with the
+# iterations each scene runs); a launch shape without a capture reports none.
 TRAFFIC_PER_SCENE_ITER = {
-    "mixed": ((8.505456896e9 + 5.764890880e9) / (608 * 239.94736842105263), "256x3"),
-    "fp64": ((76.904082432e9 + 59.028497920e9) / (608 * 239.94078947368422), "256x2"),
+    ("mixed", "256x2"): (2.329572352e9 + 2.059303424e9) / (608 * 239.94572368421052),
+    ("fp64", "256x2"): (82.794049792e9 + 60.314018048e9) / (608 * 239.94078947368422),
 }
 
 
@@ -219,7 +220,8 @@ def _grads_at(args, dev, arms, max_iter=None, eps=None, fd_entries=32, h=1e-3, s
     `warm`), and its accuracy at the same settings: `fd_entries` entries (3/4 pixel moduli,
     1/4 step tensions), each in its own arm, perturbed relative by +/- h (stencil 2: central
     differences) or also +/- 2h (stencil 4: (8 (L(h) - L(-h)) - (L(2h) - L(-2h))) / 12h, error
-    O(h^4)) in more rollouts of the whole batch (arms are independent), against the adjoint
+    O(h^4)) and +/- 3h (stencil 6: (45 D1 - 9 D2 + D3) / 60h with Dk = L(kh) - L(-kh), error
+    O(h^6)) in more rollouts of the whole batch (arms are independent), against the adjoint
     gradient, relative to the entry or to 1 % of the largest checked entry for smaller ones.
     The forward steps and their replay run in mixed precision, the adjoint solves in FP64 at
     those states. max_iter / eps: the forward's iteration budget and energy-decrease
@@ -284,7 +286,10 @@ def _grads_at(args, dev, arms, max_iter=None, eps=None, fd_entries=32, h=1e-3, s
             ten[k, i] = ten0[k, i] * (1.0 + c)
         return rollout(T, 10, E, ten, False)[-1][:n_fd]
 
-    if stencil == 4:
+    if stencil == 6:
+        d1, d2, d3 = (perturbed_loss(k * h) - perturbed_loss(-k * h) for k in (1, 2, 3))
+        fd = (45.0 * d1 - 9.0 * d2 + d3) / (60 * h)
+    elif stencil == 4:
         fd = (8.0 * (perturbed_loss(h) - perturbed_loss(-h)) - (perturbed_loss(2 * h) - perturbed_loss(-2 * h))) / (12 * h)
     else:
         fd = (perturbed_loss(h) - perturbed_loss(-h)) / (2 * h)
@@ -316,13 +321,14 @@ def measure_grads(args, dev):
     the same settings. The headline runs every forward step to convergence (iteration budget
     --grad-iters, energy-decrease tolerance 1e-13): the adjoint differentiates the converged
     step (the implicit-function argument), so its gradient is the forward map's. The checked
-    entries use a 4-point stencil at h = 5e-2 (truncation O(h^4)): the converged forward
+    entries use a 6-point stencil at h = 5e-2 (truncation O(h^6)): the converged forward
     stops where its energy test first passes, which moves the positions by ~1e-10 from one
     perturbed run to the next, and central differences at h = 1e-3 amplify that past 1e-4 on
-    the smallest entries. `at_reference_budget`: the same at
+    the smallest entries, while the 4-point stencil's O(h^4) truncation at this h left 2.6e-4
+    on the most nonlinear entry. `at_reference_budget`: the same at
     the reference's CFL iteration budget, where the forward steps stop at the cap before
     converging and the gradient is not the truncated forward map's."""
-    out = _grads_at(args, dev, args.arms, max_iter=args.grad_iters, eps=1e-13, h=5e-2, stencil=4)
+    out = _grads_at(args, dev, args.arms, max_iter=args.grad_iters, eps=1e-13, h=5e-2, stencil=6)
     out["at_reference_budget"] = _grads_at(args, dev, args.arms, warm=False)
     return out
 
@@ -689,8 +695,9 @@ def run_ours(args, rank, world):
     peaks, src = _peaks()
     hbm = float(peaks.get("hbm_gbs", HBM_FALLBACK_GBS))
     achieved = launch_bytes / (launch_ms / 1e3) / 1e9
-    tps, tshape = TRAFFIC_PER_SCENE_ITER[args.precision]
-    traffic = float(tps * np.sum(it_l))
+    tshape = f"{head_nt}x{head_bps}"
+    tps = TRAFFIC_PER_SCENE_ITER.get((args.precision, tshape))
+    traffic = float(tps * np.sum(it_l)) if tps is not None else None
     rec = {
         "metric": "batched scene-steps/s (implicit PNCG step)",
         "value": value, "unit": "scene-steps/s", "n_gpus": world, "steps": args.steps,
@@ -716,8 +723,9 @@ def run_ours(args, rank, world):
         "e2e": {"value": e2e, "unit": "scene-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_source": src,
-                     "traffic_source": f"ncu capture of 608 scenes ({tshape} launch shape), scaled by "
-                                       f"scene-iterations ({int(np.sum(it_l))} in this launch)",
+                     "traffic_source": (f"ncu capture of 608 scenes ({tshape} launch shape), scaled by "
+                                        f"scene-iterations ({int(np.sum(it_l))} in this launch)")
+                                       if traffic is not None else f"no ncu capture at the {tshape} launch shape",
                      "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": launch_ms},
         "cpu_baseline": {"value": cpu_val, "unit": "scene-steps/s", "cores": threads, "kind": "port",
                          "sample": cpu_desc},
