@@ -439,22 +439,24 @@ def measure_contact_batch(args, dev):
 def measure_large_scene(args, dev):
     """The large-scene workload: a 256 x 1024-pixel slab (0.5 mm pixels, E 1 MPa, nu 0.40) with
     200 holes and 32 affine discs dropped onto it, dt 1e-3, one scene and a batch of 8, mixed
-    precision on a thread-block cluster per scene (the library's default for such batches).
-    Scene-steps/s from CUDA events over `large_steps` steps after one warm-up step; the
-    position error of the first step (from rest) against the FP64 path on the same scene (the
-    FP64 path runs a block per scene)."""
+    precision on a thread-block cluster per scene (the library's default for such batches),
+    and the single scene again with every SM on it (`B1_all_sms`, blocks_per_scene =
+    D2F_ALL_SMS). Scene-steps/s from CUDA events over `large_steps` steps after one warm-up
+    step; the position error of the first step (from rest) against the FP64 path on the same
+    scene (the FP64 path runs a block per scene), and the all-SM first step against the
+    cluster's."""
     import warnings
     import torch
     from diff_2d_fem_gb300 import workloads, scene, ImplicitIntegrator
     from diff_2d_fem_gb300.device import DeviceSolver
     out = {}
     stream = torch.cuda.current_stream(dev)
-    for B in (1, 8):
+    for B, bps in ((1, 0), (8, 0), (1, -1)):
         with warnings.catch_warnings():
             warnings.simplefilter("ignore")
             m, kw, dt = workloads.slab_with_holes(B, seed=0)
             prob = scene.solver_problem(m, ImplicitIntegrator(**kw), dt)
-        s = DeviceSolver(prob, precision="mixed")
+        s = DeviceSolver(prob, precision="mixed", blocks_per_scene=bps)
         blocks, threads, cs = s.launch_shape()
         s.step()
         x1 = s.get_x()
@@ -473,7 +475,14 @@ def measure_large_scene(args, dev):
                "boundary_nodes": int(len(prob["bnd"])), "iter_max": int(prob["iter_max"]),
                "iters_mean": float(np.mean(it)), "status_ok": bool((st == 0).all()),
                "launch": {"blocks": blocks, "threads": threads, "blocks_per_scene": cs}}
+        if bps == -1:  # every SM on the scene (D2F_ALL_SMS), against the default cluster
+            rec["first_step_vs_cluster_rel_to_coords"] = float(np.abs(x1 - x1_cluster).max() / np.abs(x1_cluster).max())
+            del s
+            torch.cuda.empty_cache()
+            out["B1_all_sms"] = rec
+            continue
         if B == 1:
+            x1_cluster = x1
             s64 = DeviceSolver(prob, precision="fp64")
             t64 = time.perf_counter()
             s64.step()

@@ -15,7 +15,7 @@ _P = C.c_void_p
 
 D2F_ABI_VERSION = 7
 D2F_FP64, D2F_MIXED = 0, 1
-ERRORS = {0: "ok", -1: "D2F_EINVAL", -2: "D2F_ECUDA", -3: "D2F_ECAP", -4: "D2F_ENAN"}
+ERRORS = {0: "ok", -1: "D2F_EINVAL", -2: "D2F_ECUDA", -3: "D2F_ECAP", -4: "D2F_ENAN", -5: "D2F_ESPIN"}
 
 
 class Seg(C.Structure):

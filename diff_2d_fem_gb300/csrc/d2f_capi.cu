@@ -98,9 +98,9 @@ static int validate(const d2f_scene_desc &d, bool scratch) {
     if (d.n_pe < 0 || d.n_ch < 0 || (d.n_pe > 0 && (d.n_ch <= 0 || !d.pe_a || !d.pe_b || !d.pe_ch || !d.ch_p || !d.ch_ref)))
         return fail(D2F_EINVAL, "d2f: pressure arrays missing");
     if (d.blocks_per_scene != 0 && d.blocks_per_scene != 1 && d.blocks_per_scene != 8 && d.blocks_per_scene != 12 &&
-        d.blocks_per_scene != 16)
-        return fail(D2F_EINVAL, "d2f: blocks_per_scene must be 0, 1, 8, 12 or 16");
-    if (d.blocks_per_scene > 1 && d.precision != D2F_MIXED)
+        d.blocks_per_scene != 16 && d.blocks_per_scene != D2F_ALL_SMS)
+        return fail(D2F_EINVAL, "d2f: blocks_per_scene must be 0, 1, 8, 12, 16 or D2F_ALL_SMS (-1)");
+    if ((d.blocks_per_scene > 1 || d.blocks_per_scene == D2F_ALL_SMS) && d.precision != D2F_MIXED)
         return fail(D2F_EINVAL, "d2f: several blocks per scene run in mixed precision only");
     return D2F_OK;
 }
@@ -112,8 +112,13 @@ static int validate(const d2f_scene_desc &d, bool scratch) {
 // scene's time on 16 / 12 / 8 blocks as 1 / 1.15 / 1.3 (measured on a 0.26M-node slab) and
 // counting the waves of scenes the clusters that fit at once need.
 static int blocks_per_scene(const d2f_scene_desc &d, int nsm, int smem) {
-    const int want = d.blocks_per_scene;
+    int want = d.blocks_per_scene;
     if (want == 1) return 1;
+    if (want == D2F_ALL_SMS) {  // every SM on one scene, when the device and the scratch allow it
+        if (nsm <= d2f::grid_max_blocks() && d2f::grid_blocks_mixed(smem) >= nsm)
+            return D2F_ALL_SMS;
+        want = 0;  // else the library's choice
+    }
     if (want == 0 && (d.precision != D2F_MIXED || d.n_scenes >= nsm || d.N / d.n_scenes < 16384)) return 1;
     const int sizes[3] = {16, 12, 8}, cost[3] = {100, 115, 130};
     int best = 1;
@@ -137,6 +142,10 @@ static int launch_shape(const d2f_scene_desc &d, int *grid, int *smem, int *cs) 
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return fail(D2F_ECUDA, "d2f: no CUDA device");
     *cs = blocks_per_scene(d, nsm, *smem);
+    if (*cs == D2F_ALL_SMS) {  // one block per SM, all on one scene at a time
+        *grid = nsm;
+        return D2F_OK;
+    }
     if (*cs > 1) {  // persistent clusters, one scene each at a time
         int nc = d2f::max_clusters_mixed(*cs, *smem);
         if (nc > d.n_scenes) nc = d.n_scenes;
@@ -153,6 +162,7 @@ static int launch_shape(const d2f_scene_desc &d, int *grid, int *smem, int *cs) 
 }
 
 static cudaError_t launch(const d2f_scene_desc &d, int grid, int smem, int cs, cudaStream_t st) {
+    if (cs == D2F_ALL_SMS) return d2f::launch_mixed_grid(d, grid, smem, st);
     if (cs > 1) return d2f::launch_mixed_cluster(cs, d, grid, smem, st);
     int vnt, vminb;
     pick_variant(d2f_default_threads(d), d.blocks_per_sm, &vnt, &vminb);
@@ -244,7 +254,7 @@ int32_t d2f_launch_shape(const d2f_solver *s, int32_t *blocks, int32_t *threads,
         if (s->cs == 1) pick_variant(d2f_default_threads(s->d), s->d.blocks_per_sm, &vnt, &vminb);
         *threads = vnt;
     }
-    if (blocks_per_scene) *blocks_per_scene = s->cs;
+    if (blocks_per_scene) *blocks_per_scene = s->cs == D2F_ALL_SMS ? s->grid : s->cs;
     return D2F_OK;
 }
 

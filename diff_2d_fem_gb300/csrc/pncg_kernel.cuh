@@ -1427,4 +1427,9 @@ constexpr int kClusterThreads = 512;
 // that fit on the device at once (0: that cluster size cannot be launched)
 cudaError_t launch_mixed_cluster(int cs, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st);
 int max_clusters_mixed(int cs, int smem);
+// every SM on one scene (pncg_mixed_cluster.cu): a cooperative launch of `grid` blocks of
+// kClusterThreads, one per SM; grid_blocks_mixed = the blocks that can be co-resident
+cudaError_t launch_mixed_grid(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st);
+int grid_blocks_mixed(int smem);
+int grid_max_blocks();
 }  // namespace d2f

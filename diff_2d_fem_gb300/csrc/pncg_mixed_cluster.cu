@@ -1,7 +1,8 @@
-// pncg_mixed_cluster.cu — the mixed-precision step kernel with one thread-block cluster per
-// scene (pncg_mixed_kernel.cuh, CS > 1), for large scenes: one block cannot keep a scene of
-// 10^5 nodes moving, while a cluster of 8, 12 or 16 blocks on as many SMs splits every phase and
-// combines its reductions through distributed shared memory.
+// pncg_mixed_cluster.cu — the mixed-precision step kernel with several blocks per scene, for
+// large scenes: one block cannot keep a scene of 10^5 nodes moving, while a thread-block cluster
+// of 8, 12 or 16 blocks on as many SMs (pncg_mixed_kernel.cuh, CS > 1) splits every phase and
+// combines its reductions through distributed shared memory, and the all-SM mode (CS == 0)
+// spreads one scene over one block per SM, exchanging through global memory.
 #include "pncg_mixed_kernel.cuh"
 
 namespace d2f {
@@ -60,6 +61,46 @@ int max_clusters_c(int smem) {
     return n;
 }
 }  // namespace
+
+// Every SM on one scene: a cooperative launch (all blocks co-resident, which the grid barrier
+// needs) of one kClusterThreads block per SM. The blocks exchange through their part of the
+// mixed scratch, whose barrier header starts at zero.
+cudaError_t launch_mixed_grid(const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
+    if (grid > GX_MAX_BLOCKS) return cudaErrorInvalidConfiguration;
+    auto k = pncg_mixed_kernel<kClusterThreads, 1, 0>;
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+    }
+    MixedPtrs mp = mixed_ptrs(d);
+    cudaError_t e = cudaMemsetAsync(mp.gx, 0, 256, st);
+    if (e != cudaSuccess) return e;
+    d2f_scene_desc dd = d;
+    void *args[2] = {&dd, &mp};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(k), dim3((unsigned)grid), dim3(kClusterThreads),
+                                       args, (size_t)smem, st);
+}
+
+int grid_blocks_mixed(int smem) {
+    int dev = 0, coop = 0, nsm = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || !coop) {
+        cudaGetLastError();
+        return 0;
+    }
+    auto k = pncg_mixed_kernel<kClusterThreads, 1, 0>;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kClusterThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return per_sm * nsm;
+}
+
+int grid_max_blocks() { return GX_MAX_BLOCKS; }
 
 cudaError_t launch_mixed_cluster(int cs, const d2f_scene_desc &d, int grid, int smem, cudaStream_t st) {
     if (cs == 16) return launch_c<16>(d, grid, smem, st);

@@ -127,15 +127,111 @@ __device__ __forceinline__ void block_reduce_mx(FF (&s)[NS], float (&m)[NM], con
     // first barrier, which every thread reaches after reading this call's results
 }
 
+// ---------------------------------------------------------------------- every SM on one scene
+// The grid mode (CS == 0): all blocks of one cooperative launch, one per SM, work on one scene
+// at a time. Blocks exchange through global memory, a part of the mixed step's scratch: a
+// barrier header, then per block a reduction slot (two alternating buffers), a list-count slot
+// and an ordered list of the candidates below the running cap (GX_REL of them: a block with
+// more sends the replay to its full walk, as a cluster block past REL_CAP does).
+// the multi-block paths' ACCD replay: candidates below the running cap, per block
+constexpr int REL_CAP = 512;
+constexpr int GX_RED = 20;          // doubles per block per reduction buffer
+constexpr int GX_REL = 64;          // ordered candidates per block
+constexpr int GX_MAX_BLOCKS = 256;  // blocks (SMs) the exchange is sized for
+struct GridX {
+    unsigned *count, *gen;
+    int *err;
+    double *red;   // [2][nb][GX_RED]
+    int *cnt;      // [nb]
+    int *nrel;     // [nb]
+    int *rel;      // [nb][GX_REL]
+    int nb, parity;
+};
+__host__ __device__ inline size_t grid_exchange_bytes(int nb) {
+    return 256 + (size_t)2 * nb * GX_RED * sizeof(double) + (size_t)nb * (2 + GX_REL) * sizeof(int);
+}
+__device__ inline GridX grid_exchange(void *base, int nb) {
+    unsigned char *b = static_cast<unsigned char *>(base);
+    GridX g;
+    g.count = reinterpret_cast<unsigned *>(b);
+    g.gen = reinterpret_cast<unsigned *>(b) + 1;
+    g.err = reinterpret_cast<int *>(b) + 2;
+    g.red = reinterpret_cast<double *>(b + 256);
+    g.cnt = reinterpret_cast<int *>(g.red + (size_t)2 * nb * GX_RED);
+    g.nrel = g.cnt + nb;
+    g.rel = g.nrel + nb;
+    g.nb = nb;
+    g.parity = 0;
+    return g;
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Every block of the launch (co-resident: a cooperative launch). Thread 0 of each block
+// arrives on a counter; the last one resets it and advances the generation the others wait
+// for. The wait is bounded (2 s): past it the block sets the shared error flag and every later
+// barrier returns at once, so a fault in the protocol ends the kernel with an error status
+// instead of hanging the device.
+static __device__ __noinline__ void grid_barrier(GridX &g) {
+    block_barrier();
+    if (threadIdx.x == 0 && !*reinterpret_cast<volatile int *>(g.err)) {
+        const unsigned gen0 = ld_acquire_u32(g.gen);
+        __threadfence();
+        if (atomicAdd(g.count, 1u) == (unsigned)g.nb - 1u) {
+            atomicExch(g.count, 0u);
+            __threadfence();
+            atomicAdd(g.gen, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (ld_acquire_u32(g.gen) == gen0) {
+                if (*reinterpret_cast<volatile int *>(g.err)) break;
+                if (global_ns() - t0 > 2000000000ull) {
+                    atomicExch(g.err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    block_barrier();
+}
+
 // Reductions over the thread group working on one scene. CS == 1: the block reduction. A
 // cluster of CS blocks on one scene (large scenes): the block reduction, then the CS block
 // results combined in rank order through distributed shared memory, so every block of the
 // cluster holds the same, deterministic result. `cres` / `cmres`: per-block scratch.
 template <int NT, int CS, int NV>
-__device__ __forceinline__ void scene_reduce(double (&v)[NV], const int (&ops)[NV], double *red, double *cres) {
+__device__ __forceinline__ void scene_reduce(double (&v)[NV], const int (&ops)[NV], double *red, double *cres,
+                                             GridX *gx = nullptr) {
     static_assert(NV <= 20, "red / cres of the step kernel");
     block_reduce<NT, NV>(v, ops, red);
-    if constexpr (CS > 1) {
+    if constexpr (CS == 0) {  // every block's result through global memory, combined in block order
+        constexpr int NW = NT / 32;
+        double *buf = gx->red + (size_t)gx->parity * gx->nb * GX_RED;
+        gx->parity ^= 1;  // the next reduction writes the other buffer: no barrier after the reads
+        if (threadIdx.x < NV) buf[(size_t)blockIdx.x * GX_RED + threadIdx.x] = red[NW * NV + threadIdx.x];
+        grid_barrier(*gx);
+        if (threadIdx.x < NV) {
+            const int k = threadIdx.x;
+            double a = buf[k];
+            for (int r = 1; r < gx->nb; ++r) {
+                const double b = buf[(size_t)r * GX_RED + k];
+                a = ops[k] == 0 ? a + b : (ops[k] == 1 ? dmax(a, b) : dmin(a, b));
+            }
+            cres[k] = a;
+        }
+        block_barrier();
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = cres[k];
+    } else if constexpr (CS > 1) {
         namespace cg = cooperative_groups;
         cg::cluster_group cl = cg::this_cluster();
         constexpr int NW = NT / 32;
@@ -159,9 +255,36 @@ __device__ __forceinline__ void scene_reduce(double (&v)[NV], const int (&ops)[N
 template <int NT, int CS, int NS, int NM>
 __device__ __forceinline__ void scene_reduce_mx(FF (&s)[NS], float (&m)[NM], const int (&mops)[NM],
                                                 double (&out_s)[NS], float (&out_m)[NM], float *fred,
-                                                double *dres, float *mres, double *cres, float *cmres) {
+                                                double *dres, float *mres, double *cres, float *cmres,
+                                                GridX *gx = nullptr) {
     block_reduce_mx<NT, NS, NM>(s, m, mops, out_s, out_m, fred, dres, mres);
-    if constexpr (CS > 1) {
+    if constexpr (CS == 0) {  // every block's sums and extrema through global memory, in block order
+        static_assert(NS + NM <= GX_RED, "grid reduction slot");
+        double *buf = gx->red + (size_t)gx->parity * gx->nb * GX_RED;
+        gx->parity ^= 1;
+        const int k = threadIdx.x;
+        if (k < NS) buf[(size_t)blockIdx.x * GX_RED + k] = dres[k];
+        else if (k < NS + NM) buf[(size_t)blockIdx.x * GX_RED + k] = (double)mres[k - NS];
+        grid_barrier(*gx);
+        if (k < NS) {
+            double a = 0.0;
+            for (int r = 0; r < gx->nb; ++r) a += buf[(size_t)r * GX_RED + k];
+            cres[k] = a;
+        } else if (k < NS + NM) {
+            const int j = k - NS;
+            float a = (float)buf[k];
+            for (int r = 1; r < gx->nb; ++r) {
+                const float b = (float)buf[(size_t)r * GX_RED + k];
+                a = mops[j] == 1 ? fmaxf(a, b) : mops[j] == 2 ? fminf(a, b) : a + b;
+            }
+            cmres[j] = a;
+        }
+        block_barrier();
+#pragma unroll
+        for (int q = 0; q < NS; ++q) out_s[q] = cres[q];
+#pragma unroll
+        for (int q = 0; q < NM; ++q) out_m[q] = cmres[q];
+    } else if constexpr (CS > 1) {
         namespace cg = cooperative_groups;
         cg::cluster_group cl = cg::this_cluster();
         cluster_barrier();
@@ -189,7 +312,7 @@ __device__ __forceinline__ void scene_reduce_mx(FF (&s)[NS], float (&m)[NM], con
 
 // Byte layout of the mixed path's per-step scratch (d2f_scene_desc.mscr), 256-aligned parts.
 struct MixedLayout {
-    size_t xd, hvm, g0, gd, xbd, xr, db, rarm, ninfo, du0, phi0, rcs, pb, total;
+    size_t xd, hvm, g0, gd, xbd, xr, db, rarm, ninfo, du0, phi0, rcs, pb, gx, total;
 };
 __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, long n_col, long n_rig) {
     auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -208,6 +331,7 @@ __host__ __device__ inline MixedLayout mixed_layout(long N, long T, long Nb, lon
     L.phi0 = o; o = up(o + (size_t)N * (n_col > 0 ? n_col : 1) * 4);
     L.rcs = o; o = up(o + (size_t)(n_rig > 0 ? n_rig : 1) * 8);
     L.pb = o; o = up(o + (size_t)(Nb > 0 ? Nb : 1) * 8);
+    L.gx = o; o = up(o + grid_exchange_bytes(GX_MAX_BLOCKS));  // the all-SM mode's block exchange
     L.total = o;
     return L;
 }
@@ -238,8 +362,6 @@ constexpr int NI_AFF = 4, NI_RIG = 8;
 // contact candidate lists of scenes with at least HASH_MIN_NB boundary nodes on a cluster are
 // built through a spatial hash of HASH_B buckets (every other scene tests all edge-node pairs)
 constexpr int HASH_MIN_NB = 4096, HASH_B = 4096;
-// the cluster path's ACCD replay: candidates below the running cap, per block
-constexpr int REL_CAP = 512;
 // the hash (HASH_B bucket ends + the slots, 4 bytes each) reuses the 8 bytes per boundary node
 // of dynamic shared memory the exhaustive build holds its positions in
 static_assert(HASH_MIN_NB >= HASH_B, "hash tables must fit the boundary-position buffer");
@@ -319,6 +441,7 @@ struct MixedPtrs {
     double2 *g0d, *xbd;
     int2 *ninfo;
     float *phi0;
+    unsigned char *gx;
 };
 inline MixedPtrs mixed_ptrs(const d2f_scene_desc &d) {
     const MixedLayout L = mixed_layout(d.N, d.T, d.Nb, d.n_col, d.n_rig);
@@ -338,6 +461,7 @@ inline MixedPtrs mixed_ptrs(const d2f_scene_desc &d) {
     p.xbd = reinterpret_cast<double2 *>(ms + L.xbd);
     p.ninfo = reinterpret_cast<int2 *>(ms + L.ninfo);
     p.phi0 = reinterpret_cast<float *>(ms + L.phi0);
+    p.gx = ms + L.gx;
     return p;
 }
 
@@ -400,8 +524,11 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                                                               const __grid_constant__ MixedPtrs mp) {
     namespace cg = cooperative_groups;
     constexpr int NW = NT / 32;
-    constexpr bool CL = CS > 1;
-    constexpr int GS = CS * NT;  // threads working on one scene
+    constexpr bool GR = CS == 0;   // every block of the launch on one scene (cooperative launch)
+    constexpr bool CLU = CS > 1;   // a thread-block cluster on one scene
+    constexpr bool CL = CS != 1;   // several blocks on one scene (either form)
+    const int NBS = GR ? (int)gridDim.x : CS;  // blocks working on one scene
+    const int GS = NBS * NT;                   // threads working on one scene
     __shared__ SceneSh S;
     __shared__ SceneF F;
     __shared__ Col cols[MAX_COL];
@@ -424,10 +551,17 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
     extern __shared__ float2 pos32[];
 
     const int tid = threadIdx.x;
-    const int crank = CL ? (int)cg::this_cluster().block_rank() : 0;
+    int crank = 0;
+    if constexpr (GR) crank = (int)blockIdx.x;
+    else if constexpr (CLU) crank = (int)cg::this_cluster().block_rank();
     const int gt = crank * NT + tid;  // this thread's index among the scene's threads
+    GridX gxv{};
+    if constexpr (GR) gxv = grid_exchange(mp.gx, (int)gridDim.x);
+    GridX *const gxp = GR ? &gxv : nullptr;
     auto gsync = [&]() {              // a phase barrier of the scene's thread group
-        if constexpr (CL) cluster_barrier(); else block_barrier();
+        if constexpr (GR) grid_barrier(gxv);
+        else if constexpr (CLU) cluster_barrier();
+        else block_barrier();
     };
     const double dt = d.dt, h2 = dt * dt, inv_dt = 1.0 / dt;
     const double dhat = d.dhat;
@@ -484,10 +618,12 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
         colf[tid][1] = (float)c[4];
     }
 
-    for (;;) {
-        if (tid == 0 && crank == 0) sc_next = atomicAdd(d.work, 1);
+    for (int sc_seq = 0;; ++sc_seq) {
+        if (!GR && tid == 0 && crank == 0) sc_next = atomicAdd(d.work, 1);
         int sc;
-        if constexpr (CL) {  // rank 0 takes the next scene; the cluster reads it from rank 0
+        if constexpr (GR) {  // the whole grid on each scene in turn
+            sc = sc_seq;
+        } else if constexpr (CL) {  // rank 0 takes the next scene; the cluster reads it from rank 0
             cg::cluster_group cl = cg::this_cluster();
             cluster_barrier();
             sc = *cl.map_shared_rank(&sc_next, 0);
@@ -690,7 +826,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 c[0] += m * xi.x; c[1] += m * xi.y; c[2] += m;
             }
             const int ops3[3] = {0, 0, 0};
-            scene_reduce<NT, CS, 3>(c, ops3, red, cres);
+            scene_reduce<NT, CS, 3>(c, ops3, red, cres, gxp);
             const double cx = c[0] / c[2], cy = c[1] / c[2];
             for (int k = sg.rign0 + gt; k < sg.rign0 + sg.nrign; k += GS) {
                 if (d.r_grp[k] != b) continue;
@@ -760,14 +896,26 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     if (tid == 0) s_cnt = 0;
                     block_barrier();
                     if ((tid & 31) == 0 && mine) atomicAdd(&s_cnt, mine);
-                    cg::cluster_group cl = cg::this_cluster();
-                    cluster_barrier();
-                    for (int r = 0; r < CS; ++r) {
-                        const int c = *cl.map_shared_rank(&s_cnt, r);
-                        if (r < crank) base_off += c;
-                        n_all += c;
+                    if constexpr (GR) {  // the counts through global memory
+                        block_barrier();
+                        if (tid == 0) gxv.cnt[crank] = s_cnt;
+                        grid_barrier(gxv);
+                        for (int r = 0; r < NBS; ++r) {
+                            const int c = *reinterpret_cast<volatile int *>(gxv.cnt + r);
+                            if (r < crank) base_off += c;
+                            n_all += c;
+                        }
+                        grid_barrier(gxv);  // every read done before the counts are reused
+                    } else {
+                        cg::cluster_group cl = cg::this_cluster();
+                        cluster_barrier();
+                        for (int r = 0; r < CS; ++r) {
+                            const int c = *cl.map_shared_rank(&s_cnt, r);
+                            if (r < crank) base_off += c;
+                            n_all += c;
+                        }
+                        cluster_barrier();
                     }
-                    cluster_barrier();
                 }
             };
             if (hashed) {
@@ -853,7 +1001,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     return n;
                 };
                 // this block's contiguous share of the edges (all of them for a block per scene)
-                const int echunk = (sg.ne + CS - 1) / CS;
+                const int echunk = (sg.ne + NBS - 1) / NBS;
                 const int e0 = CL ? min(crank * echunk, sg.ne) : 0;
                 const int e1 = CL ? min(e0 + echunk, sg.ne) : sg.ne;
                 if constexpr (CL) {  // pass 1: count
@@ -888,7 +1036,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             } else {
                 const long npair = (long)sg.ne * nbl;
                 // this block's contiguous share of the pair space (all of it for a block per scene)
-                const long chunk = (npair + CS - 1) / CS;
+                const long chunk = (npair + NBS - 1) / NBS;
                 const long q0 = CL ? (crank * chunk < npair ? crank * chunk : npair) : 0;
                 const long q1 = CL ? (q0 + chunk < npair ? q0 + chunk : npair) : npair;
                 block_barrier();  // pos32 complete
@@ -932,7 +1080,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             block_barrier();
             double vm[1] = {(double)dmn};
             const int opm[1] = {2};
-            scene_reduce<NT, CS, 1>(vm, opm, red, cres);
+            scene_reduce<NT, CS, 1>(vm, opm, red, cres, gxp);
             if (tid == 0) {
                 const int cnt = CL ? n_all : S.count;
                 if (cnt > sg.ncap) { S.status = D2F_ECAP; S.ncand = sg.ncap; }
@@ -1252,7 +1400,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 // each block filters its contiguous share of the candidates into an ordered list
                 // in shared memory; thread 0 of every block walks the lists in rank order
                 // (distributed shared memory): the same pairs in the same order as the full walk
-                const int cchunk = (nc + CS - 1) / CS;
+                const int cchunk = (nc + NBS - 1) / NBS;
                 const int c0 = min(crank * cchunk, nc), c1 = min(c0 + cchunk, nc);
                 if (tid == 0) s_nrel = 0;
                 block_barrier();
@@ -1272,27 +1420,51 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     block_barrier();
                     if (tid == 0) s_nrel += tot;
                 }
-                cg::cluster_group cl = cg::this_cluster();
-                cluster_barrier();
                 bool over = false;  // a list that did not fit: the full walk below, every block
-                for (int r = 0; r < CS; ++r) over |= *cl.map_shared_rank(&s_nrel, r) > REL_CAP;
                 double m = m0;
-                if (!over && tid == 0) {
-                    double t_c = m0;
-                    int prevk = -1;
-                    for (int r = 0; r < CS; ++r) {
-                        const int n = *cl.map_shared_rank(&s_nrel, r);
-                        const int *lst = cl.map_shared_rank(s_rel, r);
-                        for (int i = 0; i < n; ++i) {
-                            const int cc = lst[i];
-                            const int k = (int)((unsigned)d.cand[sg.cand0 + cc] >> 16);
-                            const double2 pr = Ctr[sg.cand0 + cc];
-                            if (k != prevk) { t_c = m; prevk = k; }
-                            m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+                if constexpr (GR) {  // the lists through global memory
+                    block_barrier();
+                    if (tid == 0) gxv.nrel[crank] = s_nrel;
+                    for (int i = tid; i < s_nrel && i < GX_REL; i += NT) gxv.rel[(size_t)crank * GX_REL + i] = s_rel[i];
+                    grid_barrier(gxv);
+                    for (int r = 0; r < NBS; ++r) over |= *reinterpret_cast<volatile int *>(gxv.nrel + r) > GX_REL;
+                    if (!over && tid == 0) {
+                        double t_c = m0;
+                        int prevk = -1;
+                        for (int r = 0; r < NBS; ++r) {
+                            const int n = *reinterpret_cast<volatile int *>(gxv.nrel + r);
+                            const volatile int *lst = gxv.rel + (size_t)r * GX_REL;
+                            for (int i = 0; i < n; ++i) {
+                                const int cc = lst[i];
+                                const int k = (int)((unsigned)d.cand[sg.cand0 + cc] >> 16);
+                                const double2 pr = Ctr[sg.cand0 + cc];
+                                if (k != prevk) { t_c = m; prevk = k; }
+                                m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+                            }
                         }
                     }
+                    grid_barrier(gxv);  // every read done before the lists are rebuilt
+                } else {
+                    cg::cluster_group cl = cg::this_cluster();
+                    cluster_barrier();
+                    for (int r = 0; r < CS; ++r) over |= *cl.map_shared_rank(&s_nrel, r) > REL_CAP;
+                    if (!over && tid == 0) {
+                        double t_c = m0;
+                        int prevk = -1;
+                        for (int r = 0; r < CS; ++r) {
+                            const int n = *cl.map_shared_rank(&s_nrel, r);
+                            const int *lst = cl.map_shared_rank(s_rel, r);
+                            for (int i = 0; i < n; ++i) {
+                                const int cc = lst[i];
+                                const int k = (int)((unsigned)d.cand[sg.cand0 + cc] >> 16);
+                                const double2 pr = Ctr[sg.cand0 + cc];
+                                if (k != prevk) { t_c = m; prevk = k; }
+                                m = dmin(m, t_c <= pr.x ? t_c : pr.y);
+                            }
+                        }
+                    }
+                    cluster_barrier();  // every remote read done before the lists are rebuilt
                 }
-                cluster_barrier();  // every remote read done before the lists are rebuilt
                 if (!over) return m;
             }
             double m = m0, t_c = m0;
@@ -1331,7 +1503,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
             ipc_pairs(3, dummy, 1.0);
             double v[1] = {qi};
             const int ops[1] = {1};
-            scene_reduce<NT, CS, 1>(v, ops, red, cres);
+            scene_reduce<NT, CS, 1>(v, ops, red, cres, gxp);
             const double a_tc = tc_scan(1.0);
             if (tid == 0) {
                 double a_s = a_tc;
@@ -1366,7 +1538,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 },
                 Bm, Ar, Mu, La, cols, colmu, [&](double &acc) { if (scene_ipc) ipc_pairs(2, acc, 0.0); })};
             const int ops[1] = {0};
-            scene_reduce<NT, CS, 1>(v, ops, red, cres);
+            scene_reduce<NT, CS, 1>(v, ops, red, cres, gxp);
             return v[0];
         };
 
@@ -1385,6 +1557,12 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     if (it % 8 == 7) S.pending = !(S.alpha_s >= 1.0);
                 }
                 gsync();
+            }
+            if constexpr (GR) {  // a grid barrier gave up waiting: end the step with an error
+                if (*reinterpret_cast<volatile int *>(gxv.err)) {
+                    if (tid == 0) S.status = D2F_ESPIN;
+                    break;
+                }
             }
             if (!S.active && !S.pending) break;
             if (S.status != 0) break;
@@ -1563,7 +1741,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         L[0] += sqrt(ex * ex + ey * ey);
                     }
                     const int ops1[1] = {0};
-                    scene_reduce<NT, CS, 1>(L, ops1, red, cres);
+                    scene_reduce<NT, CS, 1>(L, ops1, red, cres, gxp);
                     if (gt == 0) tendon_state(sg.ten0, L[0]);
                 } else {
                     for (int k = sg.ten0 + gt; k < sg.ten0 + sg.nten; k += GS) {
@@ -1708,7 +1886,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int nmo[1] = {1};
                 double so[2];
                 float mo_[1];
-                scene_reduce_mx<NT, CS, 2, 1>(cs2, nm, nmo, so, mo_, fred, dres, mres, cres, cmres);
+                scene_reduce_mx<NT, CS, 2, 1>(cs2, nm, nmo, so, mo_, fred, dres, mres, cres, cmres, gxp);
                 const float Mtot = (float)d.r_acc[3 * b + 2];
                 const float csx = (float)so[0] / Mtot, csy = (float)so[1] / Mtot;
                 FF v[11];
@@ -1728,7 +1906,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                     ff_add(v[10], dx * ry * ry + dy * rx * rx);
                 }
                 double vs[11];
-                scene_reduce_mx<NT, CS, 11, 1>(v, nm, nmo, vs, mo_, fred, dres, mres, cres, cmres);
+                scene_reduce_mx<NT, CS, 11, 1>(v, nm, nmo, vs, mo_, fred, dres, mres, cres, cmres, gxp);
                 if (tid == 0) {
                     float v32[11];
                     for (int q = 0; q < 11; ++q) v32[q] = (float)vs[q];
@@ -1750,7 +1928,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                         affine_solve(d.a_q, d.a_Mu, d.a_La, d.a_gq, d.a_gq_prev, d.a_H, d.a_pq, d.a_zq, h2, sg.aff0 + gt,
                                      sg.aff0 + sg.naff, GS, ab);
                         const int ops5[5] = {0, 0, 0, 0, 0};
-                        scene_reduce<NT, CS, 5>(ab, ops5, red, cres);
+                        scene_reduce<NT, CS, 5>(ab, ops5, red, cres, gxp);
                     }
                 } else if (tid == 0) {  // the batch kernel: thread 0, inline, 6x6 work in shared memory
                     for (int b = sg.aff0; b < sg.aff0 + sg.naff; ++b) {
@@ -1846,7 +2024,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 }
                 double vs[NS];
                 float mo_[NM];
-                scene_reduce_mx<NT, CS, NS, NM>(v, r, rops, vs, mo_, fred, dres, mres, cres, cmres);
+                scene_reduce_mx<NT, CS, NS, NM>(v, r, rops, vs, mo_, fred, dres, mres, cres, cmres, gxp);
                 if constexpr (RIG) {
                     if (tid == 0) {  // rigid_reduce_kernel, affine.py:456-473
                         rigid_precondition(mo_ + 1, F, nullptr, s_zf[0]);
@@ -2103,7 +2281,7 @@ __global__ void __launch_bounds__(NT, MINB) pncg_mixed_kernel(const __grid_const
                 const int mops[3] = {1, 2, 2};
                 double so[3];
                 float mo[3];
-                scene_reduce_mx<NT, CS, 3, 3>(sv, mv, mops, so, mo, fred, dres, mres, cres, cmres);
+                scene_reduce_mx<NT, CS, 3, 3>(sv, mv, mops, so, mo, fred, dres, mres, cres, cmres, gxp);
                 const double a_ccd = scene_ipc ? tc_scan(d.alpha_max) : 0.0;
                 // ---------------------------------------------- B5: step length and convergence
                 // (alpha_finalize_kernel, kernels.py:374-423): the step length and the

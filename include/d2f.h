@@ -33,6 +33,11 @@ extern "C" {
 #define D2F_ECUDA (-2)    /* a CUDA call failed */
 #define D2F_ECAP (-3)     /* a scene's contact candidate list overflowed its capacity */
 #define D2F_ENAN (-4)     /* a scene produced a non-finite step length */
+#define D2F_ESPIN (-5)    /* a grid-wide barrier of the all-SM mode waited past its limit (2 s) */
+
+/* blocks_per_scene: every SM on one scene at a time (a cooperative launch of one block per SM;
+ * mixed precision; scenes taken in turn) */
+#define D2F_ALL_SMS (-1)
 
 /* precision modes */
 #define D2F_FP64 0        /* every operation in FP64, as the reference runs */
@@ -142,7 +147,9 @@ typedef struct d2f_scene_desc {
                                     cluster of 512-thread blocks: 1, 8, 12 or 16 (0: a cluster of
                                     16, 12 or 8, whichever finishes the batch first, when the
                                     batch has fewer scenes than SMs and at least 16384 nodes per
-                                    scene; else 1) */
+                                    scene; else 1), or D2F_ALL_SMS: one 512-thread block per SM,
+                                    all on one scene at a time (a cooperative launch; the library's
+                                    choice where the device cannot co-schedule them) */
     const int32_t *a_ptr;        /* n_aff + 1: affine body b owns entries a_ptr[b] .. a_ptr[b+1]-1 of
                                     a_node / a_grp / a_w (required with affine bodies) */
     /* springs and pins (Springs, implicit/actuation.py:381-476): E = k/2 (|x_a - x_b| - L0)^2,
