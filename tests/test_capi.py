@@ -89,6 +89,8 @@ def _valid_desc():
 @pytest.mark.parametrize("field,value,needle", [
     ("blocks_per_scene", 5, b"blocks_per_scene"),
     ("blocks_per_scene", 16, b"mixed precision only"),
+    ("blocks_per_scene", -1, b"mixed precision only"),     # D2F_ALL_SMS, every SM on one scene
+    ("blocks_per_scene", -2, b"D2F_ALL_SMS"),
     ("n_sp", 1, b"spring"),
     ("n_pe", 4, b"pressure"),
     ("threads", 96, b"threads"),
