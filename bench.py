@@ -565,7 +565,7 @@ def run_ours(args, rank, world):
             warnings.simplefilter("ignore")
             m, kw, dt = workloads.slab_with_holes(args.profile_large, seed=0)
             prob = scene.solver_problem(m, ImplicitIntegrator(**kw), dt)
-        sol = DeviceSolver(prob, precision="mixed")
+        sol = DeviceSolver(prob, precision="mixed", blocks_per_scene=args.profile_bps)
         for _ in range(args.warmup + args.steps):
             sol.step()
         torch.cuda.synchronize(dev)
@@ -777,6 +777,8 @@ def main():
     ap.add_argument("--no-contact", action="store_true", help="skip the contact-heavy measurement")
     ap.add_argument("--profile-large", type=int, default=0,
                     help="run only the large-scene step (this many slabs), for profilers")
+    ap.add_argument("--profile-bps", type=int, default=0,
+                    help="with --profile-large: blocks per scene (0 library default, -1 every SM)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only warmup + steps of the step kernel (for ncu)")
     args = ap.parse_args()
